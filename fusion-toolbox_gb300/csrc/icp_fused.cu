@@ -1,0 +1,686 @@
+// Fused Gauss-Newton ICP for one frame pair (ICPOdometry.estimate,
+// slamtb/registration/icp.py:152-262) without host synchronisation.
+//
+// Per iteration, two kernels:
+//   k_assoc  -- one thread per source point: transform, project, gate
+//               (bounds, target mask, distance, normal angle) and a 64-bit
+//               atomicMin of (epoch tag, distance bits, source index) into a
+//               per-pixel key map.  The epoch tag makes entries of earlier
+//               iterations read as empty, so the map is cleared once per
+//               call instead of once per iteration (the reference refills a
+//               fresh int64 map per term and iteration,
+//               slamtb/registration/correspondence_map.py:66-70).
+//   k_reduce -- one thread per TARGET pixel: the pixel's winner (if any)
+//               gives the source index; point-to-plane and feature residuals
+//               and Jacobians are formed and the 30 unique normal-equation
+//               terms are summed with compensated float32 (TwoSum) through
+//               warp shuffles, a per-block partial and a last-block-done
+//               ticket.  The last block finishes the sum in FP64, solves the
+//               6x6 system, applies the SE(3) update and writes the float32
+//               pose view for the next iteration.  This replaces the
+//               per-point partials + three torch.sum(0) + host solve of the
+//               reference (icp.py:39-82, 216-256).
+// After the loop one more association at the final pose feeds k_info, the
+// information matrix sum of G^T G (icp_jacobian_geometric.cu:118-158).
+#include <math.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "gn_solve.cuh"
+#include "stb_common.cuh"
+#include "stb_host.hpp"
+
+namespace stb {
+
+float distance_thresh_sq(double d);
+float angle_cos_max(double angle);
+
+namespace {
+
+constexpr int kAccs = 30;      // 21 JtJ (upper) + 6 Jr + r2 + count_geom + count_feat
+constexpr int kInfoAccs = 21;  // GtG upper triangle
+constexpr int kAssocThreads = 256;
+constexpr int kReduceThreads = 256;
+constexpr int kPixelsPerThread = 4;
+constexpr int kMaxReduceBlocks = 152 * 8;
+constexpr unsigned long long kMaxSources = 1ull << 24;
+
+// Accumulator slots.
+constexpr int kJr = 21, kR2 = 27, kCountGeom = 28, kCountFeat = 29;
+
+struct State {
+  double T[16];  // current pose, FP64
+  Pose32 pose;   // its float32 view + intrinsics
+  unsigned ticket;
+  unsigned stopped;
+  unsigned status;
+  int iters_done;
+};
+
+struct Job {
+  const float *kcam;
+  const float *sp, *sn;
+  const uint8_t *sm;
+  long long n;
+  const void *sf;
+  const float *tp, *tn;
+  const uint8_t *tm;
+  int H, W;
+  const void *tf;
+  int C, dtype;
+  const double *init;
+  int iters, channel_mode;
+  int use_geom, use_feat;
+  float wg1, wg2, wf1, wf2;
+  float thr2, cos_max, feat_thr2;
+  double *result, *history;
+  unsigned long long *keys;
+  float *part_s, *part_c;
+  int nblocks;
+  State *state;
+};
+
+constexpr size_t kSlot = 1024;
+
+__host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+inline int reduce_blocks(int64_t pixels) {
+  const int64_t per_block = (int64_t)kReduceThreads * kPixelsPerThread;
+  int64_t b = (pixels + per_block - 1) / per_block;
+  if (b < 1) b = 1;
+  if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
+  return (int)b;
+}
+
+// Workspace: [Job slot][State slot][partials s, c: kAccs x nblocks][keys H*W]
+inline size_t workspace_bytes(int64_t pixels) {
+  const int nb = reduce_blocks(pixels);
+  return 2 * kSlot + 2 * align256(sizeof(float) * kAccs * nb) +
+         align256(sizeof(unsigned long long) * pixels);
+}
+
+__device__ __forceinline__ unsigned tag_of(int epoch) { return 254u - (unsigned)epoch; }
+
+__device__ __forceinline__ void load_shared_pose(Pose32 &P, const State *S) {
+  const float *src = reinterpret_cast<const float *>(&S->pose);
+  float *dst = reinterpret_cast<float *>(&P);
+  for (int k = threadIdx.x; k < (int)(sizeof(Pose32) / sizeof(float)); k += blockDim.x)
+    dst[k] = src[k];
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_begin(Job job, Job *dst) {
+  if (threadIdx.x != 0) return;
+  *dst = job;
+  State *S = job.state;
+  for (int k = 0; k < 16; ++k)
+    S->T[k] = job.init ? job.init[k] : ((k % 5) == 0 ? 1.0 : 0.0);
+  S->pose.fx = job.kcam[0];
+  S->pose.cx = job.kcam[2];
+  S->pose.fy = job.kcam[4];
+  S->pose.cy = job.kcam[5];
+  refresh_pose32(S->pose, S->T);
+  S->ticket = 0;
+  S->stopped = 0;
+  S->status = 0;
+  S->iters_done = 0;
+  for (int k = 0; k < STB_RES_SIZE; ++k) job.result[k] = 0.0;
+  job.result[STB_RES_RESIDUAL] = INFINITY;
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kAssocThreads) k_assoc(const Job *__restrict__ J,
+                                                         int epoch, int force) {
+  __shared__ Pose32 P;
+  __shared__ int skip;
+  const State *S = J->state;
+  if (threadIdx.x == 0) skip = !force && S->stopped;
+  load_shared_pose(P, S);
+  __syncthreads();
+  if (skip) return;
+  const long long n = J->n;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float *__restrict__ sp = J->sp;
+  if (!J->sm[i]) return;
+  const int H = J->H, W = J->W;
+  const float3 Tp = transform_point(P.rt, sp[3 * i], sp[3 * i + 1], sp[3 * i + 2]);
+  float u, v;
+  project(P, Tp, u, v);
+  int ui, vi;
+  if (!round_in(u, W, ui) || !round_in(v, H, vi)) return;
+  const int64_t pix = (int64_t)vi * W + ui;
+  if (!J->tm[pix]) return;
+  const float *__restrict__ tp = J->tp;
+  const float dx = fsub(tp[3 * pix], Tp.x), dy = fsub(tp[3 * pix + 1], Tp.y),
+              dz = fsub(tp[3 * pix + 2], Tp.z);
+  const float sq = dot3(dx, dy, dz, dx, dy, dz);
+  if (sq > J->thr2) return;
+  const float *__restrict__ sn = J->sn;
+  const float *__restrict__ tn = J->tn;
+  const float3 Tn = transform_normal(P.nm, sn[3 * i], sn[3 * i + 1], sn[3 * i + 2]);
+  const float nx = tn[3 * pix], ny = tn[3 * pix + 1], nz = tn[3 * pix + 2];
+  const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, nx, ny, nz),
+                       fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
+                            __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz))));
+  if (c >= -1.0f && c <= J->cos_max) return;
+  const float dist = __fsqrt_rn(sq);
+  const unsigned long long key = ((unsigned long long)tag_of(epoch) << 56) |
+                                 ((unsigned long long)__float_as_uint(dist) << 24) |
+                                 (unsigned long long)i;
+  atomicMin(J->keys + pix, key);
+}
+
+// ---------------------------------------------------------------------------
+// Feature sampling shared with the compat kernel's arithmetic
+// (BilinearInterp, feature_map.hpp:15-41).
+template <typename T>
+__device__ __forceinline__ float bilinear(const T *__restrict__ f, int H, int W, float u,
+                                          float v) {
+  const int ui = (int)u, vi = (int)v;
+  const float ur = fsub(u, (float)ui), vr = fsub(v, (float)vi);
+  const float v00 = load_feat(f + (int64_t)vi * W + ui);
+  const float v10 = (ui + 1 < W) ? load_feat(f + (int64_t)vi * W + ui + 1) : 0.f;
+  const float v01 = (vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui) : 0.f;
+  const float v11 =
+      (ui + 1 < W && vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui + 1) : 0.f;
+  const float a0 = fadd(fmul(v00, fsub(1.f, ur)), fmul(v10, ur));
+  const float a1 = fadd(fmul(v01, fsub(1.f, ur)), fmul(v11, ur));
+  return fadd(fmul(a0, fsub(1.f, vr)), fmul(a1, vr));
+}
+
+__device__ __forceinline__ void accumulate_se3(CSum *acc, const float *Jv, float r,
+                                               float w1, float w2) {
+#pragma unroll
+  for (int a = 0; a < 6; ++a)
+#pragma unroll
+    for (int b = a; b < 6; ++b) csum_add(acc[upper_index(a, b)], w2 * (Jv[a] * Jv[b]));
+#pragma unroll
+  for (int a = 0; a < 6; ++a) csum_add(acc[kJr + a], w1 * (Jv[a] * r));
+}
+
+// Block-level compensated reduction of `nacc` accumulators; thread 0..nacc-1
+// of the block end with the block totals in out_s / out_c (shared).
+template <int kN>
+__device__ __forceinline__ void block_reduce(CSum *acc, float (*ws)[kN][2], float *out_s,
+                                             float *out_c) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < kN; ++a) {
+    csum_warp_reduce(acc[a]);
+    if (lane == 0) {
+      ws[warp][a][0] = acc[a].s;
+      ws[warp][a][1] = acc[a].c;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < kN) {
+    CSum t = {0.f, 0.f};
+    const int nw = blockDim.x >> 5;
+    for (int w = 0; w < nw; ++w) csum_merge(t, ws[w][threadIdx.x][0], ws[w][threadIdx.x][1]);
+    out_s[threadIdx.x] = t.s;
+    out_c[threadIdx.x] = t.c;
+  }
+}
+
+// Last block: FP64 totals of kN accumulators from all block partials.
+template <int kN>
+__device__ __forceinline__ void grid_totals(const float *part_s, const float *part_c,
+                                            int nblocks, double *tot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+  for (int a = warp; a < kN; a += nw) {
+    CSum t = {0.f, 0.f};
+    for (int b = lane; b < nblocks; b += 32)
+      csum_merge(t, __ldcg(part_s + a * nblocks + b), __ldcg(part_c + a * nblocks + b));
+    csum_warp_reduce(t);
+    if (lane == 0) tot[a] = (double)t.s + (double)t.c;
+  }
+}
+
+// One Gauss-Newton step from the FP64 totals (single thread).
+__device__ void gn_step(const Job *J, const double *tot, int iter) {
+  State *S = J->state;
+  double A[36], b[6], x[6];
+#pragma unroll
+  for (int a = 0; a < 6; ++a)
+#pragma unroll
+    for (int c = a; c < 6; ++c) A[a * 6 + c] = A[c * 6 + a] = tot[upper_index(a, c)];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) b[a] = tot[kJr + a];
+  const double r2 = tot[kR2];
+  const double cg = tot[kCountGeom], cf = tot[kCountFeat];
+  const double count = J->use_geom ? fmax(cg, cf) : cf;
+  double *H = J->history ? J->history + (size_t)iter * STB_HIST_SIZE : nullptr;
+  if (H) {
+    for (int k = 0; k < 36; ++k) H[STB_HIST_JTJ + k] = A[k];
+    for (int k = 0; k < 6; ++k) H[STB_HIST_JR + k] = b[k];
+    H[STB_HIST_R2] = r2;
+    H[STB_HIST_GEOM_COUNT] = cg;
+    H[STB_HIST_FEAT_COUNT] = cf;
+  }
+  if (count == 0.0) S->status |= STB_ST_NO_MATCHES;
+  if (!cholesky_solve6(A, b, x)) {
+    S->stopped = 1;
+    S->status |= STB_ST_NOT_PD;
+    J->result[STB_RES_STATUS] = (double)S->status;
+    if (H) H[STB_HIST_OK] = 0.0;
+    return;
+  }
+  bool finite = true;
+  for (int k = 0; k < 6; ++k) finite &= isfinite(x[k]);
+  if (!finite) S->status |= STB_ST_NAN;
+  double E[16], Tn[16];
+  se3_exp(x, E);
+  compose(E, S->T, Tn);
+  for (int k = 0; k < 16; ++k) S->T[k] = Tn[k];
+  refresh_pose32(S->pose, Tn);
+  S->iters_done += 1;
+  double *R = J->result;
+  for (int k = 0; k < 16; ++k) R[STB_RES_TRANSFORM + k] = Tn[k];
+  for (int k = 0; k < 36; ++k) R[STB_RES_JTJ + k] = A[k];
+  R[STB_RES_RESIDUAL] = r2 / count;
+  R[STB_RES_MATCHES] = count;
+  R[STB_RES_ITERS] = (double)S->iters_done;
+  R[STB_RES_STATUS] = (double)S->status;
+  if (H) {
+    for (int k = 0; k < 16; ++k) H[STB_HIST_TRANSFORM + k] = Tn[k];
+    H[STB_HIST_OK] = 1.0;
+  }
+}
+
+template <typename FT, bool kGeom, bool kFeat>
+__global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict__ J,
+                                                           int epoch) {
+  __shared__ Pose32 P;
+  __shared__ int skip;
+  __shared__ float ws[kReduceThreads / 32][kAccs][2];
+  __shared__ float bs[kAccs], bc[kAccs];
+  __shared__ int is_last;
+  __shared__ double tot[kAccs];
+  State *S = J->state;
+  if (threadIdx.x == 0) skip = S->stopped;
+  load_shared_pose(P, S);
+  __syncthreads();
+  if (skip) return;
+
+  CSum acc[kAccs];
+#pragma unroll
+  for (int a = 0; a < kAccs; ++a) acc[a] = {0.f, 0.f};
+
+  const int H = J->H, W = J->W;
+  const int64_t npix = (int64_t)H * W;
+  const unsigned tag = tag_of(epoch);
+  const unsigned long long *__restrict__ keys = J->keys;
+  const float *__restrict__ sp = J->sp;
+  const float *__restrict__ tp = J->tp;
+  const float *__restrict__ tn = J->tn;
+  const float wg1 = J->wg1, wg2 = J->wg2, wf1 = J->wf1, wf2 = J->wf2;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t pix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pix < npix;
+       pix += stride) {
+    const unsigned long long key = keys[pix];
+    if ((unsigned)(key >> 56) != tag) continue;
+    const int64_t i = (int64_t)(key & 0xffffffull);
+    const float3 Tp = transform_point(P.rt, sp[3 * i], sp[3 * i + 1], sp[3 * i + 2]);
+    if (kGeom) {
+      // r = (q - Tp).n, J = [n; Tp x n] (icp_jacobian_geometric.cu:82,
+      // icp_jacobian_common.hpp:41-48)
+      const float nx = tn[3 * pix], ny = tn[3 * pix + 1], nz = tn[3 * pix + 2];
+      const float r = dot3(fsub(tp[3 * pix], Tp.x), fsub(tp[3 * pix + 1], Tp.y),
+                           fsub(tp[3 * pix + 2], Tp.z), nx, ny, nz);
+      const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
+                           fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
+                           fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
+      accumulate_se3(acc, Jv, r, wg1, wg2);
+      csum_add(acc[kR2], wg1 * (r * r));
+      csum_add(acc[kCountGeom], 1.f);
+    }
+    if (kFeat) {
+      // FeatureJacobianKernel (icp_jacobian_feature.cu:65-108): the gate
+      // sum_c r_c^2 > thresh^2 is decided on the reference's float32 values.
+      const FT *__restrict__ tf = static_cast<const FT *>(J->tf);
+      const FT *__restrict__ sf = static_cast<const FT *>(J->sf);
+      const int C = J->C;
+      const long long n = J->n;
+      const int64_t plane = npix;
+      float u, v;
+      project(P, Tp, u, v);
+      float sq = 0.f;
+      for (int c = 0; c < C; ++c) {
+        const float r = fsub(bilinear(tf + c * plane, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+        sq = fadd(sq, fmul(r, r));
+      }
+      if (!(sq > J->feat_thr2)) {
+        const float h = 0.05f;
+        const float div = fdiv(1.f, fmul(2.f, h));
+        const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
+        const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
+        const float zz = fmul(Tp.z, Tp.z);
+        const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
+        const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
+        const int c0 = (J->channel_mode == 0) ? C - 1 : 0;
+        for (int c = c0; c < C; ++c) {
+          const FT *fc = tf + c * plane;
+          const float r = fsub(bilinear(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+          const float du = fmul(fsub(bilinear(fc, H, W, uu0, v), bilinear(fc, H, W, uu1, v)), div);
+          const float dv = fmul(fsub(bilinear(fc, H, W, u, vv0), bilinear(fc, H, W, u, vv1)), div);
+          const float gx = fmul(du, j00), gy = fmul(dv, j11),
+                      gz = fadd(fmul(du, j02), fmul(dv, j12));
+          const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
+                               fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
+                               fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
+          // J^T r enters with -w_f (icp.py:222)
+          accumulate_se3(acc, Jv, r, -wf1, wf2);
+        }
+        csum_add(acc[kR2], wf1 * sq);
+        csum_add(acc[kCountFeat], 1.f);
+      }
+    }
+  }
+
+  block_reduce<kAccs>(acc, ws, bs, bc);
+  const int nb = gridDim.x;
+  if (threadIdx.x < kAccs) {
+    J->part_s[threadIdx.x * nb + blockIdx.x] = bs[threadIdx.x];
+    J->part_c[threadIdx.x * nb + blockIdx.x] = bc[threadIdx.x];
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(&S->ticket, 1u) == (unsigned)nb - 1);
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  grid_totals<kAccs>(J->part_s, J->part_c, nb, tot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S->ticket = 0;
+    gn_step(J, tot, epoch);
+  }
+}
+
+// Information matrix: sum over winners of G^T G with G from the target point
+// (icp_jacobian_geometric.cu:141-151), summed as icp.py:108.
+__global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__ J,
+                                                         int epoch) {
+  __shared__ float ws[kReduceThreads / 32][kInfoAccs][2];
+  __shared__ float bs[kInfoAccs], bc[kInfoAccs];
+  __shared__ int is_last;
+  __shared__ double tot[kInfoAccs];
+  State *S = J->state;
+  CSum acc[kInfoAccs];
+#pragma unroll
+  for (int a = 0; a < kInfoAccs; ++a) acc[a] = {0.f, 0.f};
+  const int64_t npix = (int64_t)J->H * J->W;
+  const unsigned tag = tag_of(epoch);
+  const unsigned long long *__restrict__ keys = J->keys;
+  const float *__restrict__ tp = J->tp;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t pix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pix < npix;
+       pix += stride) {
+    if ((unsigned)(keys[pix] >> 56) != tag) continue;
+    const float qx = tp[3 * pix], qy = tp[3 * pix + 1], qz = tp[3 * pix + 2];
+    const float G0[6] = {0.f, qz, -qy, 1.f, 0.f, 0.f};
+    const float G1[6] = {-qz, 0.f, qx, 0.f, 1.f, 0.f};
+    const float G2[6] = {qy, -qx, 0.f, 0.f, 0.f, 1.f};
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+      for (int b = a; b < 6; ++b)
+        csum_add(acc[upper_index(a, b)], G0[a] * G0[b] + G1[a] * G1[b] + G2[a] * G2[b]);
+  }
+  block_reduce<kInfoAccs>(acc, ws, bs, bc);
+  const int nb = gridDim.x;
+  if (threadIdx.x < kInfoAccs) {
+    J->part_s[threadIdx.x * nb + blockIdx.x] = bs[threadIdx.x];
+    J->part_c[threadIdx.x * nb + blockIdx.x] = bc[threadIdx.x];
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = (atomicAdd(&S->ticket, 1u) == (unsigned)nb - 1);
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  grid_totals<kInfoAccs>(J->part_s, J->part_c, nb, tot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    S->ticket = 0;
+    double *R = J->result;
+    for (int a = 0; a < 6; ++a)
+      for (int b = a; b < 6; ++b)
+        R[STB_RES_INFO + a * 6 + b] = R[STB_RES_INFO + b * 6 + a] = tot[upper_index(a, b)];
+    R[STB_RES_STATUS] = (double)S->status;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launch sequence and CUDA-graph cache
+// ---------------------------------------------------------------------------
+struct Plan {
+  int64_t n;
+  int H, W, C, dtype, iters, use_geom, use_feat, channel_mode, nblocks;
+  Job *job_dev;
+  unsigned long long *keys;
+};
+
+using ReduceFn = void (*)(const Job *, int);
+
+ReduceFn pick_reduce(const Plan &p) {
+  if (!p.use_feat) return k_reduce<float, true, false>;
+  if (p.dtype == STB_F32)
+    return p.use_geom ? k_reduce<float, true, true> : k_reduce<float, false, true>;
+  return p.use_geom ? k_reduce<__nv_bfloat16, true, true>
+                    : k_reduce<__nv_bfloat16, false, true>;
+}
+
+// Everything after k_begin; k_begin itself is launched by the caller so that
+// a captured graph can take new Job parameters per call.
+int launch_body(const Plan &p, cudaStream_t st) {
+  const unsigned agrid = blocks_for(p.n, kAssocThreads);
+  const ReduceFn red = pick_reduce(p);
+  for (int it = 0; it < p.iters; ++it) {
+    if (p.n > 0) k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, it, 0);
+    red<<<p.nblocks, kReduceThreads, 0, st>>>(p.job_dev, it);
+  }
+  if (p.n > 0) k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, p.iters, 1);
+  k_info<<<p.nblocks, kReduceThreads, 0, st>>>(p.job_dev, p.iters);
+  return check_launch("stb_icp_estimate");
+}
+
+struct GraphEntry {
+  cudaGraph_t graph = nullptr;  // kept alive: its node handle updates the exec
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphNode_t begin_node = nullptr;
+  cudaKernelNodeParams begin_params{};
+};
+
+using GraphKey = std::tuple<void *, int64_t, int, int, int, int, int, int, int, int, bool>;
+std::mutex g_graph_mutex;
+std::map<GraphKey, GraphEntry> g_graphs;
+
+int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st) {
+  std::lock_guard<std::mutex> lock(g_graph_mutex);
+  const GraphKey key{(void *)p.job_dev, p.n, p.H, p.W, p.C, p.dtype, p.iters,
+                     p.use_geom, p.use_feat, p.channel_mode, with_history};
+  auto it = g_graphs.find(key);
+  Job job_copy = job;
+  Job *dst = p.job_dev;
+  void *args[] = {&job_copy, &dst};
+  if (it == g_graphs.end()) {
+    cudaStream_t cap;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess)
+      return check_launch("cudaStreamCreate");
+    cudaGraph_t graph;
+    cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    cudaMemsetAsync(p.keys, 0xff, sizeof(unsigned long long) * (size_t)p.H * p.W, cap);
+    k_begin<<<1, 32, 0, cap>>>(job_copy, dst);
+    launch_body(p, cap);
+    const cudaError_t cerr = cudaStreamEndCapture(cap, &graph);
+    cudaStreamDestroy(cap);
+    if (cerr != cudaSuccess)
+      return fail(STB_ECUDA, "Cuda call error stb_icp_estimate (graph capture): %s",
+                  cudaGetErrorString(cerr));
+    GraphEntry e;
+    // locate k_begin's node to update its parameters on later calls
+    size_t count = 0;
+    cudaGraphGetNodes(graph, nullptr, &count);
+    cudaGraphNode_t *nodes = new cudaGraphNode_t[count];
+    cudaGraphGetNodes(graph, nodes, &count);
+    for (size_t k = 0; k < count; ++k) {
+      cudaGraphNodeType type;
+      cudaGraphNodeGetType(nodes[k], &type);
+      if (type != cudaGraphNodeTypeKernel) continue;
+      cudaKernelNodeParams kp;
+      cudaGraphKernelNodeGetParams(nodes[k], &kp);
+      if (kp.func == (void *)k_begin) {
+        e.begin_node = nodes[k];
+        e.begin_params = kp;
+      }
+    }
+    delete[] nodes;
+    const cudaError_t ierr = cudaGraphInstantiate(&e.exec, graph, 0);
+    if (ierr != cudaSuccess || !e.begin_node) {
+      cudaGraphDestroy(graph);
+      return fail(STB_ECUDA, "Cuda call error stb_icp_estimate (graph instantiate): %s",
+                  cudaGetErrorString(ierr));
+    }
+    e.graph = graph;
+    it = g_graphs.emplace(key, e).first;
+  }
+  GraphEntry &e = it->second;
+  cudaKernelNodeParams kp = e.begin_params;
+  kp.kernelParams = args;
+  kp.extra = nullptr;
+  if (cudaGraphExecKernelNodeSetParams(e.exec, e.begin_node, &kp) != cudaSuccess)
+    return check_launch("cudaGraphExecKernelNodeSetParams");
+  if (cudaGraphLaunch(e.exec, st) != cudaSuccess) return check_launch("cudaGraphLaunch");
+  return STB_OK;
+}
+
+}  // namespace
+}  // namespace stb
+
+using namespace stb;
+
+extern "C" size_t stb_icp_workspace_bytes(int64_t num_source, int32_t height,
+                                          int32_t width) {
+  (void)num_source;
+  return workspace_bytes((int64_t)height * width);
+}
+
+extern "C" int stb_icp_estimate(
+    const float *kcam, const float *src_points, const float *src_normals,
+    const uint8_t *src_mask, int64_t num_source, const void *src_feats,
+    const float *tgt_points, const float *tgt_normals, const uint8_t *tgt_mask,
+    int32_t height, int32_t width, const void *tgt_feats, int32_t channels,
+    int32_t feat_dtype, const double *init_transform, int32_t num_iters,
+    double geom_weight, double feat_weight, double distance_thresh,
+    double normal_angle_thresh, double feat_residual_thresh, int32_t channel_mode,
+    void *workspace, size_t workspace_bytes_, double *result, double *history,
+    int32_t use_graph, void *stream) {
+  clear_error();
+  if (num_source < 0 || (unsigned long long)num_source >= kMaxSources)
+    return fail(STB_EINVAL, "Check failed: num_source must be in [0, 2^24), got %lld",
+                (long long)num_source);
+  if (height <= 0 || width <= 0)
+    return fail(STB_EINVAL, "Check failed: target size must be positive, got %dx%d",
+                height, width);
+  if (num_iters < 0 || num_iters > 254)
+    return fail(STB_EINVAL, "Check failed: num_iters must be in [0, 254], got %d", num_iters);
+  const int64_t npix = (int64_t)height * width;
+  if (workspace_bytes_ < workspace_bytes(npix))
+    return fail(STB_EINVAL, "Check failed: workspace of %zu bytes, %zu needed",
+                workspace_bytes_, workspace_bytes(npix));
+  if (((uintptr_t)workspace & 255) != 0)
+    return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
+  const bool use_feat = feat_weight > 0.0 && src_feats && tgt_feats;
+  const bool use_geom = geom_weight > 0.0;
+  if (use_feat) {
+    if (channels <= 0)
+      return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
+    if (feat_dtype != STB_F32 && feat_dtype != STB_BF16)
+      return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
+    if (channel_mode != 0 && channel_mode != 1)
+      return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
+  }
+  STB_TRY(check_device_ptr(kcam, "kcam"));
+  STB_TRY(check_device_ptr(src_points, "src_points"));
+  STB_TRY(check_device_ptr(src_normals, "src_normals"));
+  STB_TRY(check_device_ptr(src_mask, "src_mask"));
+  STB_TRY(check_device_ptr(tgt_points, "tgt_points"));
+  STB_TRY(check_device_ptr(tgt_normals, "tgt_normals"));
+  STB_TRY(check_device_ptr(tgt_mask, "tgt_mask"));
+  if (use_feat) {
+    STB_TRY(check_device_ptr(src_feats, "src_feats"));
+    STB_TRY(check_device_ptr(tgt_feats, "tgt_feats"));
+  }
+  STB_TRY(check_device_ptr(init_transform, "transform", true));
+  STB_TRY(check_device_ptr(workspace, "workspace"));
+  STB_TRY(check_device_ptr(result, "result"));
+  STB_TRY(check_device_ptr(history, "history", true));
+
+  char *ws = static_cast<char *>(workspace);
+  Plan p;
+  p.n = num_source;
+  p.H = height;
+  p.W = width;
+  p.C = use_feat ? channels : 0;
+  p.dtype = use_feat ? feat_dtype : 0;
+  p.iters = num_iters;
+  p.use_geom = use_geom;
+  p.use_feat = use_feat;
+  p.channel_mode = use_feat ? channel_mode : 0;
+  p.nblocks = reduce_blocks(npix);
+  p.job_dev = reinterpret_cast<Job *>(ws);
+
+  Job job;
+  job.kcam = kcam;
+  job.sp = src_points;
+  job.sn = src_normals;
+  job.sm = src_mask;
+  job.n = num_source;
+  job.sf = src_feats;
+  job.tp = tgt_points;
+  job.tn = tgt_normals;
+  job.tm = tgt_mask;
+  job.H = height;
+  job.W = width;
+  job.tf = tgt_feats;
+  job.C = p.C;
+  job.dtype = p.dtype;
+  job.init = init_transform;
+  job.iters = num_iters;
+  job.channel_mode = p.channel_mode;
+  job.use_geom = use_geom;
+  job.use_feat = use_feat;
+  job.wg1 = (float)geom_weight;
+  job.wg2 = (float)(geom_weight * geom_weight);
+  job.wf1 = (float)feat_weight;
+  job.wf2 = (float)(feat_weight * feat_weight);
+  job.thr2 = distance_thresh_sq(distance_thresh);
+  job.cos_max = angle_cos_max(normal_angle_thresh);
+  {
+    const float t = (float)feat_residual_thresh;  // a float in the reference
+    job.feat_thr2 = t * t;
+  }
+  job.result = result;
+  job.history = history;
+  size_t off = 2 * kSlot;
+  job.state = reinterpret_cast<State *>(ws + kSlot);
+  job.part_s = reinterpret_cast<float *>(ws + off);
+  off += align256(sizeof(float) * kAccs * p.nblocks);
+  job.part_c = reinterpret_cast<float *>(ws + off);
+  off += align256(sizeof(float) * kAccs * p.nblocks);
+  job.keys = reinterpret_cast<unsigned long long *>(ws + off);
+  job.nblocks = p.nblocks;
+  p.keys = job.keys;
+  static_assert(sizeof(Job) <= kSlot && sizeof(State) <= kSlot, "workspace slots");
+
+  const cudaStream_t st = as_stream(stream);
+  if (use_graph) return run_graph(p, job, history != nullptr, st);
+  cudaMemsetAsync(p.keys, 0xff, sizeof(unsigned long long) * (size_t)npix, st);
+  k_begin<<<1, 32, 0, st>>>(job, p.job_dev);
+  return launch_body(p, st);
+}

@@ -1,0 +1,55 @@
+// Error state and argument checks of the C ABI.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include "stb_host.hpp"
+
+namespace stb {
+
+static thread_local char g_message[512];
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_message, sizeof(g_message), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+void clear_error() { g_message[0] = '\0'; }
+
+int check_device_ptr(const void *p, const char *name, bool allow_null) {
+  if (p == nullptr) {
+    if (allow_null) return STB_OK;
+    return fail(STB_EINVAL, "Check failed: %s: null pointer", name);
+  }
+  cudaPointerAttributes attr;
+  const cudaError_t err = cudaPointerGetAttributes(&attr, p);
+  if (err != cudaSuccess) {
+    cudaGetLastError();
+    return fail(STB_EDEVICE, "Check failed: %s: Expected a gpu tensor (%s)", name,
+                cudaGetErrorString(err));
+  }
+  if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+    return fail(STB_EDEVICE, "Check failed: %s: Expected a gpu tensor", name);
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (attr.device != dev)
+    return fail(STB_EDEVICE,
+                "Check failed: %s: Expected a tensor on cuda:%d, got cuda:%d", name,
+                dev, attr.device);
+  return STB_OK;
+}
+
+int check_launch(const char *what) {
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess)
+    return fail(STB_ECUDA, "Cuda call error %s: %s", what, cudaGetErrorString(err));
+  return STB_OK;
+}
+
+}  // namespace stb
+
+extern "C" const char *stb_last_error(void) { return stb::g_message; }
+
+extern "C" const char *stb_version(void) { return "slamtb_gb300 0.1 (sm_103a)"; }

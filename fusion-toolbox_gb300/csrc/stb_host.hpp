@@ -1,0 +1,38 @@
+// Host-side helpers shared by the C-ABI translation units: the per-thread
+// error message, argument checks and launch checks.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "slamtb_gb300.h"
+
+namespace stb {
+
+// Records a printf-style message for stb_last_error() and returns `code`.
+int fail(int code, const char *fmt, ...);
+
+// Clears the message (start of every entry point).
+void clear_error();
+
+// STB_EDEVICE unless `p` is device (or managed) memory of the current device.
+// Messages keep the reference's wording: "Check failed: <where>: Expected a
+// gpu tensor" (include/slamtb/error.hpp:12-37).
+int check_device_ptr(const void *p, const char *name, bool allow_null = false);
+
+// STB_ECUDA with the CUDA error string if the last launch failed.
+int check_launch(const char *what);
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned blocks_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+}  // namespace stb
+
+#define STB_TRY(expr)            \
+  do {                           \
+    const int _rc = (expr);      \
+    if (_rc != STB_OK) return _rc; \
+  } while (0)

@@ -1,0 +1,104 @@
+"""Frame preparation on the device (``slamtb/processing.py`` subset used by
+the ICP path), backed by the ``stb_*`` prep kernels of libslamtb_gb300."""
+import torch
+
+from . import _native as N
+
+
+def _dev(t):
+    if not t.is_cuda:
+        raise RuntimeError("Check failed: Expected a gpu tensor "
+                           "(slamtb_gb300 runs on CUDA devices only)")
+    return t.device
+
+
+def _run(dev, fn, *args):
+    with torch.cuda.device(dev):
+        N.check(fn(*args, N.stream_of(dev)))
+
+
+def depth_to_points(depth, kcam, depth_scale=1.0, depth_bias=0.0):
+    """(H, W) depth -> ((H, W, 3) float32 points, (H, W) bool depth > 0)."""
+    dev = _dev(depth)
+    depth = depth.to(torch.float32).contiguous()
+    k = kcam.to(device=dev, dtype=torch.float32).contiguous()
+    h, w = depth.shape
+    pts = torch.empty(h, w, 3, dtype=torch.float32, device=dev)
+    mask = torch.empty(h, w, dtype=torch.bool, device=dev)
+    _run(dev, N.lib().stb_depth_to_points, N.ptr(depth), float(depth_scale),
+         float(depth_bias), N.ptr(k), N.ptr(pts), N.ptr(mask), h, w)
+    return pts, mask
+
+
+def erode_mask(mask):
+    dev = _dev(mask)
+    m = mask.to(torch.bool).contiguous()
+    out = torch.empty_like(m)
+    _run(dev, N.lib().stb_erode_mask, N.ptr(m), N.ptr(out), m.size(0), m.size(1))
+    return out
+
+
+def estimate_normals(points, mask):
+    dev = _dev(points)
+    p = points.to(torch.float32).contiguous()
+    m = mask.to(torch.bool).contiguous()
+    out = torch.empty_like(p)
+    _run(dev, N.lib().stb_estimate_normals, N.ptr(p), N.ptr(m), N.ptr(out), p.size(0),
+         p.size(1))
+    return out
+
+
+def downsample_xyz(xyz, mask, scale):
+    dev = _dev(xyz)
+    x = xyz.to(torch.float32).contiguous()
+    m = mask.to(torch.bool).contiguous()
+    h, w = m.shape
+    dh, dw = int(h * scale), int(w * scale)
+    out = torch.empty(dh, dw, 3, dtype=torch.float32, device=dev)
+    _run(dev, N.lib().stb_downsample_xyz, N.ptr(x), N.ptr(m), h, w, float(scale), N.ptr(out),
+         dh, dw)
+    return out
+
+
+def downsample_mask(mask, scale):
+    dev = _dev(mask)
+    m = mask.to(torch.bool).contiguous()
+    h, w = m.shape
+    dh, dw = int(h * scale), int(w * scale)
+    out = torch.empty(dh, dw, dtype=torch.bool, device=dev)
+    _run(dev, N.lib().stb_downsample_mask, N.ptr(m), h, w, float(scale), N.ptr(out), dh, dw)
+    return out
+
+
+def downsample_features(feats, scale):
+    dev = _dev(feats)
+    f = feats.contiguous()
+    c, h, w = f.shape
+    dh, dw = int(h * scale), int(w * scale)
+    out = torch.empty(c, dh, dw, dtype=f.dtype, device=dev)
+    _run(dev, N.lib().stb_downsample_features, N.ptr(f), c, h, w, N.feat_dtype_code(f),
+         float(scale), N.ptr(out), dh, dw)
+    return out
+
+
+def gaussian_blur3(feats, sigma=0.849):
+    dev = _dev(feats)
+    f = feats.contiguous()
+    c, h, w = f.shape
+    out = torch.empty_like(f)
+    _run(dev, N.lib().stb_gaussian_blur3, N.ptr(f), c, h, w, N.feat_dtype_code(f),
+         float(sigma), N.ptr(out))
+    return out
+
+
+def feature_pyramid(feature_map, scales):
+    """Blur + 2x2 mean for every scale below 1, coarsest first
+    (``slamtb/processing.py:141-159``)."""
+    pyr = []
+    f = feature_map
+    for s in scales:
+        if s < 1.0:
+            f = downsample_features(gaussian_blur3(f), s)
+        pyr.append(f)
+    pyr.reverse()
+    return pyr

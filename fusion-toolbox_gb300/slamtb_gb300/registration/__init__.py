@@ -1,0 +1,10 @@
+"""Registration algorithms (``slamtb.registration`` drop-in)."""
+from .icp import ICPOdometry
+from .multiscale import MultiscaleRegistration, MultiscaleICPOdometry
+from .result import RegistrationResult, RegistrationVerifier
+from .correspondence_map import CorrespondenceMap
+from .preset import create_multiscale_odometry
+
+__all__ = ["ICPOdometry", "MultiscaleRegistration", "MultiscaleICPOdometry",
+           "RegistrationResult", "RegistrationVerifier", "CorrespondenceMap",
+           "create_multiscale_odometry"]

@@ -1,0 +1,203 @@
+"""Pose estimation via iterative closest points, GB300 path.
+
+Same interface as ``slamtb/registration/icp.py:111-310`` (``ICPOdometry``);
+the Gauss-Newton loop runs on the device as one call into
+``libslamtb_gb300`` (``stb_icp_estimate``), with one device-to-host copy of
+the result at the end instead of the reference's ~8 synchronisations per
+iteration.
+"""
+import math
+
+import torch
+
+from .. import _native as N
+from .result import RegistrationResult
+
+
+def _kcam_matrix(kcam, device):
+    m = kcam.matrix if hasattr(kcam, "matrix") else kcam
+    m = torch.as_tensor(m)
+    return m.to(device=device, dtype=torch.float32).contiguous()
+
+
+class _Workspace:
+    """Device scratch of ``stb_icp_estimate``, grown on demand and reused
+    across calls (one per estimator: concurrent calls on several streams
+    need several estimators)."""
+
+    def __init__(self):
+        self.buf = None
+        self.result = None
+        self.history = None
+
+    def get(self, device, num_source, height, width, num_iters, history):
+        need = int(N.lib().stb_icp_workspace_bytes(num_source, height, width))
+        if self.buf is None or self.buf.device != device or self.buf.numel() < need:
+            self.buf = torch.empty(need, dtype=torch.uint8, device=device)
+            self.result = torch.empty(N.RES_SIZE, dtype=torch.float64, device=device)
+        hist = None
+        if history:
+            if (self.history is None or self.history.device != device
+                    or self.history.size(0) < max(num_iters, 1)):
+                self.history = torch.empty(max(num_iters, 1), N.HIST_SIZE,
+                                           dtype=torch.float64, device=device)
+            hist = self.history
+        return self.buf, self.result, hist
+
+
+class ICPOdometry:
+    """Iterative closest points with the point-to-plane error and
+    Gauss-Newton optimisation (``slamtb/registration/icp.py:111-150``).
+
+    Args (as the reference):
+        num_iters (int): Gauss-Newton iterations (at most 254).
+        geom_weight (float): geometric term weight, 0 disables it.
+        feat_weight (float): feature term weight, 0 disables it.
+        so3 (bool): rotation-only optimisation; not supported (the
+            reference's rotation-only call is broken: ``icp.py:71-76``
+            passes 15 arguments to an 11-argument binding).
+        distance_threshold (float): maximum matching distance.
+        normals_angle_thresh (float): maximum normal angle (radians).
+        feat_residual_thresh (float): maximum feature residual norm.
+
+    Extra keyword arguments:
+        feat_channel_mode (str): "last" (reference behaviour: with several
+            feature channels only the last channel's Jacobian enters J^T J
+            and J^T r) or "sum" (all channels).
+        use_graph (bool): replay the launch sequence as a CUDA graph.
+        record_history (bool): keep per-iteration records in
+            ``self.last_history`` (float64 (num_iters, 64) CPU tensor, layout
+            ``STB_HIST_*`` of ``include/slamtb_gb300.h``).
+    """
+
+    def __init__(self, num_iters, geom_weight=1.0, feat_weight=1.0, so3=False,
+                 distance_threshold=.5, normals_angle_thresh=math.pi / 4,
+                 feat_residual_thresh=2.75, feat_channel_mode="last",
+                 use_graph=True, record_history=False):
+        if so3:
+            raise NotImplementedError(
+                "so3=True is not supported: the reference's rotation-only path "
+                "cannot run (icp.py:71-76 calls estimate_feature_so3 with 15 "
+                "arguments; the binding takes 11)")
+        if num_iters > 254:
+            raise ValueError("num_iters must be at most 254")
+        if feat_channel_mode not in ("last", "sum"):
+            raise ValueError("feat_channel_mode must be 'last' or 'sum'")
+        self.num_iters = num_iters
+        self.geom_weight = geom_weight
+        self.feat_weight = feat_weight
+        self.so3 = so3
+        self.distance_threshold = distance_threshold
+        self.normals_angle_thresh = normals_angle_thresh
+        self.feat_residual_thresh = feat_residual_thresh
+        self.feat_channel_mode = feat_channel_mode
+        self.use_graph = use_graph
+        self.record_history = record_history
+        self.last_history = None
+        self._ws = _Workspace()
+
+    def estimate(self, kcam, source_points, source_normals, source_mask,
+                 source_feats=None, target_points=None, target_mask=None,
+                 target_normals=None, target_feats=None, transform=None):
+        """Estimate the transform taking the source points onto the target
+        point grid (``icp.py:152-262``).
+
+        Args:
+            kcam: intrinsics, a ``KCamera``-like object with ``.matrix`` or
+                a (3, 3) tensor.
+            source_points, source_normals: (N, 3) (or (H, W, 3)) float32.
+            source_mask: (N,) bool.
+            source_feats: (C, N) (or (C, H, W)) float32 / bfloat16, optional.
+            target_points, target_normals: (H, W, 3) float32.
+            target_mask: (H, W) bool.
+            target_feats: (C, H, W) float32 / bfloat16, optional.
+            transform: (4, 4) initial transform, optional.
+
+        Returns:
+            RegistrationResult
+        """
+        device = target_points.device
+        if device.type != "cuda":
+            raise RuntimeError("Check failed: target_points: Expected a gpu tensor "
+                               "(slamtb_gb300 runs on CUDA devices only)")
+        k = _kcam_matrix(kcam, device)
+        sp = source_points.reshape(-1, 3)
+        sn = source_normals.reshape(-1, 3)
+        sm = source_mask.reshape(-1)
+        n = sp.size(0)
+        for name, t in (("source_points", sp), ("source_normals", sn),
+                        ("target_points", target_points), ("target_normals", target_normals)):
+            if t.dtype != torch.float32:
+                raise RuntimeError(f"Check failed: {name}: expected float32, got {t.dtype}")
+            if t.device != device:
+                raise RuntimeError(f"Check failed: {name}: Expected a gpu tensor on {device}")
+        if sm.numel() != n:
+            raise RuntimeError("Check failed: source_mask must have one entry per source point")
+        sp, sn = sp.contiguous(), sn.contiguous()
+        sm = sm.to(torch.bool).contiguous()
+        tp = target_points.contiguous()
+        tn = target_normals.contiguous()
+        tm = target_mask.to(device=device, dtype=torch.bool).contiguous()
+        h, w = tm.shape
+
+        has_features = (source_feats is not None and target_feats is not None
+                        and self.feat_weight > 0)
+        sf = tf = None
+        channels = 0
+        code = N.STB_F32
+        if has_features:
+            tf = target_feats.to(device).contiguous()
+            sf = source_feats.to(device).reshape(source_feats.size(0), -1).contiguous()
+            code = N.feat_dtype_code(tf)
+            if sf.dtype != tf.dtype:
+                raise RuntimeError("Check failed: source and target features must share a dtype")
+            channels = tf.size(0)
+            if tf.shape[1:] != (h, w) or sf.size(1) != n:
+                raise RuntimeError("Check failed: feature maps do not match the point grids")
+        init = None
+        if transform is not None:
+            init = torch.as_tensor(transform).to(device=device, dtype=torch.float64).contiguous()
+
+        ws, res, hist = self._ws.get(device, n, h, w, self.num_iters, self.record_history)
+        with torch.cuda.device(device):
+            N.check(N.lib().stb_icp_estimate(
+                N.ptr(k), N.ptr(sp), N.ptr(sn), N.ptr(sm), n, N.ptr(sf), N.ptr(tp),
+                N.ptr(tn), N.ptr(tm), h, w, N.ptr(tf), channels, code, N.ptr(init),
+                self.num_iters, float(self.geom_weight),
+                float(self.feat_weight if has_features else 0.0),
+                float(self.distance_threshold), float(self.normals_angle_thresh),
+                float(self.feat_residual_thresh),
+                0 if self.feat_channel_mode == "last" else 1,
+                N.ptr(ws), ws.numel(), N.ptr(res), N.ptr(hist), int(self.use_graph),
+                N.stream_of(device)))
+        out = res.cpu()
+        if hist is not None:
+            self.last_history = hist[:self.num_iters].cpu()
+        return self._result(out, n, sp.dtype)
+
+    @staticmethod
+    def _result(out, n, dtype):
+        info = out[N.RES_INFO:N.RES_INFO + 36].view(6, 6).to(dtype)
+        if int(out[N.RES_ITERS]) == 0:
+            return RegistrationResult(information=info)
+        return RegistrationResult(
+            out[N.RES_TRANSFORM:N.RES_TRANSFORM + 16].view(4, 4).clone(), info,
+            float(out[N.RES_RESIDUAL]), float(out[N.RES_MATCHES]) / n)
+
+    def estimate_frame(self, source_frame, target_frame, source_feats=None,
+                       target_feats=None, transform=None, device=None):
+        """Estimate between two frames (``icp.py:264-310``).  Frames may be
+        ``slamtb_gb300.frame.Frame`` or ``FramePointCloud``; ``device``
+        defaults to the current CUDA device (a CPU device is refused)."""
+        from ..frame import Frame, FramePointCloud, resolve_device
+        device = resolve_device(device)
+        if isinstance(source_frame, Frame):
+            source_frame = FramePointCloud.from_frame(source_frame).to(device)
+        if isinstance(target_frame, Frame):
+            target_frame = FramePointCloud.from_frame(target_frame).to(device)
+        return self.estimate(
+            source_frame.kcam, source_frame.points, source_frame.normals,
+            source_frame.mask, source_feats=source_feats,
+            target_points=target_frame.points, target_normals=target_frame.normals,
+            target_mask=target_frame.mask, target_feats=target_feats,
+            transform=transform)

@@ -1,0 +1,293 @@
+/*
+ * slamtb_gb300 -- C ABI of the GB300 (sm_103a) ICP registration path.
+ *
+ * Conventions shared by every entry point:
+ *   - All array arguments are DEVICE pointers to contiguous row-major data
+ *     on the calling thread's current CUDA device, unless stated otherwise.
+ *   - Masks are one byte per element (0 = invalid), like torch.bool.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Every
+ *     entry point is asynchronous on that stream; none synchronises.
+ *   - The library never allocates or frees memory the caller sees: outputs
+ *     and scratch ("workspace") are caller-provided.
+ *   - Return value: STB_OK (0) or one of the STB_E* codes below;
+ *     stb_last_error() returns a message for the calling thread.
+ *
+ * Reference interfaces replaced (fusion-toolbox, paths in that project):
+ *   _cslamtb.CorrespondenceMap.compute_correspondence_map
+ *        include/slamtb/matching.hpp:12-18, src/correspondence_map.cu:64-102
+ *   _cslamtb.ICPJacobian.estimate_geometric
+ *        include/slamtb/icp_jacobian.hpp:72-77, src/icp_jacobian_geometric.cu:163-214
+ *   _cslamtb.ICPJacobian.estimate_feature
+ *        include/slamtb/icp_jacobian.hpp:140-146, src/icp_jacobian_feature.cu:113-169
+ *   _cslamtb.ICPJacobian.estimate_feature_so3
+ *        include/slamtb/icp_jacobian.hpp:201-207, src/icp_jacobian_feature.cu:171-228
+ *   _cslamtb.ICPJacobian.get_information_matrix
+ *        include/slamtb/icp_jacobian.hpp:79-85, src/icp_jacobian_geometric.cu:216-249
+ *   slamtb.registration.icp.ICPOdometry.estimate (the whole Gauss-Newton
+ *        loop, with the sums of icp.py:78-80, the CPU Cholesky solve and
+ *        SE3.exp update of icp.py:236-256 and the information matrix of
+ *        icp.py:258-261 moved onto the device)
+ *        slamtb/registration/icp.py:152-262
+ */
+#ifndef SLAMTB_GB300_H_
+#define SLAMTB_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define STB_API __attribute__((visibility("default")))
+#else
+#define STB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define STB_OK 0
+#define STB_EINVAL 1   /* bad size, shape or argument value          */
+#define STB_EDEVICE 2  /* pointer is not device memory of this device */
+#define STB_EDTYPE 3   /* unsupported element type                    */
+#define STB_ECUDA 4    /* CUDA runtime error                          */
+#define STB_ETIMEOUT 5 /* a bounded device-side wait gave up          */
+
+/* ---- element types for feature maps ----------------------------------- */
+#define STB_F32 0
+#define STB_BF16 1
+
+/* ---- per-registration status bits (result block, STB_RES_STATUS) ------- */
+#define STB_ST_NOT_PD 1u     /* 6x6 J^T J was not positive definite: stopped */
+#define STB_ST_NO_MATCHES 2u /* an iteration found no correspondence        */
+#define STB_ST_NAN 4u        /* a non-finite update was produced            */
+
+/* ---- layout of the device result block (doubles) ----------------------- */
+#define STB_RES_TRANSFORM 0   /* 16: final 4x4 pose, row-major             */
+#define STB_RES_JTJ 16        /* 36: combined J^T J of the last good step  */
+#define STB_RES_INFO 52       /* 36: information matrix at the final pose  */
+#define STB_RES_RESIDUAL 88   /* residual / match count of last good step  */
+#define STB_RES_MATCHES 89    /* match count of the last good step         */
+#define STB_RES_ITERS 90      /* number of successful iterations           */
+#define STB_RES_STATUS 91     /* STB_ST_* bits                             */
+#define STB_RES_SIZE 96
+
+/* ---- layout of one per-iteration history record (doubles) ------------- */
+#define STB_HIST_TRANSFORM 0 /* 16: pose after this iteration's update     */
+#define STB_HIST_JTJ 16      /* 36: combined J^T J                          */
+#define STB_HIST_JR 52       /*  6: combined J^T r                          */
+#define STB_HIST_R2 58       /* weighted sum of squared residuals           */
+#define STB_HIST_GEOM_COUNT 59
+#define STB_HIST_FEAT_COUNT 60
+#define STB_HIST_OK 61       /* 1 when the solve succeeded                 */
+#define STB_HIST_SIZE 64
+
+/* Message of the last failing call on this thread ("" if none). */
+STB_API const char *stb_last_error(void);
+
+/* Library version string. */
+STB_API const char *stb_version(void);
+
+/* ======================================================================= *
+ * _cslamtb-compatible entry points (per-point partial outputs)
+ * ======================================================================= */
+
+/*
+ * Projective data association into a reference-layout correspondence map.
+ * Replaces CorrespondenceMap::ComputeCorrespondenceMap
+ * (src/correspondence_map.cu:64-102; pybind at src/matching.cpp:12-16).
+ *
+ * source_points/normals: float32 [num_source, 3]; source_mask: bool
+ * [source_mask_len] (the mask is ignored unless source_mask_len ==
+ * num_source, as the reference).  rt_cam: float32 row-major 3x4 or 4x4
+ * (first three rows used).  target_points/normals: float32 [height, width,
+ * 3]; target_mask: bool [height, width].  kcam: float32 row-major 3x3.
+ * merge_map: int64 [height, width], in/out, normally prefilled with
+ * 0x0fffffff7f800000; an entry is (source index << 32) | float bits of the
+ * distance, and a candidate replaces it when its (distance, index) pair is
+ * lexicographically smaller.
+ */
+STB_API int stb_correspondence_map(const float *source_points,
+                           const float *source_normals,
+                           const uint8_t *source_mask, int64_t num_source,
+                           int64_t source_mask_len, const float *rt_cam,
+                           const float *target_points,
+                           const float *target_normals,
+                           const uint8_t *target_mask, int32_t height,
+                           int32_t width, const float *kcam, int64_t *merge_map,
+                           double distance_thresh, double normal_angle_thresh,
+                           void *stream);
+
+/*
+ * Point-to-plane partials.  Replaces ICPJacobian::EstimateGeometric
+ * (src/icp_jacobian_geometric.cu:163-214).
+ * Writes JtJ_partial float32 [num_source, 6, 6], Jr_partial [num_source, 6]
+ * and squared_residual [num_source] for every source point (zeros where
+ * unmatched) and adds the number of matches to *match_count (device int32;
+ * the caller zeroes it).
+ */
+STB_API int stb_icp_jacobian_geometric(const float *src_points, const uint8_t *src_mask,
+                               int64_t num_source, const float *rt_cam,
+                               const float *tgt_points,
+                               const float *tgt_normals, int32_t height,
+                               int32_t width, const float *kcam,
+                               const int64_t *merge_map, float *JtJ_partial,
+                               float *Jr_partial, float *squared_residual,
+                               int32_t *match_count, void *stream);
+
+/*
+ * Feature-residual partials.  Replaces ICPJacobian::EstimateFeature
+ * (src/icp_jacobian_feature.cu:113-169).  src_feats: [channels, num_source],
+ * tgt_feats: [channels, height, width], both of element type feat_dtype
+ * (STB_F32 or STB_BF16).  Reproduces the reference's partials exactly,
+ * including that with several channels only the last channel's J and J*r
+ * survive (the squared residual sums all channels).
+ */
+STB_API int stb_icp_jacobian_feature(const float *src_points, const void *src_feats,
+                             const uint8_t *src_mask, int64_t num_source,
+                             const float *rt_cam, const void *tgt_feats,
+                             int32_t channels, int32_t height, int32_t width,
+                             int32_t feat_dtype, const float *kcam,
+                             const int64_t *merge_map, float residual_thresh,
+                             float *JtJ_partial, float *Jr_partial,
+                             float *squared_residuals, int32_t *match_count,
+                             void *stream);
+
+/*
+ * Rotation-only feature partials (3x3 block of the 6x6 buffers, the rest
+ * zero).  Replaces ICPJacobian::EstimateFeatureSO3
+ * (src/icp_jacobian_feature.cu:171-228, SO3ICPJacobian at
+ * src/icp_jacobian_common.hpp:64-113).  Same arguments as
+ * stb_icp_jacobian_feature.
+ */
+STB_API int stb_icp_jacobian_feature_so3(const float *src_points, const void *src_feats,
+                                 const uint8_t *src_mask, int64_t num_source,
+                                 const float *rt_cam, const void *tgt_feats,
+                                 int32_t channels, int32_t height,
+                                 int32_t width, int32_t feat_dtype,
+                                 const float *kcam, const int64_t *merge_map,
+                                 float residual_thresh, float *JtJ_partial,
+                                 float *Jr_partial, float *squared_residuals,
+                                 int32_t *match_count, void *stream);
+
+/*
+ * Information-matrix partials G^T G.  Replaces
+ * ICPJacobian::GetInformationMatrix (src/icp_jacobian_geometric.cu:216-249).
+ * GtG_partial: float32 [num_source, 6, 6].
+ */
+STB_API int stb_icp_information_partials(const float *src_points,
+                                 const uint8_t *src_mask, int64_t num_source,
+                                 const float *rt_cam, const float *tgt_points,
+                                 int32_t height, int32_t width,
+                                 const float *kcam, const int64_t *merge_map,
+                                 float *GtG_partial, void *stream);
+
+/* ======================================================================= *
+ * Fused Gauss-Newton registration (the ICPOdometry.estimate hot loop)
+ * ======================================================================= */
+
+/* Scratch bytes stb_icp_estimate needs for these sizes (256-byte aligned
+ * base required). */
+STB_API size_t stb_icp_workspace_bytes(int64_t num_source, int32_t height,
+                               int32_t width);
+
+/*
+ * The whole ICPOdometry.estimate loop (slamtb/registration/icp.py:152-262)
+ * on the device, without host synchronisation:
+ *   per iteration: association (shared by both terms), fused residual /
+ *   Jacobian / normal-equation reduction (compensated float32), 6x6 FP64
+ *   Cholesky solve, FP64 SE(3) exponential and left pose update; then the
+ *   information matrix at the final pose.
+ * Weighting follows the reference: J^T J = sum w_t^2 J_t^T J_t,
+ * J^T r = w_g J_g^T r_g - w_f J_f^T r_f, residual = sum w_t r_t^2 divided by
+ * the larger match count.  A non-positive-definite J^T J stops the loop
+ * (STB_ST_NOT_PD) and keeps the last good step, as the reference's
+ * `except: break`.
+ *
+ * kcam: float32 3x3.  src_*: as stb_correspondence_map (source_mask must
+ * have num_source entries).  src_feats / tgt_feats: NULL for geometric-only
+ * or [channels, num_source] / [channels, height, width] of feat_dtype.
+ * init_transform: float64 4x4 device pointer or NULL (identity).
+ * channel_mode: 0 = reference behaviour (last channel's J), 1 = sum over
+ * channels.  result: float64 [STB_RES_SIZE] device block.  history: NULL or
+ * float64 [num_iters, STB_HIST_SIZE] per-iteration records.
+ * num_iters <= 254.  workspace: stb_icp_workspace_bytes() bytes.
+ * use_graph != 0 captures the launch sequence in a CUDA graph on first use
+ * for this (workspace, sizes, options) and replays it afterwards.
+ */
+STB_API int stb_icp_estimate(const float *kcam, const float *src_points,
+                     const float *src_normals, const uint8_t *src_mask,
+                     int64_t num_source, const void *src_feats,
+                     const float *tgt_points, const float *tgt_normals,
+                     const uint8_t *tgt_mask, int32_t height, int32_t width,
+                     const void *tgt_feats, int32_t channels,
+                     int32_t feat_dtype, const double *init_transform,
+                     int32_t num_iters, double geom_weight, double feat_weight,
+                     double distance_thresh, double normal_angle_thresh,
+                     double feat_residual_thresh, int32_t channel_mode,
+                     void *workspace, size_t workspace_bytes, double *result,
+                     double *history, int32_t use_graph, void *stream);
+
+
+/* ======================================================================= *
+ * Frame preparation (inputs of every pyramid level)
+ * ======================================================================= */
+
+/*
+ * Metric depth -> camera-space points and raw validity mask.  Replaces
+ * depth_image_to_uvz (slamtb/_utils.py:11-37) + KCamera.backproject
+ * (slamtb/camera.py:127-149): z = depth * depth_scale + depth_bias,
+ * x = (u - cx) z / fx, y = (v - cy) z / fy; raw_mask = depth > 0
+ * (slamtb/frame.py:290).  depth float32 [h, w]; points float32 [h, w, 3].
+ */
+STB_API int stb_depth_to_points(const float *depth, float depth_scale,
+                                float depth_bias, const float *kcam,
+                                float *points, uint8_t *raw_mask,
+                                int32_t height, int32_t width, void *stream);
+
+/* Mask erosion.  Replaces Processing::ErodeMask (src/erode_mask.cu:42-54),
+ * including its neighbourhood (above, right, left; never below). */
+STB_API int stb_erode_mask(const uint8_t *in_mask, uint8_t *out_mask,
+                           int32_t height, int32_t width, void *stream);
+
+/* Central-difference normals.  Replaces Processing::EstimateNormals with
+ * kCentralDifferences (src/normals.cu:27-100,190-208). */
+STB_API int stb_estimate_normals(const float *xyz, const uint8_t *mask,
+                                 float *normals, int32_t height, int32_t width,
+                                 void *stream);
+
+/* Nearest-to-mean 2x2 XYZ downsample.  Replaces Processing::DownsampleXYZ
+ * (src/downsample.cu:25-98); dst is int(size * scale). */
+STB_API int stb_downsample_xyz(const float *xyz, const uint8_t *mask,
+                               int32_t height, int32_t width, float scale,
+                               float *dst, int32_t dst_height,
+                               int32_t dst_width, void *stream);
+
+/* Nearest mask downsample.  Replaces Processing::DownsampleMask
+ * (src/downsample.cu:100-131). */
+STB_API int stb_downsample_mask(const uint8_t *mask, int32_t height,
+                                int32_t width, float scale, uint8_t *dst,
+                                int32_t dst_height, int32_t dst_width,
+                                void *stream);
+
+/* 2x2 mean feature downsample.  Replaces Processing::DownsampleFeatures
+ * (src/downsample.cu:133-191).  feats/dst: [channels, h, w] of feat_dtype. */
+STB_API int stb_downsample_features(const void *feats, int32_t channels,
+                                    int32_t height, int32_t width,
+                                    int32_t feat_dtype, float scale, void *dst,
+                                    int32_t dst_height, int32_t dst_width,
+                                    void *stream);
+
+/* 3x3 Gaussian blur with reflect borders: the kornia
+ * GaussianBlur2d((3, 3), (sigma, sigma)) of feature_pyramid
+ * (slamtb/processing.py:141-159). */
+STB_API int stb_gaussian_blur3(const void *feats, int32_t channels,
+                               int32_t height, int32_t width,
+                               int32_t feat_dtype, double sigma, void *dst,
+                               void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLAMTB_GB300_H_ */

@@ -1,0 +1,64 @@
+"""Extract the known-answer fixtures from the reference's own test data.
+
+Run in a container where the reference is mounted (it is read here, never
+at test time):
+
+    python tests/golden/make_golden.py /root/reference
+
+It decodes the 16-bit depth PNGs of ``test-data/rgbd/sample2`` frames used
+by the reference's tests (frames 0 and 3: the synthetic pair of
+``slamtb/registration/_test/test_icp.py:19-27``; frame 13: the pair of
+``slamtb/registration/_test/test_correspondence_map.py:16-19``) and stores
+them, with their intrinsics, depth scale and ground-truth camera-to-world
+poses from ``frames.json``, as ``sample2.npz`` (depth stored as row-wise
+first differences; ``load_sample2`` undoes that).
+"""
+import json
+import pathlib
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from oracle.png16 import read_png  # noqa: E402
+
+FRAMES = (0, 3, 13)
+
+
+def load_sample2(path=HERE / "sample2.npz"):
+    """Return {frame: dict(depth uint16 (480, 640), rt_cam f64 (4, 4),
+    kcam f32 (3, 3), depth_scale, depth_bias)}."""
+    z = np.load(path)
+    out = {}
+    for i in FRAMES:
+        depth = np.cumsum(z[f"depth_dx_{i}"].astype(np.int32), axis=1)
+        out[i] = dict(depth=depth.astype(np.uint16), rt_cam=z[f"rt_cam_{i}"],
+                      kcam=z[f"kcam_{i}"], depth_scale=z[f"depth_scale_{i}"],
+                      depth_bias=z[f"depth_bias_{i}"])
+    return out
+
+
+def main(reference_root):
+    root = pathlib.Path(reference_root) / "test-data" / "rgbd" / "sample2"
+    meta = json.load(open(root / "frames.json"))["root"]
+    out = {}
+    for i in FRAMES:
+        entry = meta[i]
+        depth = read_png(root / entry["depth_image"])
+        assert depth.dtype == np.uint16 and depth.shape == (480, 640)
+        info = entry["info"]
+        # row-wise first differences compress ~2.3x better than raw depth
+        out[f"depth_dx_{i}"] = np.diff(depth.astype(np.int32), axis=1,
+                                       prepend=0).astype(np.int16)
+        out[f"rt_cam_{i}"] = np.array(info["rt_cam"]["matrix"], dtype=np.float64)
+        out[f"kcam_{i}"] = np.array(info["kcam"]["matrix"], dtype=np.float32)
+        out[f"depth_scale_{i}"] = np.float32(info["depth_scale"])
+        out[f"depth_bias_{i}"] = np.float32(info["depth_bias"])
+    np.savez_compressed(HERE / "sample2.npz", **out)
+    print("wrote", HERE / "sample2.npz")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

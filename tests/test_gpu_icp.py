@@ -1,0 +1,179 @@
+"""Fused Gauss-Newton path (ICPOdometry -> stb_icp_estimate) against the
+FP64 oracle, iteration by iteration.
+
+Tolerances (the 1e-5 gate of the path):
+  * J^T J: ||A_gpu - A_oracle||_F <= 1e-5 ||A_oracle||_F
+  * J^T r: ||b_gpu - b_oracle||  <= 1e-5 sum_i |J_i||r_i|  (J^T r cancels
+    towards 0 at convergence, so it is measured against the magnitude of
+    its terms)
+  * pose after each iteration: ||log(T_oracle^-1 T_gpu)|| <= 1e-5 max(
+    ||log T_oracle||, 1e-3)
+  * match counts equal up to 1e-4 (the association is bit-exact for a given
+    float32 pose; the two loops cast their own FP64 poses, which can differ
+    in a last bit).
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import icp_oracle as io
+from _helpers import synthetic_pair, sample2_pair, pose_error, ANGLE_20
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def _dev(d, cuda, feats_dtype=torch.float32):
+    s, t = d["src"], d["tgt"]
+    out = dict(kcam=torch.from_numpy(d["kcam"]).to(cuda),
+               sp=torch.from_numpy(s["points"]).to(cuda).view(-1, 3),
+               sn=torch.from_numpy(s["normals"]).to(cuda).view(-1, 3),
+               sm=torch.from_numpy(s["mask"]).to(cuda).view(-1),
+               tp=torch.from_numpy(t["points"]).to(cuda),
+               tn=torch.from_numpy(t["normals"]).to(cuda),
+               tm=torch.from_numpy(t["mask"]).to(cuda))
+    if "src_feats" in d:
+        out["sf"] = torch.from_numpy(d["src_feats"]).to(cuda).to(feats_dtype)
+        out["tf"] = torch.from_numpy(d["tgt_feats"]).to(cuda).to(feats_dtype)
+    return out
+
+
+def _run_gpu(x, icp, transform=None):
+    return icp.estimate(x["kcam"], x["sp"], x["sn"], x["sm"], source_feats=x.get("sf"),
+                        target_points=x["tp"], target_mask=x["tm"], target_normals=x["tn"],
+                        target_feats=x.get("tf"), transform=transform)
+
+
+def _run_oracle(d, x, kw, transform=None, channel_mode="last"):
+    s, t = d["src"], d["tgt"]
+    sf = x["sf"].float().cpu().numpy() if "sf" in x else None
+    tf = x["tf"].float().cpu().numpy() if "tf" in x else None
+    return io.icp_estimate(d["kcam"], s["points"], s["normals"], s["mask"], t["points"],
+                           t["normals"], t["mask"], src_feats=sf, tgt_feats=tf,
+                           transform=transform, channel_mode=channel_mode, **kw)
+
+
+def _rel_pose(a, b):
+    d = io.se3_log(np.linalg.inv(b) @ a)
+    return np.linalg.norm(d) / max(np.linalg.norm(io.se3_log(b)), 1e-3)
+
+
+def _compare(hist, ores, check_counts=True):
+    from slamtb_gb300 import _native as N
+    h = hist.numpy()
+    assert len(ores.history) > 0
+    for k, o in enumerate(ores.history):
+        g = h[k]
+        assert g[N.HIST_OK] == 1.0
+        A = g[N.HIST_JTJ:N.HIST_JTJ + 36].reshape(6, 6)
+        b = g[N.HIST_JR:N.HIST_JR + 6]
+        T = g[N.HIST_TRANSFORM:N.HIST_TRANSFORM + 16].reshape(4, 4)
+        if check_counts:
+            # equal unless the two FP64 loops' float32 pose casts differ in a
+            # last bit and flip a handful of correspondences
+            gc = max(g[N.HIST_GEOM_COUNT], g[N.HIST_FEAT_COUNT])
+            assert abs(gc - o["count"]) <= max(2, 1e-4 * o["count"]), (k, gc, o["count"])
+        assert np.linalg.norm(A - o["JtJ"]) <= TOL * np.linalg.norm(o["JtJ"]), k
+        assert np.linalg.norm(b - o["Jr"]) <= TOL * o["Jr_scale"], k
+        assert _rel_pose(T, o["transform"]) <= TOL, (k, _rel_pose(T, o["transform"]))
+
+
+GEOM = dict(num_iters=10, geom_weight=1.0, feat_weight=0.0, distance_threshold=0.1,
+            normals_angle_thresh=ANGLE_20)
+
+
+@pytest.fixture(scope="module")
+def pair0():
+    return synthetic_pair(0, feature_channels=0)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_geometric_matches_oracle_per_iteration(cuda, pair0, use_graph):
+    from slamtb_gb300.registration.icp import ICPOdometry
+    x = _dev(pair0, cuda)
+    x.pop("sf"), x.pop("tf")
+    icp = ICPOdometry(record_history=True, use_graph=use_graph, **GEOM)
+    res = _run_gpu(x, icp)
+    ores = _run_oracle(pair0, x, GEOM)
+    assert len(ores.history) == 10
+    _compare(icp.last_history, ores)
+    assert abs(res.residual - ores.residual) <= TOL * ores.residual
+    assert res.match_ratio == pytest.approx(ores.match_ratio, abs=0)
+    np.testing.assert_allclose(res.information.double().numpy(), ores.information, rtol=1e-5)
+    assert res.information.dtype == torch.float32
+
+
+def test_hybrid_matches_oracle_per_iteration(cuda, pair0):
+    from slamtb_gb300.registration.icp import ICPOdometry
+    kw = dict(GEOM, feat_weight=0.1)
+    x = _dev(pair0, cuda)
+    icp = ICPOdometry(record_history=True, **kw)
+    _run_gpu(x, icp)
+    _compare(icp.last_history, _run_oracle(pair0, x, kw))
+
+
+@pytest.mark.parametrize("mode", ["last", "sum"])
+def test_bf16_multichannel_features(cuda, mode):
+    from slamtb_gb300.registration.icp import ICPOdometry
+    d = synthetic_pair(3, width=320, height=240, feature_channels=4)
+    kw = dict(GEOM, num_iters=6, feat_weight=0.05)
+    x = _dev(d, cuda, torch.bfloat16)
+    icp = ICPOdometry(record_history=True, feat_channel_mode=mode, **kw)
+    _run_gpu(x, icp)
+    _compare(icp.last_history, _run_oracle(d, x, kw, channel_mode=mode))
+
+
+def test_feature_only_and_initial_transform(cuda):
+    from slamtb_gb300.registration.icp import ICPOdometry
+    d = synthetic_pair(2, width=320, height=240, feature_channels=0)
+    kw = dict(num_iters=5, geom_weight=0.0, feat_weight=1.0, distance_threshold=0.1,
+              normals_angle_thresh=ANGLE_20)
+    init = io.se3_exp([0.002, -0.001, 0.003, 0.001, 0.002, -0.001])
+    x = _dev(d, cuda)
+    icp = ICPOdometry(record_history=True, **kw)
+    _run_gpu(x, icp, transform=torch.from_numpy(init))
+    _compare(icp.last_history, _run_oracle(d, x, kw, transform=init))
+
+
+def test_deterministic_and_graph_equals_direct(cuda, pair0):
+    from slamtb_gb300.registration.icp import ICPOdometry
+    x = _dev(pair0, cuda)
+    kw = dict(GEOM, feat_weight=0.1)
+    outs = []
+    for use_graph in (True, True, False):
+        icp = ICPOdometry(record_history=True, use_graph=use_graph, **kw)
+        res = _run_gpu(x, icp)
+        outs.append((res.transform.numpy().copy(), icp.last_history.numpy().copy()))
+    for T, H in outs[1:]:
+        np.testing.assert_array_equal(T, outs[0][0])
+        np.testing.assert_array_equal(H, outs[0][1])
+
+
+def test_no_matches_returns_empty_result(cuda, pair0):
+    """Zero matches -> J^T J = 0 -> the Cholesky fails on the first
+    iteration: the reference breaks out (icp.py:241-242) and returns an
+    empty RegistrationResult whose information is still computed."""
+    from slamtb_gb300.registration.icp import ICPOdometry
+    x = _dev(pair0, cuda)
+    x["tm"] = torch.zeros_like(x["tm"])
+    res = _run_gpu(x, ICPOdometry(**GEOM))
+    assert res.transform is None and res.residual == math.inf and res.match_ratio == 0
+    assert torch.count_nonzero(res.information) == 0
+
+
+def test_sample2_known_answer(cuda):
+    from slamtb_gb300.registration.icp import ICPOdometry
+    d = sample2_pair(0, 3)
+    x = _dev(d, cuda)
+    kw = dict(num_iters=15, geom_weight=1, feat_weight=0, distance_threshold=0.1,
+              normals_angle_thresh=math.pi / 4)
+    icp = ICPOdometry(record_history=True, **kw)
+    res = _run_gpu(x, icp)
+    ores = _run_oracle(d, x, kw)
+    _compare(icp.last_history, ores)
+    _, gt_r = pose_error(np.eye(4), d["gt"])
+    err_t, err_r = pose_error(res.transform.numpy(), d["gt"])
+    assert err_r < 0.1 * gt_r and err_t < 1e-3

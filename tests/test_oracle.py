@@ -1,0 +1,208 @@
+"""Self-tests of the CPU oracle (no GPU): SE(3) algebra, the Jacobian sign
+conventions against finite differences, the 6x6 solve, and hand-built
+association cases (ties, bounds, thresholds, NaN angle)."""
+import math
+
+import numpy as np
+import pytest
+import scipy.linalg
+
+from oracle import icp_oracle as io
+from oracle import frame_prep as fp
+
+
+def _twist_matrix(xi):
+    v, w = xi[:3], xi[3:]
+    M = np.zeros((4, 4))
+    M[:3, :3] = [[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]]
+    M[:3, 3] = v
+    return M
+
+
+@pytest.mark.parametrize("scale", [1e-9, 1e-4, 5e-3, 0.05, 0.8, 2.5])
+def test_se3_exp_matches_matrix_exponential(scale):
+    rng = np.random.default_rng(1)
+    for _ in range(5):
+        xi = rng.normal(size=6) * scale
+        np.testing.assert_allclose(io.se3_exp(xi), scipy.linalg.expm(_twist_matrix(xi)),
+                                   rtol=0, atol=1e-13)
+
+
+def test_se3_log_roundtrip():
+    rng = np.random.default_rng(2)
+    for s in (1e-7, 1e-3, 0.3, 2.0):
+        xi = rng.normal(size=6) * s
+        np.testing.assert_allclose(io.se3_log(io.se3_exp(xi)), xi, rtol=1e-9, atol=1e-12)
+
+
+def test_cholesky_solve6():
+    rng = np.random.default_rng(3)
+    A = rng.normal(size=(6, 6))
+    A = A @ A.T + 0.1 * np.eye(6)
+    b = rng.normal(size=6)
+    ok, x = io.cholesky_solve6(A, b)
+    assert ok
+    np.testing.assert_allclose(x, np.linalg.solve(A, b), rtol=1e-10)
+    assert not io.cholesky_solve6(np.zeros((6, 6)), b)[0]
+    B = A.copy()
+    B[2, 2] = -1.0
+    assert not io.cholesky_solve6(B, b)[0]
+    C = A.copy()
+    C[0, 0] = np.nan
+    assert not io.cholesky_solve6(C, b)[0]
+
+
+def test_geometric_jacobian_is_minus_residual_derivative():
+    """J = [n; p x n] (icp_jacobian_common.hpp:41-48) equals -dr/dxi for the
+    left update T <- exp(xi) T, so the reference's update +solve(JtJ, Jtr)
+    (icp.py:233-240) is a Gauss-Newton step."""
+    rng = np.random.default_rng(4)
+    p = rng.normal(size=3) + [0, 0, 2]
+    q = p + rng.normal(size=3) * 0.01
+    n = rng.normal(size=3)
+    n /= np.linalg.norm(n)
+
+    def r(xi):
+        tp = (io.se3_exp(xi) @ np.append(p, 1.0))[:3]
+        return (q - tp) @ n
+
+    J = np.concatenate([n, np.cross(p, n)])
+    eps = 1e-6
+    fd = np.array([(r(eps * e) - r(-eps * e)) / (2 * eps) for e in np.eye(6)])
+    np.testing.assert_allclose(fd, -J, rtol=1e-6, atol=1e-9)
+
+
+def test_feature_jacobian_is_plus_residual_derivative():
+    """J_f = [g; p x g] with g = grad(f) dpi/dp equals +dr/dxi for
+    r = f(pi(exp(xi) p)) - f_s, hence the reference's -w_f J^T r
+    (icp.py:222).  Checked on a linear intensity ramp."""
+    k = np.array([[525, 0, 319.5], [0, 525, 239.5], [0, 0, 1]], dtype=np.float64)
+    gu, gv = 0.013, -0.007
+    p = np.array([0.2, -0.1, 2.0])
+
+    def f(uv):
+        return gu * uv[0] + gv * uv[1]
+
+    def proj(x):
+        return np.array([k[0, 0] * x[0] / x[2] + k[0, 2], k[1, 1] * x[1] / x[2] + k[1, 2]])
+
+    def r(xi):
+        return f(proj((io.se3_exp(xi) @ np.append(p, 1.0))[:3]))
+
+    fx, fy, z = k[0, 0], k[1, 1], p[2]
+    g = np.array([gu * fx / z, gv * fy / z, -gu * p[0] * fx / z ** 2 - gv * p[1] * fy / z ** 2])
+    J = np.concatenate([g, np.cross(p, g)])
+    eps = 1e-6
+    fd = np.array([(r(eps * e) - r(-eps * e)) / (2 * eps) for e in np.eye(6)])
+    np.testing.assert_allclose(fd, J, rtol=1e-6, atol=1e-9)
+
+
+def _grid(h=4, w=5, z=2.0):
+    pts = np.zeros((h, w, 3), np.float32)
+    k = np.array([[100, 0, 2], [0, 100, 1.5], [0, 0, 1]], np.float32)
+    for v in range(h):
+        for u in range(w):
+            pts[v, u] = [(u - k[0, 2]) * z / k[0, 0], (v - k[1, 2]) * z / k[1, 1], z]
+    nrm = np.zeros_like(pts)
+    nrm[..., 2] = -1
+    return pts, nrm, np.ones((h, w), bool), k
+
+
+def test_association_tie_goes_to_smaller_index():
+    pts, nrm, mask, k = _grid()
+    # two identical sources land on the same pixel at the same distance
+    src = np.stack([pts[1, 2], pts[1, 2]]).astype(np.float32)
+    a = io.associate32(src, np.stack([nrm[1, 2]] * 2), np.ones(2, bool), io.pose_rt32(np.eye(4)),
+                       pts, nrm, mask, k, 0.1, math.pi / 4)
+    assert a.winner[1, 2] == 0 and a.count == 1
+    assert (a.ref_map[1, 2] >> 32) == 0
+    assert a.ref_map[0, 0] == io.CORRESP_EMPTY
+
+
+def test_association_bounds_and_rounding():
+    pts, nrm, mask, k = _grid()
+    # u in [-0.5, 0) rounds to column 0 (kept); u = -0.5 rounds to -1 (dropped)
+    z = np.float32(2.0)
+    def at_u(u):
+        return np.array([[(u - k[0, 2]) * z / k[0, 0], 0.0, z]], np.float32)
+    keep = io.associate32(at_u(-0.4), nrm[:1, 0], np.ones(1, bool), io.pose_rt32(np.eye(4)),
+                          pts, nrm, mask, k, 10.0, math.pi)
+    drop = io.associate32(at_u(-0.5), nrm[:1, 0], np.ones(1, bool), io.pose_rt32(np.eye(4)),
+                          pts, nrm, mask, k, 10.0, math.pi)
+    assert keep.count == 1 and drop.count == 0
+
+
+def test_association_thresholds_and_nan_angle():
+    pts, nrm, mask, k = _grid()
+    src = pts[2, 3][None].copy()
+    far = src.copy()
+    far[0, 2] += 0.2
+    eye = io.pose_rt32(np.eye(4))
+    one = np.ones(1, bool)
+    assert io.associate32(far, nrm[2, 3][None], one, eye, pts, nrm, mask, k, 0.1, math.pi).count == 0
+    tilted = np.array([[0.0, math.sin(0.5), -math.cos(0.5)]], np.float32)  # 0.5 rad off
+    assert io.associate32(src, tilted, one, eye, pts, nrm, mask, k, 0.1, 0.4).count == 0
+    assert io.associate32(src, tilted, one, eye, pts, nrm, mask, k, 0.1, 0.6).count == 1
+    # a zero normal gives a NaN cosine, which the reference accepts
+    zero = np.zeros((1, 3), np.float32)
+    assert io.associate32(src, zero, one, eye, pts, nrm, mask, k, 0.1, 0.1).count == 1
+    # masked target pixel
+    m2 = mask.copy()
+    m2[2, 3] = False
+    assert io.associate32(src, nrm[2, 3][None], one, eye, pts, nrm, m2, k, 0.1, math.pi).count == 0
+
+
+def test_angle_threshold_rounding():
+    for th in (0.1, math.pi / 9, math.pi / 4, 1.0, 3.0):
+        c = io.angle_cos_threshold(th)
+        assert float(c) <= math.cos(float(np.float32(th)))
+        assert float(np.nextafter(c, np.float32(1))) > math.cos(float(np.float32(th)))
+    assert io.angle_cos_threshold(math.pi) == -np.inf
+
+
+def test_partials_sum_to_terms():
+    """The float32 per-point partials (the _cslamtb contract) sum to the
+    float64 reduced terms within float32 accuracy."""
+    from _helpers import synthetic_pair
+    d = synthetic_pair(5, width=160, height=120, feature_channels=0)
+    s, t = d["src"], d["tgt"]
+    rt = io.pose_rt32(np.eye(4))
+    a = io.associate32(s["points"], s["normals"], s["mask"], rt, t["points"], t["normals"],
+                       t["mask"], d["kcam"], 0.1, math.radians(20))
+    JtJ, Jtr, r2, cnt = io.geometric_partials32(s["points"], s["mask"], rt, t["points"],
+                                                t["normals"], d["kcam"], a.ref_map)
+    g = io.geometric_terms64(a, s["points"], rt, t["points"], t["normals"])
+    assert cnt == g.count == a.count > 100
+    np.testing.assert_allclose(JtJ.astype(np.float64).sum(0), g.JtJ, rtol=1e-5,
+                               atol=1e-5 * np.abs(g.JtJ).max())
+    np.testing.assert_allclose(Jtr.astype(np.float64).sum(0), g.Jtr, rtol=0, atol=1e-5 * g.scale)
+    JtJ, Jtr, r2, cnt, passed = io.feature_partials32(
+        s["points"], d["src_feats"], s["mask"], rt, d["tgt_feats"], d["kcam"], a.ref_map, 2.75)
+    f = io.feature_terms64(a, s["points"], d["src_feats"], rt, d["tgt_feats"], d["kcam"], 2.75)
+    assert cnt == f.count
+    np.testing.assert_allclose(JtJ.astype(np.float64).sum(0), f.JtJ, rtol=1e-4,
+                               atol=1e-4 * np.abs(f.JtJ).max())
+
+
+def test_erode_quirk_ignores_row_below():
+    m = np.ones((5, 5), bool)
+    m[3, 2] = False  # the pixel below (2, 2)
+    e = fp.erode_mask(m)
+    assert e[2, 2]  # reference neighbourhood never looks down (erode_mask.cu:24)
+    assert not e[4, 2]  # looks up
+    assert not e[3, 1] and not e[3, 3]  # left / right
+
+
+def test_normals_of_a_plane():
+    k = np.array([[300, 0, 31.5], [0, 300, 23.5], [0, 0, 1]], np.float32)
+    v, u = np.mgrid[0:48, 0:64].astype(np.float32)
+    n = np.array([0.2, -0.3, -1.0])
+    n /= np.linalg.norm(n)
+    # plane n.x = d  ->  z = d / (n . ((u-cx)/fx, (v-cy)/fy, 1))
+    rays = np.stack([(u - k[0, 2]) / k[0, 0], (v - k[1, 2]) / k[1, 1], np.ones_like(u)], -1)
+    z = (-2.0 / (rays @ n)).astype(np.float32)
+    pts = fp.depth_to_points(z, k)
+    nr = fp.estimate_normals(pts, np.ones(z.shape, bool))
+    inner = nr[1:-1, 1:-1].reshape(-1, 3)
+    dots = np.abs(inner @ n)
+    assert dots.min() > 0.999
