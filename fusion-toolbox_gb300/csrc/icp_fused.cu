@@ -27,6 +27,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "gn_solve.cuh"
 #include "stb_common.cuh"
@@ -456,6 +457,53 @@ __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__
 }
 
 // ---------------------------------------------------------------------------
+// Per-kernel CUDA-event timing (stb_profile_*): when enabled, every launch of
+// the sequence is bracketed by two events recorded on the launching stream
+// (captured as event nodes when the sequence is a graph).
+// ---------------------------------------------------------------------------
+enum ProfKind { kProfAssoc = 0, kProfReduce = 1, kProfInfo = 2, kProfSetup = 3, kProfKinds = 4 };
+
+struct ProfSet {
+  std::vector<cudaEvent_t> start, stop;
+  std::vector<int> kind;
+  int used = 0;
+  void reset() { used = 0; }
+  void before(int k, cudaStream_t st) {
+    if ((int)start.size() <= used) {
+      cudaEvent_t a, b;
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      start.push_back(a);
+      stop.push_back(b);
+      kind.push_back(k);
+    }
+    kind[used] = k;
+    // External: inside stream capture this becomes an event-record node
+    // that records at every replay (a plain record only orders the capture).
+    cudaEventRecordWithFlags(start[used], st, cudaEventRecordExternal);
+  }
+  void after(cudaStream_t st) {
+    cudaEventRecordWithFlags(stop[used++], st, cudaEventRecordExternal);
+  }
+};
+
+std::mutex g_prof_mutex;
+bool g_prof_on = false;
+ProfSet g_prof_direct;
+ProfSet *g_prof_last = nullptr;
+
+struct Timed {
+  ProfSet *ps;
+  cudaStream_t st;
+  Timed(ProfSet *p, int k, cudaStream_t s) : ps(p), st(s) {
+    if (ps) ps->before(k, st);
+  }
+  ~Timed() {
+    if (ps) ps->after(st);
+  }
+};
+
+// ---------------------------------------------------------------------------
 // Launch sequence and CUDA-graph cache
 // ---------------------------------------------------------------------------
 struct Plan {
@@ -477,16 +525,33 @@ ReduceFn pick_reduce(const Plan &p) {
 
 // Everything after k_begin; k_begin itself is launched by the caller so that
 // a captured graph can take new Job parameters per call.
-int launch_body(const Plan &p, cudaStream_t st) {
+int launch_body(const Plan &p, cudaStream_t st, ProfSet *ps) {
   const unsigned agrid = blocks_for(p.n, kAssocThreads);
   const ReduceFn red = pick_reduce(p);
   for (int it = 0; it < p.iters; ++it) {
-    if (p.n > 0) k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, it, 0);
+    if (p.n > 0) {
+      Timed t(ps, kProfAssoc, st);
+      k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, it, 0);
+    }
+    Timed t(ps, kProfReduce, st);
     red<<<p.nblocks, kReduceThreads, 0, st>>>(p.job_dev, it);
   }
-  if (p.n > 0) k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, p.iters, 1);
-  k_info<<<p.nblocks, kReduceThreads, 0, st>>>(p.job_dev, p.iters);
+  if (p.n > 0) {
+    Timed t(ps, kProfAssoc, st);
+    k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, p.iters, 1);
+  }
+  {
+    Timed t(ps, kProfInfo, st);
+    k_info<<<p.nblocks, kReduceThreads, 0, st>>>(p.job_dev, p.iters);
+  }
   return check_launch("stb_icp_estimate");
+}
+
+// Key-map clear and k_begin (the Job for this call).
+void launch_setup(const Plan &p, Job &job, cudaStream_t st, ProfSet *ps) {
+  Timed t(ps, kProfSetup, st);
+  cudaMemsetAsync(p.keys, 0xff, sizeof(unsigned long long) * (size_t)p.H * p.W, st);
+  k_begin<<<1, 32, 0, st>>>(job, p.job_dev);
 }
 
 struct GraphEntry {
@@ -494,16 +559,18 @@ struct GraphEntry {
   cudaGraphExec_t exec = nullptr;
   cudaGraphNode_t begin_node = nullptr;
   cudaKernelNodeParams begin_params{};
+  ProfSet *prof = nullptr;  // event pairs captured in the graph (profiling)
 };
 
-using GraphKey = std::tuple<void *, int64_t, int, int, int, int, int, int, int, int, bool>;
+using GraphKey = std::tuple<void *, int64_t, int, int, int, int, int, int, int, int, bool, bool>;
 std::mutex g_graph_mutex;
 std::map<GraphKey, GraphEntry> g_graphs;
 
 int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st) {
   std::lock_guard<std::mutex> lock(g_graph_mutex);
+  const bool prof = g_prof_on;
   const GraphKey key{(void *)p.job_dev, p.n, p.H, p.W, p.C, p.dtype, p.iters,
-                     p.use_geom, p.use_feat, p.channel_mode, with_history};
+                     p.use_geom, p.use_feat, p.channel_mode, with_history, prof};
   auto it = g_graphs.find(key);
   Job job_copy = job;
   Job *dst = p.job_dev;
@@ -513,16 +580,17 @@ int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st)
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess)
       return check_launch("cudaStreamCreate");
     cudaGraph_t graph;
+    ProfSet *ps = prof ? new ProfSet() : nullptr;
     cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    cudaMemsetAsync(p.keys, 0xff, sizeof(unsigned long long) * (size_t)p.H * p.W, cap);
-    k_begin<<<1, 32, 0, cap>>>(job_copy, dst);
-    launch_body(p, cap);
+    launch_setup(p, job_copy, cap, ps);
+    launch_body(p, cap, ps);
     const cudaError_t cerr = cudaStreamEndCapture(cap, &graph);
     cudaStreamDestroy(cap);
     if (cerr != cudaSuccess)
       return fail(STB_ECUDA, "Cuda call error stb_icp_estimate (graph capture): %s",
                   cudaGetErrorString(cerr));
     GraphEntry e;
+    e.prof = ps;
     // locate k_begin's node to update its parameters on later calls
     size_t count = 0;
     cudaGraphGetNodes(graph, nullptr, &count);
@@ -550,6 +618,10 @@ int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st)
     it = g_graphs.emplace(key, e).first;
   }
   GraphEntry &e = it->second;
+  if (e.prof) {
+    std::lock_guard<std::mutex> plock(g_prof_mutex);
+    g_prof_last = e.prof;
+  }
   cudaKernelNodeParams kp = e.begin_params;
   kp.kernelParams = args;
   kp.extra = nullptr;
@@ -680,7 +752,43 @@ extern "C" int stb_icp_estimate(
 
   const cudaStream_t st = as_stream(stream);
   if (use_graph) return run_graph(p, job, history != nullptr, st);
-  cudaMemsetAsync(p.keys, 0xff, sizeof(unsigned long long) * (size_t)npix, st);
-  k_begin<<<1, 32, 0, st>>>(job, p.job_dev);
-  return launch_body(p, st);
+  ProfSet *ps = nullptr;
+  if (g_prof_on) {
+    std::lock_guard<std::mutex> plock(g_prof_mutex);
+    g_prof_direct.reset();
+    ps = g_prof_last = &g_prof_direct;
+  }
+  launch_setup(p, job, st, ps);
+  return launch_body(p, st, ps);
+}
+
+extern "C" int stb_profile_enable(int32_t on) {
+  clear_error();
+  std::lock_guard<std::mutex> plock(g_prof_mutex);
+  g_prof_on = on != 0;
+  g_prof_last = nullptr;
+  return STB_OK;
+}
+
+extern "C" int stb_profile_read(double *ms_by_kind, int64_t *launches_by_kind,
+                                int32_t num_kinds) {
+  clear_error();
+  if (num_kinds < kProfKinds)
+    return fail(STB_EINVAL, "Check failed: num_kinds must be at least %d", kProfKinds);
+  for (int k = 0; k < num_kinds; ++k) {
+    ms_by_kind[k] = 0.0;
+    launches_by_kind[k] = 0;
+  }
+  std::lock_guard<std::mutex> plock(g_prof_mutex);
+  if (!g_prof_last) return STB_OK;
+  for (int i = 0; i < g_prof_last->used; ++i) {
+    float ms = 0.f;
+    const cudaError_t err =
+        cudaEventElapsedTime(&ms, g_prof_last->start[i], g_prof_last->stop[i]);
+    if (err != cudaSuccess)
+      return fail(STB_ECUDA, "Cuda call error stb_profile_read: %s", cudaGetErrorString(err));
+    ms_by_kind[g_prof_last->kind[i]] += ms;
+    launches_by_kind[g_prof_last->kind[i]] += 1;
+  }
+  return STB_OK;
 }

@@ -47,6 +47,8 @@ _SIGNATURES = {
     "stb_icp_information_partials": (ctypes.c_int, [
         _vp, _vp, _i64, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
     "stb_icp_workspace_bytes": (_sz, [_i64, _i32, _i32]),
+    "stb_profile_enable": (ctypes.c_int, [_i32]),
+    "stb_profile_read": (ctypes.c_int, [ctypes.POINTER(_f64), ctypes.POINTER(_i64), _i32]),
     "stb_depth_to_points": (ctypes.c_int, [_vp, _f32, _f32, _vp, _vp, _vp, _i32, _i32, _vp]),
     "stb_erode_mask": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),
     "stb_estimate_normals": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _vp]),
@@ -99,6 +101,23 @@ def ptr(t):
 
 def stream_of(device):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+PROFILE_KINDS = ("association", "reduction+solve", "information", "setup")
+
+
+def profile_enable(on):
+    check(lib().stb_profile_enable(1 if on else 0))
+
+
+def profile_read():
+    """{kind: (ms, launches)} of the most recent profiled estimate call
+    (call after the stream has completed)."""
+    n = len(PROFILE_KINDS)
+    ms = (_f64 * n)()
+    cnt = (_i64 * n)()
+    check(lib().stb_profile_read(ms, cnt, n))
+    return {k: (ms[i], cnt[i]) for i, k in enumerate(PROFILE_KINDS)}
 
 
 def feat_dtype_code(t):

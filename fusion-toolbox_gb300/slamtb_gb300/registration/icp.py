@@ -116,6 +116,23 @@ class ICPOdometry:
         Returns:
             RegistrationResult
         """
+        res, hist, n, dtype = self.launch(
+            kcam, source_points, source_normals, source_mask, source_feats, target_points,
+            target_mask, target_normals, target_feats, transform)
+        out = res.cpu()
+        if hist is not None:
+            self.last_history = hist[:self.num_iters].cpu()
+        return self._result(out, n, dtype)
+
+    def launch(self, kcam, source_points, source_normals, source_mask, source_feats=None,
+               target_points=None, target_mask=None, target_normals=None, target_feats=None,
+               transform=None):
+        """Enqueue the registration on the current stream without waiting.
+
+        Returns (result, history, num_source, dtype): ``result`` is the
+        float64 device result block (``STB_RES_*`` layout), ``history`` the
+        per-iteration device records or None.  The block is reused by the
+        next call of this estimator."""
         device = target_points.device
         if device.type != "cuda":
             raise RuntimeError("Check failed: target_points: Expected a gpu tensor "
@@ -170,10 +187,7 @@ class ICPOdometry:
                 0 if self.feat_channel_mode == "last" else 1,
                 N.ptr(ws), ws.numel(), N.ptr(res), N.ptr(hist), int(self.use_graph),
                 N.stream_of(device)))
-        out = res.cpu()
-        if hist is not None:
-            self.last_history = hist[:self.num_iters].cpu()
-        return self._result(out, n, sp.dtype)
+        return res, hist, n, sp.dtype
 
     @staticmethod
     def _result(out, n, dtype):

@@ -229,6 +229,20 @@ STB_API int stb_icp_estimate(const float *kcam, const float *src_points,
                      double *history, int32_t use_graph, void *stream);
 
 
+/*
+ * Measurement hook (no counterpart in the reference, which has no device
+ * timers).  stb_profile_enable(1) makes later stb_icp_estimate calls
+ * bracket every kernel launch with CUDA events on the launching stream
+ * (event nodes when the call replays a graph; graphs are cached separately
+ * for profiled and plain calls).  After the stream has completed,
+ * stb_profile_read() returns, for the most recent profiled call, the summed
+ * event time (ms) and launch count per kernel kind:
+ *   0 association, 1 reduction + solve, 2 information, 3 setup.
+ */
+STB_API int stb_profile_enable(int32_t on);
+STB_API int stb_profile_read(double *ms_by_kind, int64_t *launches_by_kind,
+                             int32_t num_kinds);
+
 /* ======================================================================= *
  * Frame preparation (inputs of every pyramid level)
  * ======================================================================= */

@@ -654,65 +654,87 @@ class Result:
         self.history = []
 
 
+def gn_step(T, kcam, src_points, src_normals, src_mask, tgt_points, tgt_normals,
+            tgt_mask, src_feats=None, tgt_feats=None, geom_weight=1.0, feat_weight=1.0,
+            distance_threshold=0.5, normals_angle_thresh=math.pi / 4,
+            feat_residual_thresh=2.75, channel_mode="last"):
+    """One Gauss-Newton iteration of ``ICPOdometry.estimate`` at pose ``T``
+    (icp.py:211-253): association at the float32 cast of ``T``, the
+    weighted normal equations (JtJ by w^2, Jtr by +w for the geometric and
+    -w for the feature term, residual by w; icp.py:216-235), the Cholesky
+    solve (icp.py:236-242) and the left update T <- exp(x) T
+    (icp.py:245-247).  Returns a dict; ``ok`` is False when the solve
+    failed (the reference's ``break``)."""
+    sp = np.asarray(src_points, dtype=F32).reshape(-1, 3)
+    sn = np.asarray(src_normals, dtype=F32).reshape(-1, 3)
+    sm = np.asarray(src_mask, dtype=bool).reshape(-1)
+    T = np.asarray(T, dtype=F64)
+    use_geom = geom_weight > 0
+    use_feat = feat_weight > 0 and src_feats is not None and tgt_feats is not None
+    rt = pose_rt32(T)
+    assoc = associate32(sp, sn, sm, rt, tgt_points, tgt_normals, tgt_mask, kcam,
+                        distance_threshold, normals_angle_thresh)
+    JtJ = np.zeros((6, 6))
+    Jr = np.zeros(6)
+    residual = 0.0
+    count = 0
+    scale = 0.0
+    geom_count = feat_count = 0
+    if use_feat:
+        f = feature_terms64(assoc, sp, src_feats, rt, tgt_feats, kcam,
+                            feat_residual_thresh, channel_mode)
+        JtJ = f.JtJ * feat_weight * feat_weight
+        Jr = f.Jtr * -feat_weight
+        residual = f.r2 * feat_weight
+        count = feat_count = f.count
+        scale += f.scale * feat_weight
+    if use_geom:
+        g = geometric_terms64(assoc, sp, rt, tgt_points, tgt_normals)
+        JtJ = JtJ + g.JtJ * geom_weight * geom_weight
+        Jr = Jr + g.Jtr * geom_weight
+        residual = residual + g.r2 * geom_weight
+        geom_count = g.count
+        count = max(g.count, count)
+        scale += g.scale * geom_weight
+    ok, update = cholesky_solve6(JtJ, Jr)
+    out = dict(ok=ok, JtJ=JtJ, Jr=Jr, r2=residual, count=count, geom_count=geom_count,
+               feat_count=feat_count, Jr_scale=scale, update=update, assoc=assoc)
+    if ok:
+        out["transform"] = se3_exp(update) @ T
+        out["residual"] = residual / count
+    return out
+
+
 def icp_estimate(kcam, src_points, src_normals, src_mask, tgt_points,
                  tgt_normals, tgt_mask, src_feats=None, tgt_feats=None,
                  num_iters=10, geom_weight=1.0, feat_weight=1.0,
                  distance_threshold=0.5, normals_angle_thresh=math.pi / 4,
                  feat_residual_thresh=2.75, transform=None,
                  channel_mode="last"):
-    """``ICPOdometry.estimate`` (icp.py:152-262) in float64 on the CPU.
-
-    The loop keeps the reference's weighting (JtJ by w^2, Jtr by +w for the
-    geometric and -w for the feature term, residual by w,
-    icp.py:216-235), the early exit when the Cholesky factorisation fails
-    (icp.py:236-242), the residual normalisation by the larger match count
-    (icp.py:235,253), the left update T <- exp(x) T (icp.py:245-247), and the
-    final information matrix at the last pose (icp.py:258-261)."""
+    """``ICPOdometry.estimate`` (icp.py:152-262) in float64 on the CPU:
+    ``gn_step`` until ``num_iters`` or a failed solve, then the information
+    matrix at the last pose (icp.py:258-261)."""
     sp = np.asarray(src_points, dtype=F32).reshape(-1, 3)
-    sn = np.asarray(src_normals, dtype=F32).reshape(-1, 3)
-    sm = np.asarray(src_mask, dtype=bool).reshape(-1)
     n = sp.shape[0]
     T = np.eye(4) if transform is None else np.asarray(transform, dtype=F64).copy()
-    use_geom = geom_weight > 0
-    use_feat = feat_weight > 0 and src_feats is not None and tgt_feats is not None
+    kw = dict(src_feats=src_feats, tgt_feats=tgt_feats, geom_weight=geom_weight,
+              feat_weight=feat_weight, distance_threshold=distance_threshold,
+              normals_angle_thresh=normals_angle_thresh,
+              feat_residual_thresh=feat_residual_thresh, channel_mode=channel_mode)
     res = Result()
     for _ in range(num_iters):
-        rt = pose_rt32(T)
-        assoc = associate32(sp, sn, sm, rt, tgt_points, tgt_normals, tgt_mask,
-                            kcam, distance_threshold, normals_angle_thresh)
-        JtJ = np.zeros((6, 6))
-        Jr = np.zeros(6)
-        residual = 0.0
-        count = 0
-        scale = 0.0
-        if use_feat:
-            f = feature_terms64(assoc, sp, src_feats, rt, tgt_feats, kcam,
-                                feat_residual_thresh, channel_mode)
-            JtJ = f.JtJ * feat_weight * feat_weight
-            Jr = f.Jtr * -feat_weight
-            residual = f.r2 * feat_weight
-            count = f.count
-            scale += f.scale * feat_weight
-        if use_geom:
-            g = geometric_terms64(assoc, sp, rt, tgt_points, tgt_normals)
-            JtJ = JtJ + g.JtJ * geom_weight * geom_weight
-            Jr = Jr + g.Jtr * geom_weight
-            residual = residual + g.r2 * geom_weight
-            count = max(g.count, count)
-            scale += g.scale * geom_weight
-        ok, update = cholesky_solve6(JtJ, Jr)
-        if not ok:
+        st = gn_step(T, kcam, sp, src_normals, src_mask, tgt_points, tgt_normals, tgt_mask,
+                     **kw)
+        if not st["ok"]:
             break
-        T = se3_exp(update) @ T
-        residual = residual / count
+        T = st["transform"]
         res.transform = T.copy()
-        res.JtJ = JtJ
-        res.residual = residual
-        res.match_ratio = count / n
-        res.history.append(dict(transform=T.copy(), JtJ=JtJ, Jr=Jr,
-                                residual=residual, count=count,
-                                update=update, Jr_scale=scale))
-    assoc = associate32(sp, sn, sm, pose_rt32(T), tgt_points, tgt_normals,
+        res.JtJ = st["JtJ"]
+        res.residual = st["residual"]
+        res.match_ratio = st["count"] / n
+        st.pop("assoc")
+        res.history.append(st)
+    assoc = associate32(sp, src_normals, src_mask, pose_rt32(T), tgt_points, tgt_normals,
                         tgt_mask, kcam, distance_threshold, normals_angle_thresh)
     res.information = information64(assoc, tgt_points)
     return res

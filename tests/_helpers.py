@@ -53,3 +53,49 @@ def pose_error(a, b):
     D = np.linalg.inv(np.asarray(a, dtype=np.float64)) @ np.asarray(b, dtype=np.float64)
     c = min(1.0, max(-1.0, (np.trace(D[:3, :3]) - 1.0) / 2.0))
     return float(np.linalg.norm(D[:3, 3])), math.acos(c)
+
+
+def rel_pose(a, b):
+    """||log(b^-1 a)|| / max(||log b||, 1e-3)."""
+    from oracle import icp_oracle as io
+    d = io.se3_log(np.linalg.inv(b) @ a)
+    return np.linalg.norm(d) / max(np.linalg.norm(io.se3_log(b)), 1e-3)
+
+
+def compare_forced(hist, d, x, kw, init=None, channel_mode="last", tol=1e-5):
+    """Teacher-forced comparison of a GPU history (``ICPOdometry.last_history``)
+    with the oracle's step evaluated at the GPU's previous pose; ``x`` holds
+    the device feature maps as used (``sf``/``tf``).  Returns the worst pose
+    error."""
+    from oracle import icp_oracle as io
+    from slamtb_gb300 import _native as N
+    s, t = d["src"], d["tgt"]
+    sf = x["sf"].float().cpu().numpy() if "sf" in x else None
+    tf = x["tf"].float().cpu().numpy() if "tf" in x else None
+    step_kw = {k: v for k, v in kw.items() if k != "num_iters"}
+    h = hist.numpy()
+    T_prev = np.eye(4) if init is None else np.asarray(init, dtype=np.float64)
+    worst = 0.0
+    for k in range(kw["num_iters"]):
+        g = h[k]
+        o = io.gn_step(T_prev, d["kcam"], s["points"], s["normals"], s["mask"], t["points"],
+                       t["normals"], t["mask"], src_feats=sf, tgt_feats=tf,
+                       channel_mode=channel_mode, **step_kw)
+        assert g[N.HIST_OK] == float(o["ok"]), k
+        if not o["ok"]:
+            break
+        assert g[N.HIST_GEOM_COUNT] == o["geom_count"], k
+        assert g[N.HIST_FEAT_COUNT] == o["feat_count"], k
+        A = g[N.HIST_JTJ:N.HIST_JTJ + 36].reshape(6, 6)
+        b = g[N.HIST_JR:N.HIST_JR + 6]
+        T = g[N.HIST_TRANSFORM:N.HIST_TRANSFORM + 16].reshape(4, 4)
+        assert np.linalg.norm(A - o["JtJ"]) <= tol * np.linalg.norm(o["JtJ"]), k
+        assert np.linalg.norm(b - o["Jr"]) <= tol * o["Jr_scale"], k
+        assert abs(g[N.HIST_R2] - o["r2"]) <= tol * o["r2"], k
+        err = rel_pose(T, o["transform"])
+        assert err <= tol, (k, err)
+        worst = max(worst, err)
+        T_prev = T
+    return worst
+
+

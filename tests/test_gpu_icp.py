@@ -1,16 +1,21 @@
 """Fused Gauss-Newton path (ICPOdometry -> stb_icp_estimate) against the
 FP64 oracle, iteration by iteration.
 
-Tolerances (the 1e-5 gate of the path):
+Each GPU iteration k is checked against the oracle's step evaluated at the
+GPU's own pose before that iteration (teacher forcing): with the same
+float32 pose the association is identical, so the match counts must be
+equal and the reduced terms and the updated pose are compared within the
+1e-5 gate:
   * J^T J: ||A_gpu - A_oracle||_F <= 1e-5 ||A_oracle||_F
   * J^T r: ||b_gpu - b_oracle||  <= 1e-5 sum_i |J_i||r_i|  (J^T r cancels
     towards 0 at convergence, so it is measured against the magnitude of
     its terms)
-  * pose after each iteration: ||log(T_oracle^-1 T_gpu)|| <= 1e-5 max(
-    ||log T_oracle||, 1e-3)
-  * match counts equal up to 1e-4 (the association is bit-exact for a given
-    float32 pose; the two loops cast their own FP64 poses, which can differ
-    in a last bit).
+  * pose: ||log(T_oracle^-1 T_gpu)|| <= 1e-5 max(||log T_oracle||, 1e-3)
+The geometric-only loop is also compared free-running (both loops from the
+same start), which it passes; with a feature term the per-pixel float32
+arithmetic (the reference's own) moves each update by ~1e-6 relative to the
+float64 oracle and feature-driven iterations can amplify that, so only the
+teacher-forced comparison is meaningful there.
 """
 import math
 
@@ -19,11 +24,11 @@ import pytest
 import torch
 
 from oracle import icp_oracle as io
-from _helpers import synthetic_pair, sample2_pair, pose_error, ANGLE_20
+from _helpers import synthetic_pair, sample2_pair, pose_error, ANGLE_20, compare_forced, rel_pose
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-5
+TOL = 1e-5  # the gate of the path
 
 
 def _dev(d, cuda, feats_dtype=torch.float32):
@@ -56,12 +61,8 @@ def _run_oracle(d, x, kw, transform=None, channel_mode="last"):
                            transform=transform, channel_mode=channel_mode, **kw)
 
 
-def _rel_pose(a, b):
-    d = io.se3_log(np.linalg.inv(b) @ a)
-    return np.linalg.norm(d) / max(np.linalg.norm(io.se3_log(b)), 1e-3)
-
-
 def _compare(hist, ores, check_counts=True):
+    """Free-running comparison of the GPU history with an oracle run."""
     from slamtb_gb300 import _native as N
     h = hist.numpy()
     assert len(ores.history) > 0
@@ -78,7 +79,7 @@ def _compare(hist, ores, check_counts=True):
             assert abs(gc - o["count"]) <= max(2, 1e-4 * o["count"]), (k, gc, o["count"])
         assert np.linalg.norm(A - o["JtJ"]) <= TOL * np.linalg.norm(o["JtJ"]), k
         assert np.linalg.norm(b - o["Jr"]) <= TOL * o["Jr_scale"], k
-        assert _rel_pose(T, o["transform"]) <= TOL, (k, _rel_pose(T, o["transform"]))
+        assert rel_pose(T, o["transform"]) <= TOL, (k, rel_pose(T, o["transform"]))
 
 
 GEOM = dict(num_iters=10, geom_weight=1.0, feat_weight=0.0, distance_threshold=0.1,
@@ -100,6 +101,7 @@ def test_geometric_matches_oracle_per_iteration(cuda, pair0, use_graph):
     ores = _run_oracle(pair0, x, GEOM)
     assert len(ores.history) == 10
     _compare(icp.last_history, ores)
+    compare_forced(icp.last_history, pair0, x, GEOM)
     assert abs(res.residual - ores.residual) <= TOL * ores.residual
     assert res.match_ratio == pytest.approx(ores.match_ratio, abs=0)
     np.testing.assert_allclose(res.information.double().numpy(), ores.information, rtol=1e-5)
@@ -112,7 +114,7 @@ def test_hybrid_matches_oracle_per_iteration(cuda, pair0):
     x = _dev(pair0, cuda)
     icp = ICPOdometry(record_history=True, **kw)
     _run_gpu(x, icp)
-    _compare(icp.last_history, _run_oracle(pair0, x, kw))
+    compare_forced(icp.last_history, pair0, x, kw)
 
 
 @pytest.mark.parametrize("mode", ["last", "sum"])
@@ -123,7 +125,7 @@ def test_bf16_multichannel_features(cuda, mode):
     x = _dev(d, cuda, torch.bfloat16)
     icp = ICPOdometry(record_history=True, feat_channel_mode=mode, **kw)
     _run_gpu(x, icp)
-    _compare(icp.last_history, _run_oracle(d, x, kw, channel_mode=mode))
+    compare_forced(icp.last_history, d, x, kw, channel_mode=mode)
 
 
 def test_feature_only_and_initial_transform(cuda):
@@ -135,7 +137,7 @@ def test_feature_only_and_initial_transform(cuda):
     x = _dev(d, cuda)
     icp = ICPOdometry(record_history=True, **kw)
     _run_gpu(x, icp, transform=torch.from_numpy(init))
-    _compare(icp.last_history, _run_oracle(d, x, kw, transform=init))
+    compare_forced(icp.last_history, d, x, kw, init=init)
 
 
 def test_deterministic_and_graph_equals_direct(cuda, pair0):
@@ -172,8 +174,7 @@ def test_sample2_known_answer(cuda):
               normals_angle_thresh=math.pi / 4)
     icp = ICPOdometry(record_history=True, **kw)
     res = _run_gpu(x, icp)
-    ores = _run_oracle(d, x, kw)
-    _compare(icp.last_history, ores)
+    compare_forced(icp.last_history, d, x, kw)
     _, gt_r = pose_error(np.eye(4), d["gt"])
     err_t, err_r = pose_error(res.transform.numpy(), d["gt"])
     assert err_r < 0.1 * gt_r and err_t < 1e-3
