@@ -792,3 +792,176 @@ extern "C" int stb_profile_read(double *ms_by_kind, int64_t *launches_by_kind,
   }
   return STB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Registration without any allocation: the same launch sequence as
+// stb_icp_estimate, with its scratch in a fixed device array.
+//
+// Who needs it: callers that cannot call cudaMalloc while they track --
+// hosts that bind the C ABI from a runtime without a CUDA allocator of its
+// own (a plain C or FFI host, no torch caching allocator to borrow from),
+// and applications that fix their device-memory budget at start-up and
+// forbid later allocations (cudaMalloc and cudaFree synchronise the device,
+// which stalls a real-time tracking loop sharing the GPU).
+//
+// The scratch is kStaticMaxPixels target pixels' worth (about 8.6 MB) in
+// g_static_workspace, which every GPU that loads this library holds until
+// the process exits.  The first call on a device looks up the array's device
+// address with cudaGetSymbolAddress (host code cannot use the symbol itself:
+// it names a host-side stand-in); make that first call before any stream
+// capture.  All calls share the one array: two calls whose work overlaps on
+// the GPU race and corrupt each other.  What must start cleared is cleared by
+// every call (the key map and the per-call state), the rest is written
+// before it is read.
+// ---------------------------------------------------------------------------
+namespace stb {
+namespace {
+
+constexpr int64_t kStaticMaxPixels = 1 << 20;  // e.g. 1280x720 fits
+constexpr size_t kStaticWorkspaceBytes =
+    2 * kSlot + 2 * ((sizeof(float) * kAccs * ((kStaticMaxPixels + 1023) / 1024) + 255) & ~size_t(255)) +
+    sizeof(unsigned long long) * kStaticMaxPixels;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_workspace[kStaticWorkspaceBytes];
+
+std::mutex g_static_mutex;
+void *g_static_ptr[kMaxDevices] = {};
+
+// Device address of g_static_workspace on the current device (looked up
+// once per device).
+int static_workspace(void **out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return fail(STB_ECUDA, "Cuda call error stb_icp_estimate_static: no usable device");
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_ptr[dev]) {
+    void *p = nullptr;
+    const cudaError_t err = cudaGetSymbolAddress(&p, g_static_workspace);
+    if (err != cudaSuccess || !p)
+      return fail(STB_ECUDA, "Cuda call error stb_icp_estimate_static "
+                  "(cudaGetSymbolAddress): %s", cudaGetErrorString(err));
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return STB_OK;
+}
+
+}  // namespace
+}  // namespace stb
+
+extern "C" int stb_icp_estimate_static(
+    const float *kcam, const float *src_points, const float *src_normals,
+    const uint8_t *src_mask, int64_t num_source, const void *src_feats,
+    const float *tgt_points, const float *tgt_normals, const uint8_t *tgt_mask,
+    int32_t height, int32_t width, const void *tgt_feats, int32_t channels,
+    int32_t feat_dtype, const double *init_transform, int32_t num_iters,
+    double geom_weight, double feat_weight, double distance_thresh,
+    double normal_angle_thresh, double feat_residual_thresh, int32_t channel_mode,
+    double *result, double *history, void *stream) {
+  clear_error();
+  if (height <= 0 || width <= 0)
+    return fail(STB_EINVAL, "Check failed: target size must be positive, got %dx%d",
+                height, width);
+  const int64_t npix = (int64_t)height * width;
+  if (npix > kStaticMaxPixels)
+    return fail(STB_EINVAL,
+                "Check failed: stb_icp_estimate_static handles at most %lld target pixels "
+                "(its fixed scratch), got %dx%d = %lld; use stb_icp_estimate with a "
+                "caller-provided workspace", (long long)kStaticMaxPixels, height, width,
+                (long long)npix);
+  if (num_source < 0 || (unsigned long long)num_source >= kMaxSources)
+    return fail(STB_EINVAL, "Check failed: num_source must be in [0, 2^24), got %lld",
+                (long long)num_source);
+  if (num_iters < 0 || num_iters > 254)
+    return fail(STB_EINVAL, "Check failed: num_iters must be in [0, 254], got %d", num_iters);
+  const bool use_feat = feat_weight > 0.0 && src_feats && tgt_feats;
+  const bool use_geom = geom_weight > 0.0;
+  if (use_feat) {
+    if (channels <= 0)
+      return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
+    if (feat_dtype != STB_F32 && feat_dtype != STB_BF16)
+      return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
+    if (channel_mode != 0 && channel_mode != 1)
+      return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
+  }
+  STB_TRY(check_device_ptr(kcam, "kcam"));
+  STB_TRY(check_device_ptr(src_points, "src_points"));
+  STB_TRY(check_device_ptr(src_normals, "src_normals"));
+  STB_TRY(check_device_ptr(src_mask, "src_mask"));
+  STB_TRY(check_device_ptr(tgt_points, "tgt_points"));
+  STB_TRY(check_device_ptr(tgt_normals, "tgt_normals"));
+  STB_TRY(check_device_ptr(tgt_mask, "tgt_mask"));
+  if (use_feat) {
+    STB_TRY(check_device_ptr(src_feats, "src_feats"));
+    STB_TRY(check_device_ptr(tgt_feats, "tgt_feats"));
+  }
+  STB_TRY(check_device_ptr(init_transform, "transform", true));
+  STB_TRY(check_device_ptr(result, "result"));
+  STB_TRY(check_device_ptr(history, "history", true));
+  void *workspace = nullptr;
+  STB_TRY(static_workspace(&workspace));
+
+  char *ws = static_cast<char *>(workspace);
+  Plan p;
+  p.n = num_source;
+  p.H = height;
+  p.W = width;
+  p.C = use_feat ? channels : 0;
+  p.dtype = use_feat ? feat_dtype : 0;
+  p.iters = num_iters;
+  p.use_geom = use_geom;
+  p.use_feat = use_feat;
+  p.channel_mode = use_feat ? channel_mode : 0;
+  p.nblocks = reduce_blocks(npix);
+  p.job_dev = reinterpret_cast<Job *>(ws);
+
+  Job job;
+  job.kcam = kcam;
+  job.sp = src_points;
+  job.sn = src_normals;
+  job.sm = src_mask;
+  job.n = num_source;
+  job.sf = src_feats;
+  job.tp = tgt_points;
+  job.tn = tgt_normals;
+  job.tm = tgt_mask;
+  job.H = height;
+  job.W = width;
+  job.tf = tgt_feats;
+  job.C = p.C;
+  job.dtype = p.dtype;
+  job.init = init_transform;
+  job.iters = num_iters;
+  job.channel_mode = p.channel_mode;
+  job.use_geom = use_geom;
+  job.use_feat = use_feat;
+  job.wg1 = (float)geom_weight;
+  job.wg2 = (float)(geom_weight * geom_weight);
+  job.wf1 = (float)feat_weight;
+  job.wf2 = (float)(feat_weight * feat_weight);
+  job.thr2 = distance_thresh_sq(distance_thresh);
+  job.cos_max = angle_cos_max(normal_angle_thresh);
+  {
+    const float t = (float)feat_residual_thresh;
+    job.feat_thr2 = t * t;
+  }
+  job.result = result;
+  job.history = history;
+  size_t off = 2 * kSlot;
+  job.state = reinterpret_cast<State *>(ws + kSlot);
+  job.part_s = reinterpret_cast<float *>(ws + off);
+  off += align256(sizeof(float) * kAccs * p.nblocks);
+  job.part_c = reinterpret_cast<float *>(ws + off);
+  off += align256(sizeof(float) * kAccs * p.nblocks);
+  job.keys = reinterpret_cast<unsigned long long *>(ws + off);
+  job.nblocks = p.nblocks;
+  p.keys = job.keys;
+  if (off + sizeof(unsigned long long) * (size_t)npix > kStaticWorkspaceBytes)
+    return fail(STB_EINVAL, "Check failed: stb_icp_estimate_static scratch too small");
+
+  // Direct launches only: no graph, no stream and no event is created here.
+  const cudaStream_t st = as_stream(stream);
+  launch_setup(p, job, st, nullptr);
+  return launch_body(p, st, nullptr);
+}

@@ -47,6 +47,9 @@ _SIGNATURES = {
     "stb_icp_information_partials": (ctypes.c_int, [
         _vp, _vp, _i64, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
     "stb_icp_workspace_bytes": (_sz, [_i64, _i32, _i32]),
+    "stb_icp_estimate_static": (ctypes.c_int, [
+        _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _i32,
+        _i32, _vp, _i32, _f64, _f64, _f64, _f64, _f64, _i32, _vp, _vp, _vp]),
     "stb_profile_enable": (ctypes.c_int, [_i32]),
     "stb_profile_read": (ctypes.c_int, [ctypes.POINTER(_f64), ctypes.POINTER(_i64), _i32]),
     "stb_depth_to_points": (ctypes.c_int, [_vp, _f32, _f32, _vp, _vp, _vp, _i32, _i32, _vp]),

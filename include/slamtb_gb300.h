@@ -230,6 +230,30 @@ STB_API int stb_icp_estimate(const float *kcam, const float *src_points,
 
 
 /*
+ * stb_icp_estimate without any allocation.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc while they track -- C or
+ * FFI hosts with no CUDA allocator of their own, and applications that fix
+ * their device-memory budget at start-up (cudaMalloc / cudaFree synchronise
+ * the device and would stall a real-time loop).  The scratch is a fixed
+ * device array inside the library, sized for at most 1,048,576 target
+ * pixels (height * width; about 8.6 MB, held by every GPU that loads the
+ * library until the process exits); larger frames are rejected with
+ * STB_EINVAL.  The first call on a device looks up that array's address
+ * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
+ * uses the same array: calls whose work overlaps on the GPU race.  Same
+ * arguments and results as stb_icp_estimate, minus workspace and graphs.
+ */
+STB_API int stb_icp_estimate_static(
+    const float *kcam, const float *src_points, const float *src_normals,
+    const uint8_t *src_mask, int64_t num_source, const void *src_feats,
+    const float *tgt_points, const float *tgt_normals, const uint8_t *tgt_mask,
+    int32_t height, int32_t width, const void *tgt_feats, int32_t channels,
+    int32_t feat_dtype, const double *init_transform, int32_t num_iters,
+    double geom_weight, double feat_weight, double distance_thresh,
+    double normal_angle_thresh, double feat_residual_thresh, int32_t channel_mode,
+    double *result, double *history, void *stream);
+
+/*
  * Measurement hook (no counterpart in the reference, which has no device
  * timers).  stb_profile_enable(1) makes later stb_icp_estimate calls
  * bracket every kernel launch with CUDA events on the launching stream
