@@ -129,3 +129,146 @@ __host__ __device__ constexpr int upper_index(int a, int b) {
 }
 
 }  // namespace stb
+
+// ---------------------------------------------------------------------------
+// Warp-parallel FP64 Gauss-Newton step.  FP64 latency is ~66 cycles per
+// dependent operation on this part, so the step is laid out to keep the
+// dependent chain short: lanes 0..5 hold the rows of the 6x6 system
+// (right-looking Cholesky, pivot reciprocals by Newton-Raphson on the
+// float32 rsqrt), divisions by constants are multiplications by
+// reciprocals, and matrix products run one entry per lane.
+// ---------------------------------------------------------------------------
+namespace stb {
+
+// 1/sqrt(d) for d > 0: float32 seed, two Newton-Raphson steps in FP64
+// (y <- y + y/2 (1 - d y^2); each step doubles the correct bits: 2^-22 ->
+// 2^-44 -> full double).  Seeds outside the float32 range fall back to the
+// library call.
+__device__ __forceinline__ double rsqrt_fp64(double d) {
+  const float f = (float)d;
+  if (!(f > 1e-37f && f < 1e37f)) return 1.0 / sqrt(d);
+  double y = (double)rsqrtf(f);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const double e = fma(-d, y * y, 1.0);
+    y = fma(0.5 * y, e, y);
+  }
+  return y;
+}
+
+// SE(3) exponential like se3_exp, entries spread over the warp.  All lanes
+// call it with the same xi; every lane returns the full E (row-major 4x4)
+// via shared memory `E` (16 doubles).
+__device__ inline void warp_se3_exp(const double *xi, double *E, int lane) {
+  const double wx = xi[3], wy = xi[4], wz = xi[5];
+  const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
+  double A, B, C;
+  if (t2 < 1e-4) {
+    const double t4 = t2 * t2, t6 = t4 * t2;
+    A = fma(t6, -1.0 / 5040.0, fma(t4, 1.0 / 120.0, fma(t2, -1.0 / 6.0, 1.0)));
+    B = fma(t6, -1.0 / 40320.0, fma(t4, 1.0 / 720.0, fma(t2, -1.0 / 24.0, 0.5)));
+    C = fma(t6, -1.0 / 362880.0, fma(t4, 1.0 / 5040.0, fma(t2, -1.0 / 120.0, 1.0 / 6.0)));
+  } else {
+    const double t = sqrt(t2);
+    double s, c;
+    sincos(t, &s, &c);
+    const double it = 1.0 / t, it2 = it * it;
+    A = s * it;
+    B = (1.0 - c) * it2;
+    C = (t - s) * (it2 * it);
+  }
+  if (lane < 12) {
+    const int i = lane >> 2, j = lane & 3;
+    const double w[3] = {wx, wy, wz};
+    // W = hat(w): W[i][k] = -eps_ikm w_m ; W2 = w w^T - |w|^2 I
+    if (j < 3) {
+      const double Wij = (i == j) ? 0.0 : ((j == (i + 1) % 3) ? -w[(i + 2) % 3] : w[(i + 1) % 3]);
+      const double W2ij = w[i] * w[j] - ((i == j) ? t2 : 0.0);
+      E[i * 4 + j] = ((i == j) ? 1.0 : 0.0) + A * Wij + B * W2ij;
+    } else {
+      // t_i = sum_k (I + B W + C W^2)_ik v_k
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const double Wik = (i == k) ? 0.0 : ((k == (i + 1) % 3) ? -w[(i + 2) % 3] : w[(i + 1) % 3]);
+        const double W2ik = w[i] * w[k] - ((i == k) ? t2 : 0.0);
+        acc = fma(((i == k) ? 1.0 : 0.0) + B * Wik + C * W2ik, xi[k], acc);
+      }
+      E[i * 4 + 3] = acc;
+    }
+  } else if (lane < 16) {
+    E[lane] = (lane == 15) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+}
+
+// 6x6 Cholesky solve A x = b by one warp.  A: 36 doubles (row-major, full
+// symmetric), b: 6 doubles, x: 6 doubles out; all in shared memory.  Returns
+// the LAPACK potrf verdict (false when a pivot is not > 0 or NaN), uniform
+// across the warp.
+__device__ inline bool warp_cholesky_solve6(const double *A, const double *b, double *x,
+                                            double *L /* 36 doubles scratch */, int lane) {
+  const unsigned full = 0xffffffffu;
+  const int i = lane < 6 ? lane : 5;
+  double row[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) row[k] = A[i * 6 + k];
+  double inv[6];
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const double d = __shfl_sync(full, row[j], j);
+    ok = ok && (d > 0.0);
+    if (!ok) break;
+    inv[j] = rsqrt_fp64(d);
+    // column j of L: L[i][j] = A'[i][j] / sqrt(d) for i >= j
+    if (i >= j) row[j] *= inv[j];
+    // trailing update A'[i][k] -= L[i][j] L[k][j] for k > j
+#pragma unroll
+    for (int k = j + 1; k < 6; ++k) {
+      const double lkj = __shfl_sync(full, row[j], k);
+      if (i >= k) row[k] = fma(-row[j], lkj, row[k]);
+    }
+  }
+  if (!ok) return false;
+  if (lane < 6) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) L[lane * 6 + k] = (k <= lane) ? row[k] : 0.0;
+  }
+  __syncwarp();
+  // forward: L y = b (lane i owns y_i / b_i)
+  double yi = lane < 6 ? b[lane] : 0.0;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const double yj = __shfl_sync(full, yi * inv[j], j);
+    if (lane == j) yi = yj;
+    if (lane > j && lane < 6) yi = fma(-L[lane * 6 + j], yj, yi);
+  }
+  // backward: L^T x = y
+  double xi = yi;
+#pragma unroll
+  for (int j = 5; j >= 0; --j) {
+    const double xj = __shfl_sync(full, xi * inv[j], j);
+    if (lane == j) xi = xj;
+    if (lane < j) xi = fma(-L[j * 6 + lane], xj, xi);
+  }
+  if (lane < 6) x[lane] = xi;
+  __syncwarp();
+  return true;
+}
+
+// Out = E * T (rigid 4x4, row-major) by one warp: lane = entry of the 3x4.
+__device__ inline void warp_compose(const double *E, const double *T, double *Out, int lane) {
+  if (lane < 12) {
+    const int i = lane >> 2, j = lane & 3;
+    double s = fma(E[i * 4 + 0], T[0 * 4 + j],
+                   fma(E[i * 4 + 1], T[1 * 4 + j], E[i * 4 + 2] * T[2 * 4 + j]));
+    if (j == 3) s += E[i * 4 + 3];
+    Out[lane] = s;
+  } else if (lane < 16) {
+    Out[lane] = (lane == 15) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+}
+
+}  // namespace stb

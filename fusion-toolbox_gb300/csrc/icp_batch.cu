@@ -1,0 +1,946 @@
+// Batched multiscale ICP in one persistent cooperative kernel.
+//
+// All frame pairs run the same schedule (levels coarsest first, each level's
+// Gauss-Newton iterations), so the whole batch advances in lock step through
+// phases separated by grid barriers:
+//
+//   A  association   -- work list of source tiles over all pairs; one
+//                       thread per source point, float32 gates in the
+//                       reference's operation order, 64-bit atomicMin of
+//                       (epoch tag, distance, index) into the pair's key map
+//   B  reduction     -- work list of target tiles over all pairs; one thread
+//                       per target pixel, residuals and Jacobians summed in
+//                       compensated float32 into a per-tile partial; the last
+//                       tile of a group of 32 folds the group, the last group
+//                       of a pair folds the pair and its warp 0 runs the FP64
+//                       Cholesky solve, SE(3) exponential and pose update
+//
+// After the last level, one more association at the final pose feeds the
+// information-matrix reduction.  Barriers spin with a bound; a barrier that
+// waits too long flags STB_ST_TIMEOUT and every block returns.
+//
+// Reference: MultiscaleRegistration.estimate_frame
+// (slamtb/registration/multiscale.py:30-67) over ICPOdometry.estimate
+// (slamtb/registration/icp.py:152-262) for each pair.
+#include <math.h>
+
+#include "gn_solve.cuh"
+#include "stb_common.cuh"
+#include "stb_host.hpp"
+
+namespace stb {
+
+float distance_thresh_sq(double d);
+float angle_cos_max(double angle);
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMaxLevels = 4;
+constexpr int kGroup = 32;            // tiles per first-level reduction group
+constexpr int kAccsB = 30;            // 21 JtJ + 6 Jr + r2 + count_geom + count_feat
+constexpr int kSlotFloats = 64;       // (s[32], c[32]) per partial slot
+constexpr int kMinTile = kThreads * 2;
+constexpr unsigned kSpinLimit = 1u << 26;  // x >= 32 ns sleeps: a few seconds
+constexpr int kJrB = 21, kR2B = 27, kCountGeomB = 28, kCountFeatB = 29;
+
+struct LevelP {
+  int iters, use_geom, use_feat;
+  float wg1, wg2, wf1, wf2, thr2, cos_max, feat_thr2;
+};
+
+struct PairState {
+  double T[16];
+  Pose32 pose;
+  unsigned stopped, status;
+  int level_iters, iters_done;
+};
+
+struct BatchArgs {
+  const stb_level *levels;
+  int B, L, C, dtype, mode, total_iters;
+  int tile;  // pixels per work item: a multiple of kMinTile
+  LevelP lp[kMaxLevels];
+  const double *init;
+  double *results, *history;
+  unsigned *sync;  // [0] arrivals, [1] generation, [2] error
+  PairState *ps;
+  long long *key_off;   // [B + 1]
+  long long *src_off;   // [L][B + 1] source tiles
+  long long *tgt_off;   // [L][B + 1] target tiles
+  long long *grp_off;   // [L][B + 1] groups
+  unsigned *grp_ticket, *pair_ticket;
+  float *tile_part, *grp_part;
+  unsigned long long *keys;
+  long long keys_cap, tiles_cap, groups_cap;
+};
+
+__host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct Layout {
+  size_t sync, ps, key_off, src_off, tgt_off, grp_off, grp_ticket, pair_ticket, tile_part,
+      grp_part, keys, total;
+  long long tiles_cap, groups_cap;
+};
+
+inline Layout layout(int B, long long total_pixels) {
+  Layout l;
+  l.tiles_cap = total_pixels / kMinTile + B;
+  l.groups_cap = l.tiles_cap / kGroup + B;
+  size_t o = 0;
+  l.sync = o;
+  o += 256;
+  l.ps = o;
+  o += al256(sizeof(PairState) * (size_t)B);
+  l.key_off = o;
+  o += al256(sizeof(long long) * (B + 1));
+  l.src_off = o;
+  o += al256(sizeof(long long) * kMaxLevels * (B + 1));
+  l.tgt_off = o;
+  o += al256(sizeof(long long) * kMaxLevels * (B + 1));
+  l.grp_off = o;
+  o += al256(sizeof(long long) * kMaxLevels * (B + 1));
+  l.grp_ticket = o;
+  o += al256(sizeof(unsigned) * (size_t)l.groups_cap);
+  l.pair_ticket = o;
+  o += al256(sizeof(unsigned) * (size_t)B);
+  l.tile_part = o;
+  o += al256(sizeof(float) * kSlotFloats * (size_t)l.tiles_cap);
+  l.grp_part = o;
+  o += al256(sizeof(float) * kSlotFloats * (size_t)l.groups_cap);
+  l.keys = o;
+  o += al256(sizeof(unsigned long long) * (size_t)total_pixels);
+  l.total = o;
+  return l;
+}
+
+// ---------------------------------------------------------------------------
+// grid barrier with a bounded wait
+// ---------------------------------------------------------------------------
+__device__ bool grid_sync(unsigned *sync) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *vgen = sync + 1;
+    volatile unsigned *verr = sync + 2;
+    const unsigned gen = *vgen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(sync, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(sync, 0u);
+      __threadfence();
+      atomicAdd(sync + 1, 1u);
+    } else {
+      unsigned spins = 0;
+      while (*vgen == gen) {
+        if (*verr) break;
+        if (++spins > kSpinLimit) {
+          atomicOr(sync + 2, 1u);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    s_ok = (*verr == 0);
+  }
+  __syncthreads();
+  return s_ok;
+}
+
+constexpr int kStageOff = 1025;  // offsets staged in shared memory up to 1024 pairs
+
+// Entry k of an offset row: a plain (shared-memory) load when the row was
+// staged, an L2 load (coherent with other blocks' writes) when it was not.
+__device__ __forceinline__ long long off_at(const long long *off, int B, long long k) {
+  return (B + 1 <= kStageOff) ? off[k] : __ldcg(off + k);
+}
+
+// Pair owning work item t: off[lo] <= t < off[lo + 1].
+__device__ __forceinline__ int find_pair(const long long *off, int B, long long t) {
+  int lo = 0, hi = B;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off_at(off, B, mid) <= t)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Copies one level's offset row to shared memory (when it fits) and returns
+// the array the phase should search.
+__device__ __forceinline__ const long long *stage_offsets(const long long *row, int B,
+                                                          long long *smem) {
+  __syncthreads();
+  if (B + 1 > kStageOff) return row;
+  for (int k = threadIdx.x; k <= B; k += blockDim.x) smem[k] = __ldcg(row + k);
+  __syncthreads();
+  return smem;
+}
+
+__device__ __forceinline__ unsigned btag(int s) { return 254u - (unsigned)s; }
+
+// Block-wide exclusive scans of the per-pair tile counts (block 0).
+__device__ void build_offsets(const BatchArgs &a) {
+  __shared__ long long carry[5];
+  __shared__ long long warp_sum[kThreads / 32][5];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int l = 0; l < a.L; ++l) {
+    if (threadIdx.x < 5) carry[threadIdx.x] = 0;
+    __syncthreads();
+    for (int base = 0; base < a.B; base += kThreads) {
+      const int p = base + threadIdx.x;
+      long long v[4] = {0, 0, 0, 0};
+      if (p < a.B) {
+        const stb_level lv = a.levels[(size_t)p * a.L + l];
+        const long long npix = (long long)lv.height * lv.width;
+        const long long tt = (npix + a.tile - 1) / a.tile;
+        v[0] = (lv.num_source + a.tile - 1) / a.tile;  // source tiles
+        v[1] = tt;                                         // target tiles
+        v[2] = (tt + kGroup - 1) / kGroup;                 // groups
+        if (l == a.L - 1) {  // key map: the pair's largest level
+          long long m = 0;
+          for (int k = 0; k < a.L; ++k) {
+            const stb_level lk = a.levels[(size_t)p * a.L + k];
+            m = max(m, (long long)lk.height * lk.width);
+          }
+          v[3] = m;
+        }
+      }
+      // inclusive warp scans
+      long long inc[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        inc[q] = v[q];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const long long n = __shfl_up_sync(0xffffffffu, inc[q], off);
+          if (lane >= off) inc[q] += n;
+        }
+      }
+      if (lane == 31)
+        for (int q = 0; q < 4; ++q) warp_sum[warp][q] = inc[q];
+      __syncthreads();
+      if (p < a.B) {
+        long long pre[4];
+        for (int q = 0; q < 4; ++q) {
+          pre[q] = carry[q] + inc[q] - v[q];
+          for (int w = 0; w < warp; ++w) pre[q] += warp_sum[w][q];
+        }
+        const size_t row = (size_t)l * (a.B + 1);
+        a.src_off[row + p] = pre[0];
+        a.tgt_off[row + p] = pre[1];
+        a.grp_off[row + p] = pre[2];
+        if (l == a.L - 1) a.key_off[p] = pre[3];
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        for (int q = 0; q < 4; ++q) {
+          long long tot = 0;
+          for (int w = 0; w < kThreads / 32; ++w) tot += warp_sum[w][q];
+          carry[q] += tot;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      const size_t row = (size_t)l * (a.B + 1);
+      a.src_off[row + a.B] = carry[0];
+      a.tgt_off[row + a.B] = carry[1];
+      a.grp_off[row + a.B] = carry[2];
+      if (l == a.L - 1) a.key_off[a.B] = carry[3];
+      if (carry[1] > a.tiles_cap || carry[2] > a.groups_cap ||
+          (l == a.L - 1 && carry[3] > a.keys_cap))
+        atomicOr(a.sync + 2, 2u);
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ float bilin(const T *__restrict__ f, int H, int W, float u, float v) {
+  const int ui = (int)u, vi = (int)v;
+  const float ur = fsub(u, (float)ui), vr = fsub(v, (float)vi);
+  const float v00 = load_feat(f + (int64_t)vi * W + ui);
+  const float v10 = (ui + 1 < W) ? load_feat(f + (int64_t)vi * W + ui + 1) : 0.f;
+  const float v01 = (vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui) : 0.f;
+  const float v11 =
+      (ui + 1 < W && vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui + 1) : 0.f;
+  const float a0 = fadd(fmul(v00, fsub(1.f, ur)), fmul(v10, ur));
+  const float a1 = fadd(fmul(v01, fsub(1.f, ur)), fmul(v11, ur));
+  return fadd(fmul(a0, fsub(1.f, vr)), fmul(a1, vr));
+}
+
+__device__ __forceinline__ void acc_se3(CSum *acc, const float *Jv, float r, float w1,
+                                        float w2) {
+#pragma unroll
+  for (int a = 0; a < 6; ++a)
+#pragma unroll
+    for (int b = a; b < 6; ++b) csum_add(acc[upper_index(a, b)], w2 * (Jv[a] * Jv[b]));
+#pragma unroll
+  for (int a = 0; a < 6; ++a) csum_add(acc[kJrB + a], w1 * (Jv[a] * r));
+}
+
+// block reduction of kN accumulators into smem out_s/out_c (threads < kN)
+template <int kN>
+__device__ __forceinline__ void block_sum(CSum *acc, float *out_s, float *out_c) {
+  __shared__ float ws[kThreads / 32][kN][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int a = 0; a < kN; ++a) {
+    csum_warp_reduce(acc[a]);
+    if (lane == 0) {
+      ws[warp][a][0] = acc[a].s;
+      ws[warp][a][1] = acc[a].c;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < kN) {
+    CSum t = {0.f, 0.f};
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w)
+      csum_merge(t, ws[w][threadIdx.x][0], ws[w][threadIdx.x][1]);
+    out_s[threadIdx.x] = t.s;
+    out_c[threadIdx.x] = t.c;
+  }
+  __syncthreads();
+}
+
+// Fold `count` partial slots (kN accumulators each) into out_s/out_c.  All
+// loads are issued before the additions.
+template <int kN>
+__device__ __forceinline__ void fold_slots(const float *slots, int count, float *out_s,
+                                           float *out_c) {
+  __shared__ float fs[kThreads / 32][32][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // thread (warp w, lane a) sums slots w, w + 8, ... for accumulator a
+  CSum t = {0.f, 0.f};
+  if (lane < kN) {
+    float vs[4], vc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int j = warp + k * (kThreads / 32);
+      vs[k] = (j < count) ? __ldcg(slots + (size_t)j * kSlotFloats + lane) : 0.f;
+      vc[k] = (j < count) ? __ldcg(slots + (size_t)j * kSlotFloats + 32 + lane) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) csum_merge(t, vs[k], vc[k]);
+  }
+  fs[warp][lane][0] = t.s;
+  fs[warp][lane][1] = t.c;
+  __syncthreads();
+  if (threadIdx.x < kN) {
+    CSum u = {0.f, 0.f};
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) csum_merge(u, fs[w][threadIdx.x][0], fs[w][threadIdx.x][1]);
+    out_s[threadIdx.x] = u.s;
+    out_c[threadIdx.x] = u.c;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void load_pose(Pose32 &P, const PairState *ps) {
+  const float *src = reinterpret_cast<const float *>(&ps->pose);
+  float *dst = reinterpret_cast<float *>(&P);
+  for (int k = threadIdx.x; k < (int)(sizeof(Pose32) / sizeof(float)); k += blockDim.x)
+    dst[k] = __ldcg(src + k);
+}
+
+// Per-block cache of the pair a work item belongs to: consecutive work items
+// of a block usually share the pair, so its descriptor and pose are loaded
+// once per phase, not once per item.
+struct TileCache {
+  stb_level lv;
+  Pose32 P;
+  int p, skip;
+};
+
+__device__ __forceinline__ void reset_cache(TileCache &tc) {
+  __syncthreads();
+  if (threadIdx.x == 0) tc.p = -1;
+  __syncthreads();
+}
+
+// Resolves work item t (thread 0), reloading descriptor and pose when the
+// pair changes.  Returns the pair; tc.skip is uniform.
+__device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *off, int level,
+                                          long long t, bool check_stop, TileCache &tc) {
+  __shared__ int s_new;
+  // every thread is done with the previous work item before the cache and
+  // the shared flags are rewritten
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int p = find_pair(off, a.B, t);
+    s_new = (p != tc.p);
+    if (s_new) {
+      tc.p = p;
+      tc.lv = a.levels[(size_t)p * a.L + level];
+      tc.skip = check_stop && __ldcg(&a.ps[p].stopped);
+    }
+  }
+  __syncthreads();
+  if (s_new && !tc.skip) {
+    load_pose(tc.P, a.ps + tc.p);
+    __syncthreads();
+  }
+  return tc.p;
+}
+
+// ---------------------------------------------------------------------------
+// phase A: association of one source tile
+// ---------------------------------------------------------------------------
+constexpr int kChunk = 2;  // points / pixels per thread per pipelined chunk
+
+__device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *off, int level,
+                                           long long t, int s, bool force, TileCache &tc) {
+  const int p = cache_pair(a, off, level, t, !force, tc);
+  if (tc.skip) return;
+  const Pose32 &P = tc.P;
+  const stb_level &lv = tc.lv;
+  const long long lt = t - off_at(off, a.B, p);
+  const LevelP &q = a.lp[level];
+  const int H = lv.height, W = lv.width;
+  unsigned long long *keys = a.keys + __ldcg(a.key_off + p);
+  const unsigned long long tag = (unsigned long long)btag(s) << 56;
+  const long long end = min((lt + 1) * (long long)a.tile, (long long)lv.num_source);
+  for (long long base = lt * (long long)a.tile; base < end; base += kThreads * kChunk) {
+    // round 1: source loads
+    float px[kChunk], py[kChunk], pz[kChunk], nx[kChunk], ny[kChunk], nz[kChunk];
+    bool ok[kChunk];
+    long long idx[kChunk];
+#pragma unroll
+    for (int k = 0; k < kChunk; ++k) {
+      idx[k] = base + k * kThreads + threadIdx.x;
+      ok[k] = idx[k] < end;
+      const long long i = ok[k] ? idx[k] : 0;
+      ok[k] = ok[k] && __ldg(lv.src_mask + i);
+      px[k] = __ldg(lv.src_points + 3 * i);
+      py[k] = __ldg(lv.src_points + 3 * i + 1);
+      pz[k] = __ldg(lv.src_points + 3 * i + 2);
+      nx[k] = __ldg(lv.src_normals + 3 * i);
+      ny[k] = __ldg(lv.src_normals + 3 * i + 1);
+      nz[k] = __ldg(lv.src_normals + 3 * i + 2);
+    }
+    // round 2: projection and target gathers
+    float3 Tp[kChunk];
+    long long pix[kChunk];
+    float qx[kChunk], qy[kChunk], qz[kChunk], mx[kChunk], my[kChunk], mz[kChunk];
+#pragma unroll
+    for (int k = 0; k < kChunk; ++k) {
+      Tp[k] = transform_point(P.rt, px[k], py[k], pz[k]);
+      float u, v;
+      project(P, Tp[k], u, v);
+      int ui = 0, vi = 0;
+      ok[k] = ok[k] && round_in(u, W, ui) && round_in(v, H, vi);
+      pix[k] = ok[k] ? (long long)vi * W + ui : 0;
+      ok[k] = ok[k] && __ldg(lv.tgt_mask + pix[k]);
+      qx[k] = __ldg(lv.tgt_points + 3 * pix[k]);
+      qy[k] = __ldg(lv.tgt_points + 3 * pix[k] + 1);
+      qz[k] = __ldg(lv.tgt_points + 3 * pix[k] + 2);
+      mx[k] = __ldg(lv.tgt_normals + 3 * pix[k]);
+      my[k] = __ldg(lv.tgt_normals + 3 * pix[k] + 1);
+      mz[k] = __ldg(lv.tgt_normals + 3 * pix[k] + 2);
+    }
+    // round 3: gates and the z-buffer
+#pragma unroll
+    for (int k = 0; k < kChunk; ++k) {
+      if (!ok[k]) continue;
+      const float dx = fsub(qx[k], Tp[k].x), dy = fsub(qy[k], Tp[k].y),
+                  dz = fsub(qz[k], Tp[k].z);
+      const float sq = dot3(dx, dy, dz, dx, dy, dz);
+      if (sq > q.thr2) continue;
+      const float3 Tn = transform_normal(P.nm, nx[k], ny[k], nz[k]);
+      const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, mx[k], my[k], mz[k]),
+                           fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
+                                __fsqrt_rn(dot3(mx[k], my[k], mz[k], mx[k], my[k], mz[k]))));
+      if (c >= -1.0f && c <= q.cos_max) continue;
+      const float dist = __fsqrt_rn(sq);
+      atomicMin(keys + pix[k], tag | ((unsigned long long)__float_as_uint(dist) << 24) |
+                                   (unsigned long long)idx[k]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-pair FP64 step by warp 0 (totals in smem)
+// ---------------------------------------------------------------------------
+__device__ void pair_step(const BatchArgs &a, int p, int level, int s, const double *tot) {
+  __shared__ double A[36], b[6], x[6], L[36], E[16], T[16], Tn[16];
+  const int lane = threadIdx.x & 31;
+  PairState *ps = a.ps + p;
+  const LevelP &q = a.lp[level];
+  for (int k = lane; k < 36; k += 32) {
+    const int r = k / 6, c = k % 6;
+    A[k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
+  }
+  if (lane < 6) b[lane] = tot[kJrB + lane];
+  if (lane < 16) T[lane] = __ldcg(ps->T + lane);
+  __syncwarp();
+  const double cg = tot[kCountGeomB], cf = tot[kCountFeatB];
+  const double count = q.use_geom ? fmax(cg, cf) : cf;
+  double *H = a.history ? a.history + ((size_t)p * a.total_iters + s) * STB_HIST_SIZE : nullptr;
+  if (H) {
+    for (int k = lane; k < 36; k += 32) H[STB_HIST_JTJ + k] = A[k];
+    if (lane < 6) H[STB_HIST_JR + lane] = b[lane];
+    if (lane == 0) {
+      H[STB_HIST_R2] = tot[kR2B];
+      H[STB_HIST_GEOM_COUNT] = cg;
+      H[STB_HIST_FEAT_COUNT] = cf;
+    }
+  }
+  const bool ok = warp_cholesky_solve6(A, b, x, L, lane);
+  double *R = a.results + (size_t)p * STB_RES_SIZE;
+  if (!ok) {
+    if (lane == 0) {
+      unsigned st = __ldcg(&ps->status) | STB_ST_NOT_PD;
+      if (count == 0.0) st |= STB_ST_NO_MATCHES;
+      ps->status = st;
+      ps->stopped = 1;
+      R[STB_RES_STATUS] = (double)st;
+      if (H) H[STB_HIST_OK] = 0.0;
+    }
+    return;
+  }
+  warp_se3_exp(x, E, lane);
+  warp_compose(E, T, Tn, lane);
+  if (lane < 16) {
+    ps->T[lane] = Tn[lane];
+    R[STB_RES_TRANSFORM + lane] = Tn[lane];
+    if (H) H[STB_HIST_TRANSFORM + lane] = Tn[lane];
+  }
+  for (int k = lane; k < 36; k += 32) R[STB_RES_JTJ + k] = A[k];
+  if (lane == 0) {
+    unsigned st = __ldcg(&ps->status);
+    bool finite = true;
+    for (int k = 0; k < 6; ++k) finite &= isfinite(x[k]);
+    if (!finite) st |= STB_ST_NAN;
+    if (count == 0.0) st |= STB_ST_NO_MATCHES;
+    ps->status = st;
+    Pose32 P;
+    P.fx = __ldcg(&ps->pose.fx);
+    P.fy = __ldcg(&ps->pose.fy);
+    P.cx = __ldcg(&ps->pose.cx);
+    P.cy = __ldcg(&ps->pose.cy);
+    refresh_pose32(P, Tn);
+    ps->pose = P;
+    const int li = __ldcg(&ps->level_iters) + 1;
+    ps->level_iters = li;
+    ps->iters_done = __ldcg(&ps->iters_done) + 1;
+    R[STB_RES_RESIDUAL] = tot[kR2B] / count;
+    R[STB_RES_MATCHES] = count;
+    R[STB_RES_ITERS] = (double)li;
+    R[STB_RES_STATUS] = (double)st;
+    if (H) H[STB_HIST_OK] = 1.0;
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// phase B: reduction of one target tile (+ group / pair folds and the step)
+// ---------------------------------------------------------------------------
+template <typename FT, bool kFeat, bool kInfo>
+__device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long *off, int level,
+                                            long long t, int s, TileCache &tc) {
+  constexpr int kN = kInfo ? 21 : kAccsB;
+  __shared__ int s_last;
+  __shared__ float bs[32], bc[32];
+  __shared__ double tot[32];
+  const int p = cache_pair(a, off, level, t, !kInfo, tc);
+  if (tc.skip) return;
+  const Pose32 &P = tc.P;
+  const stb_level &lv = tc.lv;
+  const size_t row = (size_t)level * (a.B + 1);
+  const long long t0 = off_at(off, a.B, p);
+  const long long ntiles = off_at(off, a.B, p + 1) - t0;
+  const long long lt = t - t0;
+  const LevelP &q = a.lp[level];
+  const int H = lv.height, W = lv.width;
+  const long long npix = (long long)H * W;
+  const unsigned long long *keys = a.keys + __ldcg(a.key_off + p);
+  const unsigned tag = btag(s);
+
+  CSum acc[kN];
+#pragma unroll
+  for (int k = 0; k < kN; ++k) acc[k] = {0.f, 0.f};
+
+  const long long end = min((lt + 1) * (long long)a.tile, npix);
+  for (long long base = lt * (long long)a.tile; base < end; base += kThreads * kChunk) {
+  unsigned long long key[kChunk];
+  long long pixs[kChunk];
+  constexpr int kP = kChunk;
+#pragma unroll
+  for (int k = 0; k < kP; ++k) {
+    pixs[k] = base + k * kThreads + threadIdx.x;
+    key[k] = (pixs[k] < end) ? __ldcg(keys + pixs[k]) : 0ull;
+  }
+#pragma unroll
+  for (int k = 0; k < kP; ++k) {
+    if ((unsigned)(key[k] >> 56) != tag || pixs[k] >= end) continue;
+    const long long pix = pixs[k];
+    const float qx = __ldg(lv.tgt_points + 3 * pix), qy = __ldg(lv.tgt_points + 3 * pix + 1),
+                qz = __ldg(lv.tgt_points + 3 * pix + 2);
+    if (kInfo) {
+      const float G0[6] = {0.f, qz, -qy, 1.f, 0.f, 0.f};
+      const float G1[6] = {-qz, 0.f, qx, 0.f, 1.f, 0.f};
+      const float G2[6] = {qy, -qx, 0.f, 0.f, 0.f, 1.f};
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j)
+          csum_add(acc[upper_index(i, j)], G0[i] * G0[j] + G1[i] * G1[j] + G2[i] * G2[j]);
+      continue;
+    }
+    const long long i = (long long)(key[k] & 0xffffffull);
+    const float3 Tp = transform_point(P.rt, __ldg(lv.src_points + 3 * i),
+                                      __ldg(lv.src_points + 3 * i + 1),
+                                      __ldg(lv.src_points + 3 * i + 2));
+    if (q.use_geom) {
+      const float nx = __ldg(lv.tgt_normals + 3 * pix), ny = __ldg(lv.tgt_normals + 3 * pix + 1),
+                  nz = __ldg(lv.tgt_normals + 3 * pix + 2);
+      const float r = dot3(fsub(qx, Tp.x), fsub(qy, Tp.y), fsub(qz, Tp.z), nx, ny, nz);
+      const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
+                           fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
+                           fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
+      acc_se3(acc, Jv, r, q.wg1, q.wg2);
+      csum_add(acc[kR2B], q.wg1 * (r * r));
+      csum_add(acc[kCountGeomB], 1.f);
+    }
+    if (kFeat && q.use_feat) {
+      const FT *tf = static_cast<const FT *>(lv.tgt_feats);
+      const FT *sf = static_cast<const FT *>(lv.src_feats);
+      const int C = a.C;
+      const long long n = lv.num_source;
+      float u, v;
+      project(P, Tp, u, v);
+      float sq = 0.f;
+      for (int c = 0; c < C; ++c) {
+        const float r = fsub(bilin(tf + c * npix, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+        sq = fadd(sq, fmul(r, r));
+      }
+      if (!(sq > q.feat_thr2)) {
+        const float h = 0.05f;
+        const float div = fdiv(1.f, fmul(2.f, h));
+        const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
+        const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
+        const float zz = fmul(Tp.z, Tp.z);
+        const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
+        const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
+        const int c0 = (a.mode == 0) ? C - 1 : 0;
+        for (int c = c0; c < C; ++c) {
+          const FT *fc = tf + c * npix;
+          const float r = fsub(bilin(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+          const float du = fmul(fsub(bilin(fc, H, W, uu0, v), bilin(fc, H, W, uu1, v)), div);
+          const float dv = fmul(fsub(bilin(fc, H, W, u, vv0), bilin(fc, H, W, u, vv1)), div);
+          const float gx = fmul(du, j00), gy = fmul(dv, j11),
+                      gz = fadd(fmul(du, j02), fmul(dv, j12));
+          const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
+                               fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
+                               fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
+          acc_se3(acc, Jv, r, -q.wf1, q.wf2);
+        }
+        csum_add(acc[kR2B], q.wf1 * sq);
+        csum_add(acc[kCountFeatB], 1.f);
+      }
+    }
+  }
+  }
+
+  block_sum<kN>(acc, bs, bc);
+  float *slot = a.tile_part + (size_t)t * kSlotFloats;
+  if (threadIdx.x < kN) {
+    slot[threadIdx.x] = bs[threadIdx.x];
+    slot[32 + threadIdx.x] = bc[threadIdx.x];
+  }
+  __threadfence();
+  __syncthreads();
+  const long long g_local = lt / kGroup;
+  const long long g = __ldcg(a.grp_off + row + p) + g_local;
+  const int gsize = (int)min((long long)kGroup, ntiles - g_local * kGroup);
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(a.grp_ticket + g, 1u);
+    s_last = (prev == (unsigned)gsize - 1);
+    if (s_last) a.grp_ticket[g] = 0;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  fold_slots<kN>(a.tile_part + (size_t)(t0 + g_local * kGroup) * kSlotFloats, gsize, bs, bc);
+  float *gslot = a.grp_part + (size_t)g * kSlotFloats;
+  if (threadIdx.x < kN) {
+    gslot[threadIdx.x] = bs[threadIdx.x];
+    gslot[32 + threadIdx.x] = bc[threadIdx.x];
+  }
+  __threadfence();
+  __syncthreads();
+  const long long ngroups = (ntiles + kGroup - 1) / kGroup;
+  if (threadIdx.x == 0) {
+    const unsigned prev = atomicAdd(a.pair_ticket + p, 1u);
+    s_last = (prev == (unsigned)ngroups - 1);
+    if (s_last) a.pair_ticket[p] = 0;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const long long g0 = __ldcg(a.grp_off + row + p);
+  // a pair has at most 4 * 8 * kGroup tiles per fold_slots call; fold in
+  // chunks of 32 groups
+  CSum run[1];
+  if (threadIdx.x < kN) run[0] = {0.f, 0.f};
+  for (long long c0 = 0; c0 < ngroups; c0 += 32) {
+    const int cnt = (int)min(32LL, ngroups - c0);
+    fold_slots<kN>(a.grp_part + (size_t)(g0 + c0) * kSlotFloats, cnt, bs, bc);
+    if (threadIdx.x < kN) csum_merge(run[0], bs[threadIdx.x], bc[threadIdx.x]);
+  }
+  if (threadIdx.x < kN) tot[threadIdx.x] = (double)run[0].s + (double)run[0].c;
+  __syncthreads();
+  if (kInfo) {
+    double *R = a.results + (size_t)p * STB_RES_SIZE;
+    for (int k = threadIdx.x; k < 36; k += blockDim.x) {
+      const int r = k / 6, c = k % 6;
+      R[STB_RES_INFO + k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
+    }
+  } else if (threadIdx.x < 32) {
+    pair_step(a, p, level, s, tot);
+  }
+  __syncthreads();
+}
+
+template <typename FT, bool kFeat>
+__global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
+  // the argument block is staged in shared memory so that device functions
+  // can take it by reference without a per-thread local copy
+  __shared__ BatchArgs a;
+  __shared__ long long s_off[kStageOff];
+  __shared__ TileCache tc;
+  for (int k = threadIdx.x; k < (int)(sizeof(BatchArgs) / sizeof(int)); k += blockDim.x)
+    reinterpret_cast<int *>(&a)[k] = reinterpret_cast<const int *>(&args)[k];
+  __syncthreads();
+  // phase 0: offsets (block 0), then pair states, key map, tickets
+  if (blockIdx.x == 0) build_offsets(a);
+  if (!grid_sync(a.sync)) return;
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (long long p = gtid; p < a.B; p += gthreads) {
+    PairState *ps = a.ps + p;
+    for (int k = 0; k < 16; ++k)
+      ps->T[k] = a.init ? a.init[p * 16 + k] : ((k % 5) == 0 ? 1.0 : 0.0);
+    ps->stopped = 0;
+    ps->status = 0;
+    ps->level_iters = 0;
+    ps->iters_done = 0;
+    a.pair_ticket[p] = 0;
+    double *R = a.results + p * STB_RES_SIZE;
+    for (int k = 0; k < STB_RES_SIZE; ++k) R[k] = 0.0;
+    R[STB_RES_RESIDUAL] = INFINITY;
+  }
+  const long long nkeys = __ldcg(a.key_off + a.B);
+  for (long long k = gtid; k < nkeys; k += gthreads) a.keys[k] = ~0ull;
+  for (long long k = gtid; k < a.groups_cap; k += gthreads) a.grp_ticket[k] = 0;
+  if (!grid_sync(a.sync)) return;
+
+  int s = 0;
+  for (int level = 0; level < a.L; ++level) {
+    // level start: the reference's next estimator gets the previous result's
+    // transform, None (identity) when that level's first iteration failed
+    for (long long p = gtid; p < a.B; p += gthreads) {
+      PairState *ps = a.ps + p;
+      double T[16];
+      const bool reset = level > 0 && __ldcg(&ps->level_iters) == 0;
+      for (int k = 0; k < 16; ++k)
+        T[k] = reset ? ((k % 5) == 0 ? 1.0 : 0.0) : __ldcg(ps->T + k);
+      for (int k = 0; k < 16; ++k) ps->T[k] = T[k];
+      ps->stopped = 0;
+      ps->level_iters = 0;
+      const stb_level lv = a.levels[p * a.L + level];
+      Pose32 P;
+      P.fx = lv.fx;
+      P.fy = lv.fy;
+      P.cx = lv.cx;
+      P.cy = lv.cy;
+      refresh_pose32(P, T);
+      ps->pose = P;
+      double *R = a.results + p * STB_RES_SIZE;
+      R[STB_RES_ITERS] = 0.0;
+      R[STB_RES_RESIDUAL] = INFINITY;
+    }
+    if (!grid_sync(a.sync)) return;
+    const size_t row = (size_t)level * (a.B + 1);
+    const long long src_tiles = __ldcg(a.src_off + row + a.B);
+    const long long tgt_tiles = __ldcg(a.tgt_off + row + a.B);
+    for (int it = 0; it < a.lp[level].iters; ++it, ++s) {
+      const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
+      reset_cache(tc);
+      for (long long t = blockIdx.x; t < src_tiles; t += gridDim.x)
+        assoc_tile(a, off, level, t, s, false, tc);
+      if (!grid_sync(a.sync)) return;
+      off = stage_offsets(a.tgt_off + row, a.B, s_off);
+      reset_cache(tc);
+      for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
+        reduce_tile<FT, kFeat, false>(a, off, level, t, s, tc);
+      if (!grid_sync(a.sync)) return;
+    }
+  }
+  // information matrix at the final pose (finest level)
+  const int level = a.L - 1;
+  const size_t row = (size_t)level * (a.B + 1);
+  const long long src_tiles = __ldcg(a.src_off + row + a.B);
+  const long long tgt_tiles = __ldcg(a.tgt_off + row + a.B);
+  const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
+  reset_cache(tc);
+  for (long long t = blockIdx.x; t < src_tiles; t += gridDim.x)
+    assoc_tile(a, off, level, t, s, true, tc);
+  if (!grid_sync(a.sync)) return;
+  off = stage_offsets(a.tgt_off + row, a.B, s_off);
+  reset_cache(tc);
+  for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
+    reduce_tile<FT, false, true>(a, off, level, t, s, tc);
+}
+
+// Flags every pair's status when the persistent kernel stopped early:
+// STB_ST_TIMEOUT (a barrier gave up) or STB_ST_CAPACITY (the workspace was
+// sized for fewer pixels than the levels hold).
+__global__ void k_batch_status(const unsigned *sync, double *results, int B) {
+  const unsigned err = *(volatile const unsigned *)(sync + 2);
+  if (!err) return;
+  const unsigned bits = ((err & 1u) ? STB_ST_TIMEOUT : 0u) | ((err & 2u) ? STB_ST_CAPACITY : 0u);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < B; p += gridDim.x * blockDim.x)
+    results[(size_t)p * STB_RES_SIZE + STB_RES_STATUS] =
+        (double)((unsigned)results[(size_t)p * STB_RES_SIZE + STB_RES_STATUS] | bits);
+}
+
+template <typename FT, bool kFeat>
+int launch_batch(const BatchArgs &args, cudaStream_t st) {
+  auto kern = k_batch<FT, kFeat>;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0);
+  if (per_sm < 1) return fail(STB_ECUDA, "Cuda call error stb_icp_estimate_batch: kernel does not fit an SM");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(sms * per_sm);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  BatchArgs a = args;
+  const cudaError_t err = cudaLaunchKernelEx(&cfg, kern, a);
+  if (err != cudaSuccess)
+    return fail(STB_ECUDA, "Cuda call error stb_icp_estimate_batch: %s", cudaGetErrorString(err));
+  k_batch_status<<<(args.B + 255) / 256, 256, 0, st>>>(args.sync, args.results, args.B);
+  return check_launch("stb_icp_estimate_batch");
+}
+
+}  // namespace
+}  // namespace stb
+
+using namespace stb;
+
+extern "C" size_t stb_icp_batch_workspace_bytes(int32_t num_pairs, int64_t total_target_pixels) {
+  if (num_pairs <= 0 || total_target_pixels < 0) return 0;
+  return layout(num_pairs, total_target_pixels).total;
+}
+
+extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs,
+                                      int32_t num_levels, const stb_level_params *params,
+                                      int32_t channels, int32_t feat_dtype, int32_t channel_mode,
+                                      const double *init_transforms, int64_t total_target_pixels,
+                                      void *workspace, size_t workspace_bytes, double *results,
+                                      double *history, int32_t tile_config, void *stream) {
+  clear_error();
+  if (num_pairs <= 0) return fail(STB_EINVAL, "Check failed: num_pairs must be positive");
+  if (num_levels <= 0 || num_levels > kMaxLevels)
+    return fail(STB_EINVAL, "Check failed: num_levels must be in [1, %d]", kMaxLevels);
+  if (!params) return fail(STB_EINVAL, "Check failed: params: null pointer");
+  int total_iters = 0;
+  bool any_feat = false;
+  for (int l = 0; l < num_levels; ++l) {
+    if (params[l].num_iters < 0) return fail(STB_EINVAL, "Check failed: num_iters must be >= 0");
+    total_iters += params[l].num_iters;
+    any_feat = any_feat || params[l].feat_weight > 0.0;
+  }
+  if (total_iters > 253)
+    return fail(STB_EINVAL, "Check failed: at most 253 iterations over all levels, got %d",
+                total_iters);
+  if (any_feat) {
+    if (channels <= 0)
+      return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
+    if (feat_dtype != STB_F32 && feat_dtype != STB_BF16)
+      return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
+  }
+  if (channel_mode != 0 && channel_mode != 1)
+    return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
+  const Layout lay = layout(num_pairs, total_target_pixels);
+  if (workspace_bytes < lay.total)
+    return fail(STB_EINVAL, "Check failed: workspace of %zu bytes, %zu needed", workspace_bytes,
+                lay.total);
+  if (((uintptr_t)workspace & 255) != 0)
+    return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
+  if (tile_config < 0 || tile_config > 4)
+    return fail(STB_EINVAL, "Check failed: tile_config must be in [0, 4]");
+  STB_TRY(check_device_ptr(levels, "levels"));
+  STB_TRY(check_device_ptr(init_transforms, "init_transforms", true));
+  STB_TRY(check_device_ptr(workspace, "workspace"));
+  STB_TRY(check_device_ptr(results, "results"));
+  STB_TRY(check_device_ptr(history, "history", true));
+
+  char *ws = static_cast<char *>(workspace);
+  BatchArgs a;
+  a.levels = levels;
+  a.B = num_pairs;
+  a.L = num_levels;
+  a.C = any_feat ? channels : 0;
+  a.dtype = feat_dtype;
+  a.mode = channel_mode;
+  a.total_iters = total_iters;
+  // pixels per work item: 0 -> default, 1..4 -> 512, 1024, 2048, 4096
+  a.tile = kMinTile << (tile_config == 0 ? 1 : tile_config - 1);
+  for (int l = 0; l < kMaxLevels; ++l) {
+    LevelP &q = a.lp[l];
+    if (l >= num_levels) {
+      q = LevelP{};
+      continue;
+    }
+    const stb_level_params &pp = params[l];
+    q.iters = pp.num_iters;
+    q.use_geom = pp.geom_weight > 0.0;
+    q.use_feat = any_feat && pp.feat_weight > 0.0;
+    q.wg1 = (float)pp.geom_weight;
+    q.wg2 = (float)(pp.geom_weight * pp.geom_weight);
+    q.wf1 = (float)pp.feat_weight;
+    q.wf2 = (float)(pp.feat_weight * pp.feat_weight);
+    q.thr2 = distance_thresh_sq(pp.distance_thresh);
+    q.cos_max = angle_cos_max(pp.normal_angle_thresh);
+    const float ft = (float)pp.feat_residual_thresh;
+    q.feat_thr2 = ft * ft;
+  }
+  a.init = init_transforms;
+  a.results = results;
+  a.history = history;
+  a.sync = reinterpret_cast<unsigned *>(ws + lay.sync);
+  a.ps = reinterpret_cast<PairState *>(ws + lay.ps);
+  a.key_off = reinterpret_cast<long long *>(ws + lay.key_off);
+  a.src_off = reinterpret_cast<long long *>(ws + lay.src_off);
+  a.tgt_off = reinterpret_cast<long long *>(ws + lay.tgt_off);
+  a.grp_off = reinterpret_cast<long long *>(ws + lay.grp_off);
+  a.grp_ticket = reinterpret_cast<unsigned *>(ws + lay.grp_ticket);
+  a.pair_ticket = reinterpret_cast<unsigned *>(ws + lay.pair_ticket);
+  a.tile_part = reinterpret_cast<float *>(ws + lay.tile_part);
+  a.grp_part = reinterpret_cast<float *>(ws + lay.grp_part);
+  a.keys = reinterpret_cast<unsigned long long *>(ws + lay.keys);
+  a.keys_cap = total_target_pixels;
+  a.tiles_cap = lay.tiles_cap;
+  a.groups_cap = lay.groups_cap;
+
+  const cudaStream_t st = as_stream(stream);
+  // barrier counters start at zero for every launch
+  if (cudaMemsetAsync(a.sync, 0, 256, st) != cudaSuccess) return check_launch("cudaMemsetAsync");
+  if (!any_feat) return launch_batch<float, false>(a, st);
+  if (feat_dtype == STB_F32) return launch_batch<float, true>(a, st);
+  return launch_batch<__nv_bfloat16, true>(a, st);
+}

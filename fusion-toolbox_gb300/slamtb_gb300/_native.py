@@ -47,6 +47,9 @@ _SIGNATURES = {
     "stb_icp_information_partials": (ctypes.c_int, [
         _vp, _vp, _i64, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
     "stb_icp_workspace_bytes": (_sz, [_i64, _i32, _i32]),
+    "stb_icp_batch_workspace_bytes": (_sz, [_i32, _i64]),
+    "stb_icp_estimate_batch": (ctypes.c_int, [
+        _vp, _i32, _i32, _vp, _i32, _i32, _i32, _vp, _i64, _vp, _sz, _vp, _vp, _i32, _vp]),
     "stb_icp_estimate_static": (ctypes.c_int, [
         _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _i32,
         _i32, _vp, _i32, _f64, _f64, _f64, _f64, _f64, _i32, _vp, _vp, _vp]),
@@ -65,6 +68,24 @@ _SIGNATURES = {
         _i32, _vp, _i32, _f64, _f64, _f64, _f64, _f64, _i32, _vp, _sz, _vp,
         _vp, _i32, _vp]),
 }
+
+
+class StbLevel(ctypes.Structure):
+    """``stb_level`` of the header: one pyramid level of one frame pair."""
+    _fields_ = [("src_points", _vp), ("src_normals", _vp), ("src_mask", _vp),
+                ("num_source", _i64), ("src_feats", _vp), ("tgt_points", _vp),
+                ("tgt_normals", _vp), ("tgt_mask", _vp), ("height", _i32), ("width", _i32),
+                ("tgt_feats", _vp), ("fx", _f32), ("fy", _f32), ("cx", _f32), ("cy", _f32)]
+
+
+class StbLevelParams(ctypes.Structure):
+    """``stb_level_params`` of the header."""
+    _fields_ = [("num_iters", _i32), ("geom_weight", _f64), ("feat_weight", _f64),
+                ("distance_thresh", _f64), ("normal_angle_thresh", _f64),
+                ("feat_residual_thresh", _f64)]
+
+
+ST_TIMEOUT, ST_CAPACITY = 8, 16
 
 _LIB = None
 

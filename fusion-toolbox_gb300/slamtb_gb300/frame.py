@@ -55,7 +55,14 @@ class KCamera:
         return KCamera(out, self.undist_coeff, image_size)
 
     def to(self, device):
-        return KCamera(self.matrix.to(device), self.undist_coeff, self.image_size)
+        """Intrinsics are kept on the host (kernels take them by value or
+        copy them per call); returns self."""
+        return self
+
+    def params(self):
+        """(fx, fy, cx, cy) as Python floats."""
+        m = self.matrix.detach().cpu()
+        return float(m[0, 0]), float(m[1, 1]), float(m[0, 2]), float(m[1, 2])
 
 
 class FrameInfo:
@@ -114,9 +121,8 @@ class FramePointCloud:
         kcam = frame.info.kcam
         if not isinstance(kcam, KCamera):
             kcam = KCamera(kcam)
-        kcam = kcam.to(device)
         points, raw_mask = processing.depth_to_points(
-            depth, kcam.matrix, frame.info.depth_scale, frame.info.depth_bias)
+            depth, kcam.matrix.to(device), frame.info.depth_scale, frame.info.depth_bias)
         mask = processing.erode_mask(raw_mask)
         normals = None
         if frame.normal_image is not None:

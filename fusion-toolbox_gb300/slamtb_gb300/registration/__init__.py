@@ -4,7 +4,8 @@ from .multiscale import MultiscaleRegistration, MultiscaleICPOdometry
 from .result import RegistrationResult, RegistrationVerifier
 from .correspondence_map import CorrespondenceMap
 from .preset import create_multiscale_odometry
+from .batch import BatchRegistration
 
 __all__ = ["ICPOdometry", "MultiscaleRegistration", "MultiscaleICPOdometry",
            "RegistrationResult", "RegistrationVerifier", "CorrespondenceMap",
-           "create_multiscale_odometry"]
+           "create_multiscale_odometry", "BatchRegistration"]

@@ -1,0 +1,173 @@
+"""Many frame pairs, one multiscale schedule, one persistent launch.
+
+``BatchRegistration`` runs ``MultiscaleRegistration.estimate_frame``
+(``slamtb/registration/multiscale.py:30-67``) for a list of frame pairs at
+once: ``stb_icp_estimate_batch`` advances every pair through every level
+and Gauss-Newton iteration inside one cooperative kernel (grid barriers
+between the association and reduction phases, a per-pair FP64 solve at the
+end of each reduction), so a batch of uneven resolutions costs one launch.
+"""
+import ctypes
+
+import torch
+
+from .. import _native as N
+from ..frame import Frame, FramePointCloud, resolve_device
+from ..processing import feature_pyramid
+from .icp import ICPOdometry
+from .result import RegistrationResult
+
+
+class BatchRegistration:
+    """Args:
+        estimators (list of (float, ICPOdometry)): scale and estimator per
+            level, finest first, as ``MultiscaleRegistration``; at most 4
+            levels and 253 iterations in total.
+        feat_channel_mode (str): "last" (reference) or "sum".
+        record_history (bool): keep per-iteration records in
+            ``self.last_history`` ((pairs, total iterations, 64) float64 CPU,
+            iterations numbered over the levels coarsest first).
+    """
+
+    def __init__(self, estimators, feat_channel_mode="last", record_history=False):
+        if not 1 <= len(estimators) <= 4:
+            raise ValueError("BatchRegistration takes 1 to 4 levels")
+        for _, est in estimators:
+            if not isinstance(est, ICPOdometry):
+                raise TypeError("BatchRegistration levels must be ICPOdometry estimators")
+        if feat_channel_mode not in ("last", "sum"):
+            raise ValueError("feat_channel_mode must be 'last' or 'sum'")
+        self.estimators = estimators
+        self.feat_channel_mode = feat_channel_mode
+        self.record_history = record_history
+        self.last_history = None
+        self.tile_config = 0  # 0 default; 1..4: 512, 1024, 2048, 4096 pixels per work item
+        self._ws = None
+
+    @property
+    def scales(self):
+        return [s for s, _ in self.estimators]
+
+    def _params(self):
+        levels = [est for _, est in self.estimators[::-1]]  # coarsest first
+        arr = (N.StbLevelParams * len(levels))()
+        for k, est in enumerate(levels):
+            arr[k] = N.StbLevelParams(est.num_iters, float(est.geom_weight),
+                                      float(est.feat_weight), float(est.distance_threshold),
+                                      float(est.normals_angle_thresh),
+                                      float(est.feat_residual_thresh))
+        return arr, sum(est.num_iters for est in levels)
+
+    def launch(self, sources, targets, source_feats=None, target_feats=None,
+               transforms=None):
+        """Enqueue the batch; ``sources`` / ``targets``: per pair, the list of
+        level ``FramePointCloud`` (coarsest first), ``*_feats``: per pair the
+        list of (C, H, W) maps or None.  Returns (results (B, 96) device
+        tensor, history or None, keep-alive list)."""
+        B, L = len(sources), len(self.estimators)
+        if B == 0 or len(targets) != B:
+            raise ValueError("sources and targets must be non-empty lists of equal length")
+        device = targets[0][0].points.device
+        use_feat = source_feats is not None and target_feats is not None
+        keep = []
+        lv = (N.StbLevel * (B * L))()
+        total_px = 0
+        channels, code = 0, N.STB_F32
+        for p in range(B):
+            if len(sources[p]) != L or len(targets[p]) != L:
+                raise ValueError(f"pair {p}: expected {L} levels")
+            biggest = 0
+            for l in range(L):
+                src, tgt = sources[p][l], targets[p][l]
+                sp = src.points.reshape(-1, 3).contiguous()
+                sn = src.normals.reshape(-1, 3).contiguous()
+                sm = src.mask.reshape(-1).to(torch.bool).contiguous()
+                tp, tn = tgt.points.contiguous(), tgt.normals.contiguous()
+                tm = tgt.mask.to(torch.bool).contiguous()
+                for t in (sp, sn, tp, tn):
+                    if t.dtype != torch.float32 or t.device != device:
+                        raise RuntimeError("Check failed: points and normals must be float32 "
+                                           f"tensors on {device}")
+                h, w = tm.shape
+                sf = tf = None
+                if use_feat and source_feats[p] is not None and target_feats[p] is not None:
+                    tf = target_feats[p][l].to(device).contiguous()
+                    sf = source_feats[p][l].to(device).reshape(tf.size(0), -1).contiguous()
+                    channels = tf.size(0)
+                    code = N.feat_dtype_code(tf)
+                keep += [sp, sn, sm, tp, tn, tm, sf, tf]
+                fx, fy, cx, cy = tgt.kcam.params()
+                lv[p * L + l] = N.StbLevel(
+                    sp.data_ptr(), sn.data_ptr(), sm.data_ptr(), sp.size(0),
+                    sf.data_ptr() if sf is not None else None, tp.data_ptr(), tn.data_ptr(),
+                    tm.data_ptr(), h, w, tf.data_ptr() if tf is not None else None,
+                    fx, fy, cx, cy)
+                biggest = max(biggest, h * w)
+            total_px += biggest
+        levels_dev = torch.frombuffer(bytearray(bytes(lv)), dtype=torch.uint8).to(device)
+        keep.append(levels_dev)
+        params, total_iters = self._params()
+        init = None
+        if transforms is not None:
+            init = torch.stack([torch.eye(4, dtype=torch.float64) if t is None else
+                                torch.as_tensor(t, dtype=torch.float64).cpu()
+                                for t in transforms]).to(device).contiguous()
+            keep.append(init)
+        need = int(N.lib().stb_icp_batch_workspace_bytes(B, total_px))
+        if self._ws is None or self._ws.device != device or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=device)
+        results = torch.empty(B, N.RES_SIZE, dtype=torch.float64, device=device)
+        hist = None
+        if self.record_history:
+            hist = torch.zeros(B, max(total_iters, 1), N.HIST_SIZE, dtype=torch.float64,
+                               device=device)
+        with torch.cuda.device(device):
+            N.check(N.lib().stb_icp_estimate_batch(
+                N.ptr(levels_dev), B, L, ctypes.cast(params, ctypes.c_void_p), channels, code,
+                0 if self.feat_channel_mode == "last" else 1, N.ptr(init), total_px,
+                N.ptr(self._ws), self._ws.numel(), N.ptr(results), N.ptr(hist),
+                int(self.tile_config), N.stream_of(device)))
+        return results, hist, keep
+
+    def estimate_pyramids(self, sources, targets, source_feats=None, target_feats=None,
+                          transforms=None):
+        """Register every pair; returns a list of ``RegistrationResult``
+        (the finest level's, as ``MultiscaleRegistration``)."""
+        results, hist, _ = self.launch(sources, targets, source_feats, target_feats,
+                                       transforms)
+        out = results.cpu()
+        if hist is not None:
+            self.last_history = hist.cpu()
+        res = []
+        for p in range(len(sources)):
+            n = sources[p][-1].mask.numel()
+            res.append(ICPOdometry._result(out[p], n, torch.float32))
+        status = out[:, N.RES_STATUS].to(torch.int64)
+        if bool(((status & (N.ST_TIMEOUT | N.ST_CAPACITY)) != 0).any()):
+            raise RuntimeError("stb_icp_estimate_batch stopped early "
+                               f"(status bits {int(status.max())})")
+        return res
+
+    def pyramids(self, frames, device=None):
+        """Device pyramids (coarsest first) of a list of ``Frame`` or
+        ``FramePointCloud``."""
+        device = resolve_device(device)
+        out = []
+        for f in frames:
+            if isinstance(f, Frame):
+                f = FramePointCloud.from_frame(f, device)
+            out.append(f.pyramid(self.scales))
+        return out
+
+    def estimate_frames(self, source_frames, target_frames, source_feats=None,
+                        target_feats=None, transforms=None, device=None):
+        """``MultiscaleRegistration.estimate_frame`` for lists of frame pairs."""
+        sp = self.pyramids(source_frames, device)
+        tp = self.pyramids(target_frames, device)
+        sfp = tfp = None
+        if source_feats is not None and target_feats is not None:
+            sfp = [feature_pyramid(f.to(sp[0][0].points.device), self.scales)
+                   for f in source_feats]
+            tfp = [feature_pyramid(f.to(sp[0][0].points.device), self.scales)
+                   for f in target_feats]
+        return self.estimate_pyramids(sp, tp, sfp, tfp, transforms)

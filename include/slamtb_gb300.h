@@ -61,6 +61,8 @@ extern "C" {
 #define STB_ST_NOT_PD 1u     /* 6x6 J^T J was not positive definite: stopped */
 #define STB_ST_NO_MATCHES 2u /* an iteration found no correspondence        */
 #define STB_ST_NAN 4u        /* a non-finite update was produced            */
+#define STB_ST_TIMEOUT 8u    /* a bounded grid barrier gave up (batch path) */
+#define STB_ST_CAPACITY 16u  /* workspace sized for fewer pixels (batch path) */
 
 /* ---- layout of the device result block (doubles) ----------------------- */
 #define STB_RES_TRANSFORM 0   /* 16: final 4x4 pose, row-major             */
@@ -228,6 +230,73 @@ STB_API int stb_icp_estimate(const float *kcam, const float *src_points,
                      void *workspace, size_t workspace_bytes, double *result,
                      double *history, int32_t use_graph, void *stream);
 
+
+/* ======================================================================= *
+ * Batched, multiscale registration in one persistent launch
+ * ======================================================================= */
+
+/* One pyramid level of one frame pair (device pointers; layouts as
+ * stb_icp_estimate).  src_feats / tgt_feats may be NULL. */
+typedef struct {
+  const float *src_points;
+  const float *src_normals;
+  const uint8_t *src_mask;
+  int64_t num_source;
+  const void *src_feats;
+  const float *tgt_points;
+  const float *tgt_normals;
+  const uint8_t *tgt_mask;
+  int32_t height;
+  int32_t width;
+  const void *tgt_feats;
+  float fx, fy, cx, cy; /* this level's intrinsics */
+} stb_level;
+
+/* Estimator parameters of one level, shared by all pairs: the
+ * ICPOdometry(num_iters, geom_weight, feat_weight, distance_threshold,
+ * normals_angle_thresh, feat_residual_thresh) of that level. */
+typedef struct {
+  int32_t num_iters;
+  double geom_weight;
+  double feat_weight;
+  double distance_thresh;
+  double normal_angle_thresh;
+  double feat_residual_thresh;
+} stb_level_params;
+
+/* Workspace bytes for num_pairs pairs whose largest levels hold
+ * total_target_pixels target pixels together. */
+STB_API size_t stb_icp_batch_workspace_bytes(int32_t num_pairs,
+                                             int64_t total_target_pixels);
+
+/*
+ * MultiscaleRegistration.estimate_frame (slamtb/registration/multiscale.py:
+ * 30-67) for many frame pairs at once: every pair runs the levels coarsest
+ * first, each level the Gauss-Newton loop of ICPOdometry.estimate
+ * (icp.py:152-262) with that level's parameters, the next level starting
+ * from the previous level's pose (identity when that level's first
+ * iteration failed, as the reference), then the information matrix at the
+ * final pose.  One cooperative persistent kernel covers all pairs, levels
+ * and iterations: phases (association, reduction + per-pair FP64 solve) are
+ * separated by grid barriers whose waits are bounded (a barrier that waits
+ * too long sets STB_ST_TIMEOUT in every pair's status and the kernel
+ * returns).
+ *
+ * levels: device array [num_pairs][num_levels], coarsest level first;
+ * finest level last.  params: host array [num_levels].  All levels share
+ * channels / feat_dtype.  init_transforms: device float64 [num_pairs][16]
+ * or NULL.  total_target_pixels: sum over pairs of the largest level's
+ * height * width.  results: device float64
+ * [num_pairs][STB_RES_SIZE] (the last level's RegistrationResult).
+ * history: NULL or device float64 [num_pairs][sum of num_iters][STB_HIST_SIZE].
+ * tile_config: 0 default; 1..3 select 2, 4 or 8 pixels per thread.
+ */
+STB_API int stb_icp_estimate_batch(
+    const stb_level *levels, int32_t num_pairs, int32_t num_levels,
+    const stb_level_params *params, int32_t channels, int32_t feat_dtype,
+    int32_t channel_mode, const double *init_transforms,
+    int64_t total_target_pixels, void *workspace, size_t workspace_bytes,
+    double *results, double *history, int32_t tile_config, void *stream);
 
 /*
  * stb_icp_estimate without any allocation.  No counterpart in the reference:
