@@ -140,26 +140,25 @@ __host__ __device__ constexpr int upper_index(int a, int b) {
 // ---------------------------------------------------------------------------
 namespace stb {
 
-// 1/sqrt(d) for d > 0: float32 seed, two Newton-Raphson steps in FP64
-// (y <- y + y/2 (1 - d y^2); each step doubles the correct bits: 2^-22 ->
-// 2^-44 -> full double).  Seeds outside the float32 range fall back to the
-// library call.
+// 1/sqrt(d) for d > 0: float32 seed (relative error < 2^-22), one
+// Newton-Raphson step in FP64 (y <- y + y/2 (1 - d y^2)), which squares the
+// error to below 2^-43 (~1e-13): the pivots of the 6x6 factorisation carry
+// 13 significant digits, the Gauss-Newton update needs fewer than 8.  Seeds
+// outside the float32 range fall back to the library call.
 __device__ __forceinline__ double rsqrt_fp64(double d) {
   const float f = (float)d;
   if (!(f > 1e-37f && f < 1e37f)) return 1.0 / sqrt(d);
-  double y = (double)rsqrtf(f);
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
-    const double e = fma(-d, y * y, 1.0);
-    y = fma(0.5 * y, e, y);
-  }
-  return y;
+  const double y = (double)rsqrtf(f);
+  const double e = fma(-d, y * y, 1.0);
+  return fma(0.5 * y, e, y);
 }
 
-// SE(3) exponential like se3_exp, entries spread over the warp.  All lanes
-// call it with the same xi; every lane returns the full E (row-major 4x4)
-// via shared memory `E` (16 doubles).
+// SE(3) exponential like se3_exp, entries spread over the warp: lanes 0..8
+// hold R, lanes 16..24 hold V = I + B W + C W^2, lanes 0..2 then form
+// t = V v.  All lanes call it with the same xi; E (16 doubles, shared
+// memory) receives the row-major 4x4.
 __device__ inline void warp_se3_exp(const double *xi, double *E, int lane) {
+  const unsigned full = 0xffffffffu;
   const double wx = xi[3], wy = xi[4], wz = xi[5];
   const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
   double A, B, C;
@@ -177,35 +176,33 @@ __device__ inline void warp_se3_exp(const double *xi, double *E, int lane) {
     B = (1.0 - c) * it2;
     C = (t - s) * (it2 * it);
   }
-  if (lane < 12) {
-    const int i = lane >> 2, j = lane & 3;
-    const double w[3] = {wx, wy, wz};
-    // W = hat(w): W[i][k] = -eps_ikm w_m ; W2 = w w^T - |w|^2 I
-    if (j < 3) {
-      const double Wij = (i == j) ? 0.0 : ((j == (i + 1) % 3) ? -w[(i + 2) % 3] : w[(i + 1) % 3]);
-      const double W2ij = w[i] * w[j] - ((i == j) ? t2 : 0.0);
-      E[i * 4 + j] = ((i == j) ? 1.0 : 0.0) + A * Wij + B * W2ij;
-    } else {
-      // t_i = sum_k (I + B W + C W^2)_ik v_k
-      double acc = 0.0;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const double Wik = (i == k) ? 0.0 : ((k == (i + 1) % 3) ? -w[(i + 2) % 3] : w[(i + 1) % 3]);
-        const double W2ik = w[i] * w[k] - ((i == k) ? t2 : 0.0);
-        acc = fma(((i == k) ? 1.0 : 0.0) + B * Wik + C * W2ik, xi[k], acc);
-      }
-      E[i * 4 + 3] = acc;
-    }
-  } else if (lane < 16) {
-    E[lane] = (lane == 15) ? 1.0 : 0.0;
+  // entry (i, j) of the 3x3 blocks: lanes 0..8 -> R, lanes 16..24 -> V
+  const int e = lane & 15;
+  const int i = e / 3, j = e % 3;
+  const double w[3] = {wx, wy, wz};
+  double val = 0.0;
+  if (e < 9) {
+    // W = hat(w): W[i][j] = -w[(i+2)%3] if j == (i+1)%3, w[(i+1)%3] if j == (i+2)%3
+    const double Wij = (i == j) ? 0.0 : ((j == (i + 1) % 3) ? -w[(i + 2) % 3] : w[(i + 1) % 3]);
+    const double W2ij = fma(w[i], w[j], (i == j) ? -t2 : 0.0);  // W^2 = w w^T - |w|^2 I
+    const double c1 = (lane < 16) ? A : B, c2 = (lane < 16) ? B : C;
+    val = fma(c1, Wij, fma(c2, W2ij, (i == j) ? 1.0 : 0.0));
   }
+  if (lane < 9) E[i * 4 + j] = val;
+  // t_i = sum_k V[i][k] v_k, V[i][k] on lane 16 + 3 i + k
+  const double v0 = __shfl_sync(full, val, 16 + 3 * (lane % 3) + 0);
+  const double v1 = __shfl_sync(full, val, 16 + 3 * (lane % 3) + 1);
+  const double v2 = __shfl_sync(full, val, 16 + 3 * (lane % 3) + 2);
+  if (lane < 3) E[lane * 4 + 3] = fma(v0, xi[0], fma(v1, xi[1], v2 * xi[2]));
+  if (lane >= 12 && lane < 16) E[lane] = (lane == 15) ? 1.0 : 0.0;
   __syncwarp();
 }
 
 // 6x6 Cholesky solve A x = b by one warp.  A: 36 doubles (row-major, full
-// symmetric), b: 6 doubles, x: 6 doubles out; all in shared memory.  Returns
-// the LAPACK potrf verdict (false when a pivot is not > 0 or NaN), uniform
-// across the warp.
+// symmetric), b: 6 doubles, x: 6 doubles out; all in shared memory.  Lane i
+// holds row i; the forward substitution L y = b runs inside the
+// factorisation loop.  Returns the LAPACK potrf verdict (false when a pivot
+// is not > 0 or NaN), uniform across the warp.
 __device__ inline bool warp_cholesky_solve6(const double *A, const double *b, double *x,
                                             double *L /* 36 doubles scratch */, int lane) {
   const unsigned full = 0xffffffffu;
@@ -213,16 +210,21 @@ __device__ inline bool warp_cholesky_solve6(const double *A, const double *b, do
   double row[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) row[k] = A[i * 6 + k];
-  double inv[6];
+  double yi = (lane < 6) ? b[lane] : 0.0;
+  double my_inv = 0.0;
   bool ok = true;
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
     const double d = __shfl_sync(full, row[j], j);
     ok = ok && (d > 0.0);
     if (!ok) break;
-    inv[j] = rsqrt_fp64(d);
-    // column j of L: L[i][j] = A'[i][j] / sqrt(d) for i >= j
-    if (i >= j) row[j] *= inv[j];
+    const double inv = rsqrt_fp64(d);
+    if (lane == j) my_inv = inv;
+    // column j of L and y_j
+    if (i >= j) row[j] *= inv;
+    const double yj = __shfl_sync(full, yi * inv, j);
+    if (lane == j) yi = yj;
+    if (lane > j && lane < 6) yi = fma(-row[j], yj, yi);
     // trailing update A'[i][k] -= L[i][j] L[k][j] for k > j
 #pragma unroll
     for (int k = j + 1; k < 6; ++k) {
@@ -236,19 +238,11 @@ __device__ inline bool warp_cholesky_solve6(const double *A, const double *b, do
     for (int k = 0; k < 6; ++k) L[lane * 6 + k] = (k <= lane) ? row[k] : 0.0;
   }
   __syncwarp();
-  // forward: L y = b (lane i owns y_i / b_i)
-  double yi = lane < 6 ? b[lane] : 0.0;
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    const double yj = __shfl_sync(full, yi * inv[j], j);
-    if (lane == j) yi = yj;
-    if (lane > j && lane < 6) yi = fma(-L[lane * 6 + j], yj, yi);
-  }
   // backward: L^T x = y
   double xi = yi;
 #pragma unroll
   for (int j = 5; j >= 0; --j) {
-    const double xj = __shfl_sync(full, xi * inv[j], j);
+    const double xj = __shfl_sync(full, xi * my_inv, j);
     if (lane == j) xi = xj;
     if (lane < j) xi = fma(-L[j * 6 + lane], xj, xi);
   }

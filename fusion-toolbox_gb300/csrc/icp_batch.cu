@@ -43,6 +43,9 @@ constexpr int kSlotFloats = 64;       // (s[32], c[32]) per partial slot
 constexpr int kMinTile = kThreads * 2;
 constexpr unsigned kSpinLimit = 1u << 26;  // x >= 32 ns sleeps: a few seconds
 constexpr int kJrB = 21, kR2B = 27, kCountGeomB = 28, kCountFeatB = 29;
+// barrier words: [0] root arrivals, [1] generation, [2] error, [8 + g] the
+// arrivals of group g (room for 4088 groups of 8 blocks)
+constexpr size_t kSyncBytes = 16384;
 
 struct LevelP {
   int iters, use_geom, use_feat;
@@ -59,7 +62,8 @@ struct PairState {
 struct BatchArgs {
   const stb_level *levels;
   int B, L, C, dtype, mode, total_iters;
-  int tile;  // pixels per work item: a multiple of kMinTile
+  int tile;          // largest pixels per work item (a multiple of kMinTile)
+  int *level_tile;   // [kMaxLevels] pixels per work item of each level
   LevelP lp[kMaxLevels];
   const double *init;
   double *results, *history;
@@ -78,7 +82,7 @@ struct BatchArgs {
 __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct Layout {
-  size_t sync, ps, key_off, src_off, tgt_off, grp_off, grp_ticket, pair_ticket, tile_part,
+  size_t sync, level_tile, ps, key_off, src_off, tgt_off, grp_off, grp_ticket, pair_ticket, tile_part,
       grp_part, keys, total;
   long long tiles_cap, groups_cap;
 };
@@ -89,6 +93,8 @@ inline Layout layout(int B, long long total_pixels) {
   l.groups_cap = l.tiles_cap / kGroup + B;
   size_t o = 0;
   l.sync = o;
+  o += kSyncBytes;
+  l.level_tile = o;
   o += 256;
   l.ps = o;
   o += al256(sizeof(PairState) * (size_t)B);
@@ -117,20 +123,35 @@ inline Layout layout(int B, long long total_pixels) {
 // ---------------------------------------------------------------------------
 // grid barrier with a bounded wait
 // ---------------------------------------------------------------------------
+// Arrivals are counted in two levels (groups of kBarGroup blocks, then the
+// groups) so that no counter takes more than a few dozen atomics; the last
+// arrival bumps the generation word that the others poll.
+constexpr int kBarGroup = 8;
+
 __device__ bool grid_sync(unsigned *sync) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned *vgen = sync + 1;
     volatile unsigned *verr = sync + 2;
+    unsigned *root = sync;
+    unsigned *group = sync + 8 + blockIdx.x / kBarGroup;
+    const unsigned ngroups = (gridDim.x + kBarGroup - 1) / kBarGroup;
+    const unsigned gsize = min((unsigned)kBarGroup, gridDim.x - (blockIdx.x / kBarGroup) * kBarGroup);
     const unsigned gen = *vgen;
     __threadfence();
-    const unsigned arrived = atomicAdd(sync, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(sync, 0u);
+    bool last = false;
+    if (atomicAdd(group, 1u) == gsize - 1) {
+      atomicExch(group, 0u);
       __threadfence();
-      atomicAdd(sync + 1, 1u);
-    } else {
+      if (atomicAdd(root, 1u) == ngroups - 1) {
+        atomicExch(root, 0u);
+        __threadfence();
+        atomicAdd(sync + 1, 1u);
+        last = true;
+      }
+    }
+    if (!last) {
       unsigned spins = 0;
       while (*vgen == gen) {
         if (*verr) break;
@@ -187,17 +208,37 @@ __device__ void build_offsets(const BatchArgs &a) {
   __shared__ long long carry[5];
   __shared__ long long warp_sum[kThreads / 32][5];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __shared__ long long s_lvl_px;
+  __shared__ int s_tile;
   for (int l = 0; l < a.L; ++l) {
+    // this level's work-item size: the largest power of two (at most a.tile,
+    // at least kMinTile) that still gives every other block an item per phase
+    if (threadIdx.x == 0) s_lvl_px = 0;
+    __syncthreads();
+    long long mine = 0;
+    for (int p = threadIdx.x; p < a.B; p += kThreads) {
+      const stb_level lv = a.levels[(size_t)p * a.L + l];
+      mine += (long long)lv.height * lv.width;
+    }
+    atomicAdd((unsigned long long *)&s_lvl_px, (unsigned long long)mine);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tile = a.tile;
+      while (tile > kMinTile && s_lvl_px / tile < (long long)(gridDim.x / 2)) tile >>= 1;
+      s_tile = tile;
+      a.level_tile[l] = tile;
+    }
     if (threadIdx.x < 5) carry[threadIdx.x] = 0;
     __syncthreads();
+    const int tile = s_tile;
     for (int base = 0; base < a.B; base += kThreads) {
       const int p = base + threadIdx.x;
       long long v[4] = {0, 0, 0, 0};
       if (p < a.B) {
         const stb_level lv = a.levels[(size_t)p * a.L + l];
         const long long npix = (long long)lv.height * lv.width;
-        const long long tt = (npix + a.tile - 1) / a.tile;
-        v[0] = (lv.num_source + a.tile - 1) / a.tile;  // source tiles
+        const long long tt = (npix + tile - 1) / tile;
+        v[0] = (lv.num_source + tile - 1) / tile;  // source tiles
         v[1] = tt;                                         // target tiles
         v[2] = (tt + kGroup - 1) / kGroup;                 // groups
         if (l == a.L - 1) {  // key map: the pair's largest level
@@ -273,27 +314,31 @@ __device__ __forceinline__ float bilin(const T *__restrict__ f, int H, int W, fl
   return fadd(fmul(a0, fsub(1.f, vr)), fmul(a1, vr));
 }
 
-__device__ __forceinline__ void acc_se3(CSum *acc, const float *Jv, float r, float w1,
+// Per-thread partial sums are plain float32: a thread adds at most
+// tile / 256 <= 16 pixels, so its rounding error stays below ~1e-6 of the
+// sum of magnitudes; compensation (TwoSum) starts at the warp level.
+__device__ __forceinline__ void acc_se3(float *acc, const float *Jv, float r, float w1,
                                         float w2) {
 #pragma unroll
   for (int a = 0; a < 6; ++a)
 #pragma unroll
-    for (int b = a; b < 6; ++b) csum_add(acc[upper_index(a, b)], w2 * (Jv[a] * Jv[b]));
+    for (int b = a; b < 6; ++b) acc[upper_index(a, b)] += w2 * (Jv[a] * Jv[b]);
 #pragma unroll
-  for (int a = 0; a < 6; ++a) csum_add(acc[kJrB + a], w1 * (Jv[a] * r));
+  for (int a = 0; a < 6; ++a) acc[kJrB + a] += w1 * (Jv[a] * r);
 }
 
 // block reduction of kN accumulators into smem out_s/out_c (threads < kN)
 template <int kN>
-__device__ __forceinline__ void block_sum(CSum *acc, float *out_s, float *out_c) {
+__device__ __forceinline__ void block_sum(const float *acc_in, float *out_s, float *out_c) {
   __shared__ float ws[kThreads / 32][kN][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int a = 0; a < kN; ++a) {
-    csum_warp_reduce(acc[a]);
+    CSum acc = {acc_in[a], 0.f};
+    csum_warp_reduce(acc);
     if (lane == 0) {
-      ws[warp][a][0] = acc[a].s;
-      ws[warp][a][1] = acc[a].c;
+      ws[warp][a][0] = acc.s;
+      ws[warp][a][1] = acc.c;
     }
   }
   __syncthreads();
@@ -391,7 +436,8 @@ __device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *o
 // ---------------------------------------------------------------------------
 // phase A: association of one source tile
 // ---------------------------------------------------------------------------
-constexpr int kChunk = 2;  // points / pixels per thread per pipelined chunk
+constexpr int kChunk = 4;   // pixels per thread per pipelined reduction chunk
+constexpr int kChunkA = 4;  // points per thread per pipelined association chunk
 
 __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *off, int level,
                                            long long t, int s, bool force, TileCache &tc) {
@@ -404,14 +450,15 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
   const int H = lv.height, W = lv.width;
   unsigned long long *keys = a.keys + __ldcg(a.key_off + p);
   const unsigned long long tag = (unsigned long long)btag(s) << 56;
-  const long long end = min((lt + 1) * (long long)a.tile, (long long)lv.num_source);
-  for (long long base = lt * (long long)a.tile; base < end; base += kThreads * kChunk) {
+  const long long tile = __ldcg(a.level_tile + level);
+  const long long end = min((lt + 1) * tile, (long long)lv.num_source);
+  for (long long base = lt * tile; base < end; base += kThreads * kChunkA) {
     // round 1: source loads
-    float px[kChunk], py[kChunk], pz[kChunk], nx[kChunk], ny[kChunk], nz[kChunk];
-    bool ok[kChunk];
-    long long idx[kChunk];
+    float px[kChunkA], py[kChunkA], pz[kChunkA], nx[kChunkA], ny[kChunkA], nz[kChunkA];
+    bool ok[kChunkA];
+    long long idx[kChunkA];
 #pragma unroll
-    for (int k = 0; k < kChunk; ++k) {
+    for (int k = 0; k < kChunkA; ++k) {
       idx[k] = base + k * kThreads + threadIdx.x;
       ok[k] = idx[k] < end;
       const long long i = ok[k] ? idx[k] : 0;
@@ -424,11 +471,11 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
       nz[k] = __ldg(lv.src_normals + 3 * i + 2);
     }
     // round 2: projection and target gathers
-    float3 Tp[kChunk];
-    long long pix[kChunk];
-    float qx[kChunk], qy[kChunk], qz[kChunk], mx[kChunk], my[kChunk], mz[kChunk];
+    float3 Tp[kChunkA];
+    long long pix[kChunkA];
+    float qx[kChunkA], qy[kChunkA], qz[kChunkA], mx[kChunkA], my[kChunkA], mz[kChunkA];
 #pragma unroll
-    for (int k = 0; k < kChunk; ++k) {
+    for (int k = 0; k < kChunkA; ++k) {
       Tp[k] = transform_point(P.rt, px[k], py[k], pz[k]);
       float u, v;
       project(P, Tp[k], u, v);
@@ -445,7 +492,7 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
     }
     // round 3: gates and the z-buffer
 #pragma unroll
-    for (int k = 0; k < kChunk; ++k) {
+    for (int k = 0; k < kChunkA; ++k) {
       if (!ok[k]) continue;
       const float dx = fsub(qx[k], Tp[k].x), dy = fsub(qy[k], Tp[k].y),
                   dz = fsub(qz[k], Tp[k].z);
@@ -561,26 +608,35 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   const unsigned long long *keys = a.keys + __ldcg(a.key_off + p);
   const unsigned tag = btag(s);
 
-  CSum acc[kN];
+  float acc[kN];
 #pragma unroll
-  for (int k = 0; k < kN; ++k) acc[k] = {0.f, 0.f};
+  for (int k = 0; k < kN; ++k) acc[k] = 0.f;
 
-  const long long end = min((lt + 1) * (long long)a.tile, npix);
-  for (long long base = lt * (long long)a.tile; base < end; base += kThreads * kChunk) {
+  const long long tile = __ldcg(a.level_tile + level);
+  const long long end = min((lt + 1) * tile, npix);
+  for (long long base = lt * tile; base < end; base += kThreads * kChunk) {
+  // round 1: keys and the target point / normal of every pixel (their
+  // addresses do not depend on the key); round 2: the winners' source points
   unsigned long long key[kChunk];
   long long pixs[kChunk];
+  float tq[kChunk][3], tnm[kChunk][3];
   constexpr int kP = kChunk;
 #pragma unroll
   for (int k = 0; k < kP; ++k) {
     pixs[k] = base + k * kThreads + threadIdx.x;
+    const long long pc = (pixs[k] < end) ? pixs[k] : 0;
     key[k] = (pixs[k] < end) ? __ldcg(keys + pixs[k]) : 0ull;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      tq[k][d] = __ldg(lv.tgt_points + 3 * pc + d);
+      tnm[k][d] = (kInfo || !q.use_geom) ? 0.f : __ldg(lv.tgt_normals + 3 * pc + d);
+    }
   }
 #pragma unroll
   for (int k = 0; k < kP; ++k) {
     if ((unsigned)(key[k] >> 56) != tag || pixs[k] >= end) continue;
     const long long pix = pixs[k];
-    const float qx = __ldg(lv.tgt_points + 3 * pix), qy = __ldg(lv.tgt_points + 3 * pix + 1),
-                qz = __ldg(lv.tgt_points + 3 * pix + 2);
+    const float qx = tq[k][0], qy = tq[k][1], qz = tq[k][2];
     if (kInfo) {
       const float G0[6] = {0.f, qz, -qy, 1.f, 0.f, 0.f};
       const float G1[6] = {-qz, 0.f, qx, 0.f, 1.f, 0.f};
@@ -589,7 +645,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
       for (int i = 0; i < 6; ++i)
 #pragma unroll
         for (int j = i; j < 6; ++j)
-          csum_add(acc[upper_index(i, j)], G0[i] * G0[j] + G1[i] * G1[j] + G2[i] * G2[j]);
+          acc[upper_index(i, j)] += G0[i] * G0[j] + G1[i] * G1[j] + G2[i] * G2[j];
       continue;
     }
     const long long i = (long long)(key[k] & 0xffffffull);
@@ -597,15 +653,14 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
                                       __ldg(lv.src_points + 3 * i + 1),
                                       __ldg(lv.src_points + 3 * i + 2));
     if (q.use_geom) {
-      const float nx = __ldg(lv.tgt_normals + 3 * pix), ny = __ldg(lv.tgt_normals + 3 * pix + 1),
-                  nz = __ldg(lv.tgt_normals + 3 * pix + 2);
+      const float nx = tnm[k][0], ny = tnm[k][1], nz = tnm[k][2];
       const float r = dot3(fsub(qx, Tp.x), fsub(qy, Tp.y), fsub(qz, Tp.z), nx, ny, nz);
       const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
                            fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
                            fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
       acc_se3(acc, Jv, r, q.wg1, q.wg2);
-      csum_add(acc[kR2B], q.wg1 * (r * r));
-      csum_add(acc[kCountGeomB], 1.f);
+      acc[kR2B] += q.wg1 * (r * r);
+      acc[kCountGeomB] += 1.f;
     }
     if (kFeat && q.use_feat) {
       const FT *tf = static_cast<const FT *>(lv.tgt_feats);
@@ -640,8 +695,8 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
                                fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
           acc_se3(acc, Jv, r, -q.wf1, q.wf2);
         }
-        csum_add(acc[kR2B], q.wf1 * sq);
-        csum_add(acc[kCountFeatB], 1.f);
+        acc[kR2B] += q.wf1 * sq;
+        acc[kCountFeatB] += 1.f;
       }
     }
   }
@@ -881,8 +936,8 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
                 lay.total);
   if (((uintptr_t)workspace & 255) != 0)
     return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
-  if (tile_config < 0 || tile_config > 4)
-    return fail(STB_EINVAL, "Check failed: tile_config must be in [0, 4]");
+  if (tile_config < 0 || tile_config > 5)
+    return fail(STB_EINVAL, "Check failed: tile_config must be in [0, 5]");
   STB_TRY(check_device_ptr(levels, "levels"));
   STB_TRY(check_device_ptr(init_transforms, "init_transforms", true));
   STB_TRY(check_device_ptr(workspace, "workspace"));
@@ -898,8 +953,10 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   a.dtype = feat_dtype;
   a.mode = channel_mode;
   a.total_iters = total_iters;
-  // pixels per work item: 0 -> default, 1..4 -> 512, 1024, 2048, 4096
-  a.tile = kMinTile << (tile_config == 0 ? 1 : tile_config - 1);
+  // largest pixels per work item: 0 -> default (8192), 1..5 -> 512 ... 8192;
+  // each level uses the largest power of two below it that still gives
+  // every block several work items
+  a.tile = kMinTile << (tile_config == 0 ? 4 : tile_config - 1);
   for (int l = 0; l < kMaxLevels; ++l) {
     LevelP &q = a.lp[l];
     if (l >= num_levels) {
@@ -923,6 +980,7 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   a.results = results;
   a.history = history;
   a.sync = reinterpret_cast<unsigned *>(ws + lay.sync);
+  a.level_tile = reinterpret_cast<int *>(ws + lay.level_tile);
   a.ps = reinterpret_cast<PairState *>(ws + lay.ps);
   a.key_off = reinterpret_cast<long long *>(ws + lay.key_off);
   a.src_off = reinterpret_cast<long long *>(ws + lay.src_off);
@@ -939,7 +997,8 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
 
   const cudaStream_t st = as_stream(stream);
   // barrier counters start at zero for every launch
-  if (cudaMemsetAsync(a.sync, 0, 256, st) != cudaSuccess) return check_launch("cudaMemsetAsync");
+  if (cudaMemsetAsync(a.sync, 0, kSyncBytes, st) != cudaSuccess)
+    return check_launch("cudaMemsetAsync");
   if (!any_feat) return launch_batch<float, false>(a, st);
   if (feat_dtype == STB_F32) return launch_batch<float, true>(a, st);
   return launch_batch<__nv_bfloat16, true>(a, st);

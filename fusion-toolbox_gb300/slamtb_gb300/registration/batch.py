@@ -41,7 +41,7 @@ class BatchRegistration:
         self.feat_channel_mode = feat_channel_mode
         self.record_history = record_history
         self.last_history = None
-        self.tile_config = 0  # 0 default; 1..4: 512, 1024, 2048, 4096 pixels per work item
+        self.tile_config = 0  # largest pixels per work item: 0 -> 8192; 1..5 -> 512 ... 8192
         self._ws = None
 
     @property

@@ -289,7 +289,9 @@ STB_API size_t stb_icp_batch_workspace_bytes(int32_t num_pairs,
  * height * width.  results: device float64
  * [num_pairs][STB_RES_SIZE] (the last level's RegistrationResult).
  * history: NULL or device float64 [num_pairs][sum of num_iters][STB_HIST_SIZE].
- * tile_config: 0 default; 1..3 select 2, 4 or 8 pixels per thread.
+ * tile_config: largest pixels per work item, 0 = 8192, 1..5 = 512 <<
+ * (tile_config - 1); every level uses the largest power of two up to it that
+ * still gives half of the blocks a work item per phase.
  */
 STB_API int stb_icp_estimate_batch(
     const stb_level *levels, int32_t num_pairs, int32_t num_levels,
