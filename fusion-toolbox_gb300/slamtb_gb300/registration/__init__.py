@@ -5,7 +5,9 @@ from .result import RegistrationResult, RegistrationVerifier
 from .correspondence_map import CorrespondenceMap
 from .preset import create_multiscale_odometry
 from .batch import BatchRegistration
+from .grad import PointToPlaneLoss, point_to_plane_loss, se3_exp_compose
 
 __all__ = ["ICPOdometry", "MultiscaleRegistration", "MultiscaleICPOdometry",
            "RegistrationResult", "RegistrationVerifier", "CorrespondenceMap",
-           "create_multiscale_odometry", "BatchRegistration"]
+           "create_multiscale_odometry", "BatchRegistration", "PointToPlaneLoss",
+           "point_to_plane_loss", "se3_exp_compose"]

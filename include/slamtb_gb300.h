@@ -300,6 +300,73 @@ STB_API int stb_icp_estimate_batch(
     int64_t total_target_pixels, void *workspace, size_t workspace_bytes,
     double *results, double *history, int32_t tile_config, void *stream);
 
+/* ======================================================================= *
+ * Differentiable point-to-plane loss (hand-written adjoint)
+ * ======================================================================= */
+
+/*
+ * out[p] = exp(twist[p]) * base[p] for p < num_pairs: FP64 SE(3)
+ * exponential of [translation; rotation] twists and left composition.
+ * twist: device float64 [num_pairs][6]; base, out: [num_pairs][16].  No
+ * counterpart in the reference (it uses tenviz SE3.exp on the CPU,
+ * icp.py:245-247).
+ */
+STB_API int stb_se3_exp_compose(const double *twist, const double *base,
+                                double *out, int32_t num_pairs, void *stream);
+
+/*
+ * grad_twist[p] = J_l(twist[p])^T grad_tangent[p]: turns the gradient of a
+ * loss with respect to the left perturbation of exp(twist) * base (what
+ * stb_icp_loss_backward returns) into its gradient with respect to twist.
+ * J_l is the SE(3) left Jacobian of [translation; rotation] twists, summed
+ * in FP64 from its power series.  All arrays device float64 [num_pairs][6].
+ */
+STB_API int stb_se3_twist_grad(const double *twist, const double *grad_tangent,
+                               double *grad_twist, int32_t num_pairs, void *stream);
+
+/* Workspace bytes of stb_icp_loss_forward / _backward. */
+STB_API size_t stb_icp_loss_workspace_bytes(int32_t num_pairs,
+                                            int64_t max_target_pixels);
+
+/*
+ * Point-to-plane loss L_p = sum over correspondences of ((q - T_p s).n)^2
+ * for each pair p at pose T_p (device float64 [num_pairs][16]): the
+ * association of ICPOdometry (thresholds as stb_icp_estimate) at the float32
+ * cast of T_p, then the residuals of the geometric term
+ * (icp_jacobian_geometric.cu:82) summed in compensated float32 into
+ * loss[p] (device float64 [num_pairs]).  levels: device stb_level
+ * [num_pairs] (one level per pair; feature fields ignored); every pair's
+ * height * width must be <= max_target_pixels.  The correspondences stay
+ * in the workspace for stb_icp_loss_backward.  No counterpart in the
+ * reference (its autograd ICP differentiates through PyTorch ops,
+ * slamtb/registration/autogradicp.py:145-239).
+ */
+STB_API int stb_icp_loss_forward(const stb_level *levels, int32_t num_pairs,
+                                 const double *poses, double distance_thresh,
+                                 double normal_angle_thresh,
+                                 int64_t max_target_pixels, void *workspace,
+                                 size_t workspace_bytes, double *loss,
+                                 void *stream);
+
+/*
+ * Adjoint of stb_icp_loss_forward at the correspondences it found (same
+ * levels, poses and workspace): with g = grad_loss[p],
+ *   grad_twist[p] = g * dL_p/dxi = -2 g sum r J,  J = [n; Tp x n], for the
+ *     left perturbation T <- exp(xi) T_p (device float64 [num_pairs][6]),
+ *   grad_depth[p][i] = g * dL_p/dz_i = -2 g r_i (R^T n).((u_i - cx)/fx,
+ *     (v_i - cy)/fy, 1) for the source pixel i = v_i * width + u_i (the
+ *     source grid has the target's size and intrinsics), 0 where source
+ *     pixel i has no correspondence (device float32 array per pair:
+ *     grad_depth is a device array [num_pairs] of pointers).
+ * Either output may be NULL.  Source normals only gate the association and
+ * get no gradient.
+ */
+STB_API int stb_icp_loss_backward(const stb_level *levels, int32_t num_pairs,
+                                  const double *poses, const double *grad_loss,
+                                  int64_t max_target_pixels, void *workspace,
+                                  size_t workspace_bytes, double *grad_twist,
+                                  float *const *grad_depth, void *stream);
+
 /*
  * stb_icp_estimate without any allocation.  No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc while they track -- C or

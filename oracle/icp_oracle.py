@@ -754,3 +754,104 @@ def multiscale_estimate(levels, estimators, transform=None):
         result = icp_estimate(transform=transform, **level, **est)
         transform = result.transform
     return result
+
+
+# ---------------------------------------------------------------------------
+# point-to-plane loss with frozen correspondences (the differentiable form
+# of icp_jacobian_geometric.cu:82; J convention icp_jacobian_common.hpp:41-48)
+# ---------------------------------------------------------------------------
+
+class LossMatches:
+    """Frozen correspondences of an association: source index ``idx``,
+    target point ``q`` and normal ``n`` (float64 of the float32 inputs),
+    and the matched target pixel ``pix``."""
+
+    def __init__(self, assoc, tgt_points, tgt_normals):
+        win = assoc.winner.reshape(-1)
+        self.pix = np.nonzero(win >= 0)[0]
+        self.idx = win[self.pix]
+        self.q = np.asarray(tgt_points, dtype=F32).reshape(-1, 3)[self.pix].astype(F64)
+        self.n = np.asarray(tgt_normals, dtype=F32).reshape(-1, 3)[self.pix].astype(F64)
+
+
+def loss_residuals64(T, src_points, m):
+    """r = (q - (R s + t)).n in float64 at a float64 pose."""
+    T = np.asarray(T, dtype=F64)
+    s = np.asarray(src_points, dtype=F32).reshape(-1, 3)[m.idx].astype(F64)
+    p = s @ T[:3, :3].T + T[:3, 3]
+    return ((m.q - p) * m.n).sum(axis=1)
+
+
+def point_to_plane_loss64(T, src_points, m):
+    r = loss_residuals64(T, src_points, m)
+    return float((r * r).sum())
+
+
+def loss_twist_grad_fd(T0, twist, src_points, m, h=1e-6):
+    """Central differences of L(exp(twist) T0) over the six twist
+    components (float64)."""
+    twist = np.asarray(twist, dtype=F64)
+    g = np.zeros(6)
+    for k in range(6):
+        e = np.zeros(6)
+        e[k] = h
+        lp = point_to_plane_loss64(se3_exp(twist + e) @ T0, src_points, m)
+        lm = point_to_plane_loss64(se3_exp(twist - e) @ T0, src_points, m)
+        g[k] = (lp - lm) / (2.0 * h)
+    return g
+
+
+def loss_twist_grad64(T, src_points, m):
+    """Analytic left-perturbation gradient -2 sum r J, J = [n; Tp x n]
+    (float64), and the scale sum 2 |J| |r| its errors are measured against."""
+    T = np.asarray(T, dtype=F64)
+    s = np.asarray(src_points, dtype=F32).reshape(-1, 3)[m.idx].astype(F64)
+    p = s @ T[:3, :3].T + T[:3, 3]
+    r = ((m.q - p) * m.n).sum(axis=1)
+    J = np.concatenate([m.n, np.cross(p, m.n)], axis=1)
+    return -2.0 * (J.T @ r), float(2.0 * (np.linalg.norm(J, axis=1) * np.abs(r)).sum())
+
+
+def loss_depth_grad_fd(T, src_points, m, kcam, width, pixels, h=1e-6):
+    """Central differences of L with respect to the depth of the source
+    pixels ``pixels`` (flat indices): the source point moves along its
+    back-projection ray d = ((u - cx)/fx, (v - cy)/fy, 1)
+    (slamtb/camera.py:127-149).  Returns (grad, r, a) with a = dr/dz, 0
+    for pixels without a correspondence."""
+    fx, fy, cx, cy = (float(kcam[0][0]), float(kcam[1][1]), float(kcam[0][2]),
+                      float(kcam[1][2]))
+    T = np.asarray(T, dtype=F64)
+    R, t = T[:3, :3], T[:3, 3]
+    sp = np.asarray(src_points, dtype=F32).reshape(-1, 3).astype(F64)
+    where = {int(i): k for k, i in enumerate(m.idx)}
+    out = np.zeros(len(pixels))
+    rr = np.zeros(len(pixels))
+    aa = np.zeros(len(pixels))
+    for j, i in enumerate(pixels):
+        k = where.get(int(i))
+        if k is None:
+            continue
+        u, v = i % width, i // width
+        d = np.array([(u - cx) / fx, (v - cy) / fy, 1.0])
+
+        def r_of(dz):
+            p = R @ (sp[i] + dz * d) + t
+            return float((m.q[k] - p) @ m.n[k])
+
+        out[j] = (r_of(h) ** 2 - r_of(-h) ** 2) / (2.0 * h)
+        rr[j] = r_of(0.0)
+        aa[j] = -float((R.T @ m.n[k]) @ d)
+    return out, rr, aa
+
+
+def se3_left_jacobian_fd(xi, h=1e-6):
+    """Columns log(exp(xi + h e_k) exp(xi)^-1) by central differences:
+    the SE(3) left Jacobian, exp(xi + d) = exp(J d) exp(xi) + O(|d|^2)."""
+    xi = np.asarray(xi, dtype=F64)
+    Einv = np.linalg.inv(se3_exp(xi))
+    J = np.zeros((6, 6))
+    for k in range(6):
+        e = np.zeros(6)
+        e[k] = h
+        J[:, k] = (se3_log(se3_exp(xi + e) @ Einv) - se3_log(se3_exp(xi - e) @ Einv)) / (2 * h)
+    return J

@@ -1,0 +1,216 @@
+"""Differentiable point-to-plane loss (PointToPlaneLoss -> stb_icp_loss_forward
+/ _backward / stb_se3_twist_grad) against the FP64 oracle.
+
+Each pair is registered for 5 Gauss-Newton iterations first; the loss and its
+gradients are taken at that pose, rounded to float32 so that the kernels'
+float32 pose is the oracle's pose exactly.  Tolerances (all written below):
+
+* loss: 1e-5 relative to the FP64 sum of squares over the same (bit-exact)
+  correspondences;
+* twist gradient: per component within 1e-5 of sum 2 |J| |r| (the scale of
+  the Jacobian-residual products, the Jtr gate of the registration tests)
+  against FP64 central differences (step 1e-6) and against -2 J^T r summed
+  from the reference-layout per-point partials of ICPJacobian;
+* depth gradient at 64 sampled matched pixels per pair: within
+  1e-5 |dL/dz| + 2 |dr/dz| * 8 eps32 (|q| + |Tp|), the float32 rounding
+  bound of the residual r = (q - Tp).n, against FP64 central differences
+  (step 1e-6); exactly 0 at pixels without a correspondence.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import icp_oracle as io
+from _helpers import synthetic_pair
+
+pytestmark = pytest.mark.gpu
+
+DIST = 0.1
+ANGLE = math.radians(20)
+EPS32 = 2.0 ** -24
+
+
+def _t(x, dev, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+    return t if dtype is None else t.to(dtype)
+
+
+def _batch(cuda, seeds, w, h):
+    from slamtb_gb300.registration import ICPOdometry
+    icp = ICPOdometry(5, geom_weight=1.0, feat_weight=0.0, distance_threshold=DIST,
+                      normals_angle_thresh=ANGLE)
+    pairs, poses = [], []
+    for seed in seeds:
+        d = synthetic_pair(seed, width=w, height=h)
+        s, t = d["src"], d["tgt"]
+        res = icp.estimate(_t(d["kcam"], cuda), _t(s["points"], cuda), _t(s["normals"], cuda),
+                           _t(s["mask"], cuda), target_points=_t(t["points"], cuda),
+                           target_normals=_t(t["normals"], cuda), target_mask=_t(t["mask"], cuda))
+        T0 = res.transform.numpy().astype(np.float32).astype(np.float64)
+        pairs.append(d)
+        poses.append(T0)
+    return pairs, np.stack(poses)
+
+
+def _inputs(cuda, pairs):
+    st = lambda key, part: torch.stack([_t(d[part][key], cuda) for d in pairs])
+    depth = torch.stack([_t(d["src_fpcl"].points[..., 2], cuda) for d in pairs])
+    return dict(source_depth=depth, source_normals=st("normals", "src"),
+                source_mask=st("mask", "src"), target_points=st("points", "tgt"),
+                target_normals=st("normals", "tgt"), target_mask=st("mask", "tgt"))
+
+
+def _kcam_params(K):
+    return (float(K[0][0]), float(K[1][1]), float(K[0][2]), float(K[1][2]))
+
+
+def _oracle(d, T0):
+    s, t = d["src"], d["tgt"]
+    a = io.associate32(s["points"], s["normals"], s["mask"], io.pose_rt32(T0), t["points"],
+                       t["normals"], t["mask"], d["kcam"], DIST, ANGLE)
+    return a, io.LossMatches(a, t["points"], t["normals"])
+
+
+@pytest.fixture(scope="module")
+def batch(cuda):
+    pairs, poses = _batch(cuda, [70, 71, 72], 320, 240)
+    return pairs, poses
+
+
+def _run(cuda, pairs, poses, twist=None):
+    from slamtb_gb300.registration import point_to_plane_loss
+    B = len(pairs)
+    inp = _inputs(cuda, pairs)
+    inp["source_depth"].requires_grad_(True)
+    if twist is None:
+        twist = np.zeros((B, 6))
+    tw = torch.tensor(twist, dtype=torch.float64, device=cuda, requires_grad=True)
+    loss = point_to_plane_loss(tw, kcam=_kcam_params(pairs[0]["kcam"]),
+                               poses=torch.from_numpy(poses).to(cuda), distance_threshold=DIST,
+                               normals_angle_thresh=ANGLE, **inp)
+    loss.sum().backward()
+    return loss.detach().cpu().numpy(), tw.grad.cpu().numpy(), \
+        inp["source_depth"].grad.cpu().numpy()
+
+
+def test_source_points_match_oracle_backprojection(cuda, batch):
+    """The loss back-projects the source depth on the device; the points
+    must be the oracle's float32 points bit for bit."""
+    from slamtb_gb300 import processing
+    pairs, _ = batch
+    d = pairs[0]
+    depth = _t(d["src_fpcl"].points[..., 2], cuda)
+    pts, _ = processing.depth_to_points(depth, torch.tensor(d["kcam"], dtype=torch.float32))
+    np.testing.assert_array_equal(pts.cpu().numpy(), d["src"]["points"])
+
+
+def test_loss_matches_fp64_oracle(cuda, batch):
+    pairs, poses = batch
+    loss, _, _ = _run(cuda, pairs, poses)
+    for p, d in enumerate(pairs):
+        _, m = _oracle(d, poses[p])
+        assert m.idx.size > 1000
+        ref = io.point_to_plane_loss64(poses[p], d["src"]["points"], m)
+        assert loss[p] == pytest.approx(ref, rel=1e-5)
+
+
+def test_twist_grad_vs_fd_and_reference_jacobian(cuda, batch):
+    from slamtb_gb300._cslamtb import CorrespondenceMap, ICPJacobian
+    pairs, poses = batch
+    _, gtw, _ = _run(cuda, pairs, poses)
+    for p, d in enumerate(pairs):
+        _, m = _oracle(d, poses[p])
+        sp = d["src"]["points"]
+        fd = io.loss_twist_grad_fd(poses[p], np.zeros(6), sp, m, h=1e-6)
+        an, scale = io.loss_twist_grad64(poses[p], sp, m)
+        assert np.abs(fd - an).max() <= 1e-7 * scale      # the oracle against itself
+        assert np.abs(gtw[p] - fd).max() <= 1e-5 * scale
+        # -2 J^T r from the reference-layout per-point partials
+        s, t = d["src"], d["tgt"]
+        h, w = t["mask"].shape
+        cmap = torch.full((h, w), io.CORRESP_EMPTY, dtype=torch.int64, device=cuda)
+        rt = _t(poses[p], cuda, torch.float32)
+        CorrespondenceMap.compute_correspondence_map(
+            _t(s["points"], cuda).view(-1, 3), _t(s["normals"], cuda).view(-1, 3),
+            _t(s["mask"], cuda).view(-1), rt, _t(t["points"], cuda), _t(t["normals"], cuda),
+            _t(t["mask"], cuda), _t(d["kcam"], cuda), cmap, DIST, ANGLE)
+        n = h * w
+        JtJ = torch.zeros(n, 6, 6, device=cuda)
+        Jr = torch.zeros(n, 6, device=cuda)
+        r2 = torch.zeros(n, device=cuda)
+        cnt = ICPJacobian.estimate_geometric(
+            _t(s["points"], cuda).view(-1, 3), _t(s["mask"], cuda).view(-1), rt,
+            _t(t["points"], cuda), _t(t["normals"], cuda), _t(d["kcam"], cuda), cmap, JtJ, Jr, r2)
+        assert cnt == m.idx.size
+        ref = -2.0 * Jr.double().sum(0).cpu().numpy()
+        assert np.abs(gtw[p] - ref).max() <= 1e-5 * scale
+
+
+def test_depth_grad_vs_fd(cuda, batch):
+    pairs, poses = batch
+    _, _, gz = _run(cuda, pairs, poses)
+    rng = np.random.default_rng(5)
+    for p, d in enumerate(pairs):
+        _, m = _oracle(d, poses[p])
+        h, w = d["tgt"]["mask"].shape
+        g = gz[p].reshape(-1)
+        unmatched = np.ones(h * w, dtype=bool)
+        unmatched[m.idx] = False
+        assert np.all(g[unmatched] == 0.0)
+        pix = rng.choice(m.idx, size=64, replace=False)
+        fd, r, a = io.loss_depth_grad_fd(poses[p], d["src"]["points"], m, d["kcam"], w, pix,
+                                         h=1e-6)
+        sp = d["src"]["points"].reshape(-1, 3)[pix].astype(np.float64)
+        tp = sp @ poses[p][:3, :3].T + poses[p][:3, 3]
+        where = {int(i): k for k, i in enumerate(m.idx)}
+        q = m.q[[where[int(i)] for i in pix]]
+        bound = 1e-5 * np.abs(fd) + 2.0 * np.abs(a) * 8 * EPS32 * (
+            np.abs(q).sum(1) + np.abs(tp).sum(1))
+        assert np.all(np.abs(g[pix] - fd) <= bound)
+        assert np.all(fd != 0.0)
+
+
+def test_twist_grad_maps_through_left_jacobian(cuda):
+    """stb_se3_twist_grad against the central-difference left Jacobian of the
+    oracle's exp / log."""
+    from slamtb_gb300 import _native as N
+    rng = np.random.default_rng(9)
+    xi = np.concatenate([rng.normal(0, 0.3, (8, 3)), rng.normal(0, 0.5, (8, 3))], axis=1)
+    xi[0] = 0.0
+    xi[1, 3:] = [1e-9, 0.0, 0.0]
+    g = rng.normal(size=(8, 6))
+    txi, tg = _t(xi, cuda), _t(g, cuda)
+    out = torch.empty_like(tg)
+    N.check(N.lib().stb_se3_twist_grad(N.ptr(txi), N.ptr(tg), N.ptr(out), 8, N.stream_of(cuda)))
+    out = out.cpu().numpy()
+    np.testing.assert_array_equal(out[0], g[0])
+    for k in range(8):
+        J = io.se3_left_jacobian_fd(xi[k])
+        np.testing.assert_allclose(out[k], J.T @ g[k], rtol=1e-6, atol=1e-7 * np.abs(g[k]).sum())
+
+
+def test_nonzero_twist_grad_vs_fd(cuda, batch):
+    """At twist != 0 the kernels run at the float32 cast of exp(twist) T0:
+    the gradient agrees with FP64 central differences of L(exp(twist) T0)
+    up to that cast (tolerance 1e-3 of the scale)."""
+    pairs, poses = batch
+    twist = np.tile([[2e-3, -1e-3, 1.5e-3, 1e-3, 2e-3, -1.5e-3]], (len(pairs), 1))
+    _, gtw, _ = _run(cuda, pairs, poses, twist)
+    for p, d in enumerate(pairs):
+        T = io.se3_exp(twist[p]) @ poses[p]
+        _, m = _oracle(d, T)
+        fd = io.loss_twist_grad_fd(poses[p], twist[p], d["src"]["points"], m, h=1e-6)
+        _, scale = io.loss_twist_grad64(T, d["src"]["points"], m)
+        assert np.abs(gtw[p] - fd).max() <= 1e-3 * scale
+
+
+def test_loss_is_zero_without_correspondences(cuda, batch):
+    pairs, poses = batch
+    d = dict(pairs[0])
+    d["tgt"] = dict(d["tgt"])
+    d["tgt"]["mask"] = np.zeros_like(d["tgt"]["mask"])
+    loss, gtw, gz = _run(cuda, [d, pairs[1]], poses[:2])
+    assert loss[0] == 0.0 and np.all(gtw[0] == 0.0) and np.all(gz[0] == 0.0)
+    assert loss[1] > 0.0

@@ -206,3 +206,43 @@ def test_normals_of_a_plane():
     inner = nr[1:-1, 1:-1].reshape(-1, 3)
     dots = np.abs(inner @ n)
     assert dots.min() > 0.999
+
+
+def _ad(xi):
+    A = np.zeros((6, 6))
+    A[:3, :3] = io._hat(xi[3:])
+    A[:3, 3:] = io._hat(xi[:3])
+    A[3:, 3:] = io._hat(xi[3:])
+    return A
+
+
+@pytest.mark.parametrize("scale", [0.0, 1e-4, 0.3, 1.5])
+def test_se3_left_jacobian_series(scale):
+    """The power series sum ad^n / (n+1)! that stb_se3_twist_grad sums is
+    the left Jacobian of the oracle's exp (central differences of log)."""
+    rng = np.random.default_rng(int(scale * 10) + 3)
+    xi = rng.normal(size=6) * scale
+    S, term = np.eye(6), np.eye(6)
+    for n in range(1, 60):
+        term = term @ _ad(xi) / (n + 1)
+        S = S + term
+    np.testing.assert_allclose(io.se3_left_jacobian_fd(xi), S, atol=1e-8)
+
+
+def test_loss_gradients_fd_vs_analytic():
+    """Oracle self-check of the loss gradients on a small synthetic pair:
+    the analytic -2 sum r J and dr/dz against central differences."""
+    from _helpers import synthetic_pair
+    d = synthetic_pair(3, width=80, height=60)
+    s, t = d["src"], d["tgt"]
+    T = io.se3_exp([0.004, -0.003, 0.002, 0.003, -0.002, 0.001])
+    a = io.associate32(s["points"], s["normals"], s["mask"], io.pose_rt32(T), t["points"],
+                       t["normals"], t["mask"], d["kcam"], 0.1, math.radians(20))
+    m = io.LossMatches(a, t["points"], t["normals"])
+    assert m.idx.size > 500
+    an, scale = io.loss_twist_grad64(T, s["points"], m)
+    fd = io.loss_twist_grad_fd(T, np.zeros(6), s["points"], m)
+    assert np.abs(an - fd).max() <= 1e-7 * scale
+    pix = m.idx[:16]
+    g, r, dr = io.loss_depth_grad_fd(T, s["points"], m, d["kcam"], 80, pix)
+    np.testing.assert_allclose(g, 2 * r * dr, rtol=1e-6, atol=1e-12)
