@@ -192,41 +192,49 @@ __device__ __forceinline__ float bilinear(const T *__restrict__ f, int H, int W,
   return fadd(fmul(a0, fsub(1.f, vr)), fmul(a1, vr));
 }
 
-__device__ __forceinline__ void accumulate_se3(CSum *acc, const float *Jv, float r,
-                                               float w1, float w2) {
+__device__ __forceinline__ void accumulate_se3(float *acc, const float *Jv, float r, float w1,
+                                               float w2) {
 #pragma unroll
   for (int a = 0; a < 6; ++a)
 #pragma unroll
-    for (int b = a; b < 6; ++b) csum_add(acc[upper_index(a, b)], w2 * (Jv[a] * Jv[b]));
+    for (int b = a; b < 6; ++b) acc[upper_index(a, b)] += w2 * (Jv[a] * Jv[b]);
 #pragma unroll
-  for (int a = 0; a < 6; ++a) csum_add(acc[kJr + a], w1 * (Jv[a] * r));
+  for (int a = 0; a < 6; ++a) acc[kJr + a] += w1 * (Jv[a] * r);
 }
 
-// Block-level compensated reduction of `nacc` accumulators; thread 0..nacc-1
-// of the block end with the block totals in out_s / out_c (shared).
+// Block-level compensated reduction of kN per-thread float32 partials,
+// transposed through shared memory: thread t stores its partial a at
+// red[a][t]; warp w then sums accumulators w, w + 8, ... (each lane eight
+// of the block's threads with TwoSum, then the warp's lanes by shuffles).
+// This costs ~kN / 8 warp reductions per warp instead of kN.  Threads
+// 0..kN-1 of the block end with the totals in out_s / out_c (shared).
 template <int kN>
-__device__ __forceinline__ void block_reduce(CSum *acc, float (*ws)[kN][2], float *out_s,
-                                             float *out_c) {
+__device__ __forceinline__ void block_reduce(const float *acc, float (*red)[kReduceThreads],
+                                             float *out_s, float *out_c) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int a = 0; a < kN; ++a) {
-    csum_warp_reduce(acc[a]);
+  for (int a = 0; a < kN; ++a) red[a][threadIdx.x] = acc[a];
+  __syncthreads();
+  for (int a = warp; a < kN; a += kReduceThreads / 32) {
+    float v[kReduceThreads / 32];
+#pragma unroll
+    for (int j = 0; j < kReduceThreads / 32; ++j) v[j] = red[a][lane + 32 * j];
+    CSum t = {v[0], 0.f};
+#pragma unroll
+    for (int j = 1; j < kReduceThreads / 32; ++j) csum_add(t, v[j]);
+    csum_warp_reduce(t);
     if (lane == 0) {
-      ws[warp][a][0] = acc[a].s;
-      ws[warp][a][1] = acc[a].c;
+      out_s[a] = t.s;
+      out_c[a] = t.c;
     }
   }
   __syncthreads();
-  if (threadIdx.x < kN) {
-    CSum t = {0.f, 0.f};
-    const int nw = blockDim.x >> 5;
-    for (int w = 0; w < nw; ++w) csum_merge(t, ws[w][threadIdx.x][0], ws[w][threadIdx.x][1]);
-    out_s[threadIdx.x] = t.s;
-    out_c[threadIdx.x] = t.c;
-  }
 }
 
-// Last block: FP64 totals of kN accumulators from all block partials.
+// Last block: FP64 totals of kN accumulators from all block partials.  Every
+// load of a lane is issued before its additions (up to kFoldLoads slots per
+// lane per round), so the fold costs a few L2 round trips, not one per slot.
+constexpr int kFoldLoads = 8;
 template <int kN>
 __device__ __forceinline__ void grid_totals(const float *part_s, const float *part_c,
                                             int nblocks, double *tot) {
@@ -234,70 +242,97 @@ __device__ __forceinline__ void grid_totals(const float *part_s, const float *pa
   const int nw = blockDim.x >> 5;
   for (int a = warp; a < kN; a += nw) {
     CSum t = {0.f, 0.f};
-    for (int b = lane; b < nblocks; b += 32)
-      csum_merge(t, __ldcg(part_s + a * nblocks + b), __ldcg(part_c + a * nblocks + b));
+    for (int b0 = 0; b0 < nblocks; b0 += 32 * kFoldLoads) {
+      float vs[kFoldLoads], vc[kFoldLoads];
+#pragma unroll
+      for (int k = 0; k < kFoldLoads; ++k) {
+        const int b = b0 + lane + 32 * k;
+        vs[k] = (b < nblocks) ? __ldcg(part_s + a * nblocks + b) : 0.f;
+        vc[k] = (b < nblocks) ? __ldcg(part_c + a * nblocks + b) : 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < kFoldLoads; ++k) csum_merge(t, vs[k], vc[k]);
+    }
     csum_warp_reduce(t);
     if (lane == 0) tot[a] = (double)t.s + (double)t.c;
   }
 }
 
-// One Gauss-Newton step from the FP64 totals (single thread).
-__device__ void gn_step(const Job *J, const double *tot, int iter) {
+// One Gauss-Newton step from the FP64 totals in shared memory, by one warp
+// (the warp-parallel Cholesky, exponential and composition of gn_solve.cuh).
+__device__ void gn_step_warp(const Job *J, const double *tot, int iter) {
+  __shared__ double A[36], b[6], x[6], L[36], E[16], T[16], Tn[16];
+  const int lane = threadIdx.x & 31;
   State *S = J->state;
-  double A[36], b[6], x[6];
-#pragma unroll
-  for (int a = 0; a < 6; ++a)
-#pragma unroll
-    for (int c = a; c < 6; ++c) A[a * 6 + c] = A[c * 6 + a] = tot[upper_index(a, c)];
-#pragma unroll
-  for (int a = 0; a < 6; ++a) b[a] = tot[kJr + a];
-  const double r2 = tot[kR2];
+  for (int k = lane; k < 36; k += 32) {
+    const int r = k / 6, c = k % 6;
+    A[k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
+  }
+  if (lane < 6) b[lane] = tot[kJr + lane];
+  if (lane < 16) T[lane] = __ldcg(S->T + lane);
+  __syncwarp();
   const double cg = tot[kCountGeom], cf = tot[kCountFeat];
   const double count = J->use_geom ? fmax(cg, cf) : cf;
   double *H = J->history ? J->history + (size_t)iter * STB_HIST_SIZE : nullptr;
   if (H) {
-    for (int k = 0; k < 36; ++k) H[STB_HIST_JTJ + k] = A[k];
-    for (int k = 0; k < 6; ++k) H[STB_HIST_JR + k] = b[k];
-    H[STB_HIST_R2] = r2;
-    H[STB_HIST_GEOM_COUNT] = cg;
-    H[STB_HIST_FEAT_COUNT] = cf;
+    for (int k = lane; k < 36; k += 32) H[STB_HIST_JTJ + k] = A[k];
+    if (lane < 6) H[STB_HIST_JR + lane] = b[lane];
+    if (lane == 0) {
+      H[STB_HIST_R2] = tot[kR2];
+      H[STB_HIST_GEOM_COUNT] = cg;
+      H[STB_HIST_FEAT_COUNT] = cf;
+    }
   }
-  if (count == 0.0) S->status |= STB_ST_NO_MATCHES;
-  if (!cholesky_solve6(A, b, x)) {
-    S->stopped = 1;
-    S->status |= STB_ST_NOT_PD;
-    J->result[STB_RES_STATUS] = (double)S->status;
-    if (H) H[STB_HIST_OK] = 0.0;
+  const bool ok = warp_cholesky_solve6(A, b, x, L, lane);
+  double *R = J->result;
+  if (!ok) {
+    if (lane == 0) {
+      unsigned st = S->status | STB_ST_NOT_PD;
+      if (count == 0.0) st |= STB_ST_NO_MATCHES;
+      S->status = st;
+      S->stopped = 1;
+      R[STB_RES_STATUS] = (double)st;
+      if (H) H[STB_HIST_OK] = 0.0;
+    }
     return;
   }
-  bool finite = true;
-  for (int k = 0; k < 6; ++k) finite &= isfinite(x[k]);
-  if (!finite) S->status |= STB_ST_NAN;
-  double E[16], Tn[16];
-  se3_exp(x, E);
-  compose(E, S->T, Tn);
-  for (int k = 0; k < 16; ++k) S->T[k] = Tn[k];
-  refresh_pose32(S->pose, Tn);
-  S->iters_done += 1;
-  double *R = J->result;
-  for (int k = 0; k < 16; ++k) R[STB_RES_TRANSFORM + k] = Tn[k];
-  for (int k = 0; k < 36; ++k) R[STB_RES_JTJ + k] = A[k];
-  R[STB_RES_RESIDUAL] = r2 / count;
-  R[STB_RES_MATCHES] = count;
-  R[STB_RES_ITERS] = (double)S->iters_done;
-  R[STB_RES_STATUS] = (double)S->status;
-  if (H) {
-    for (int k = 0; k < 16; ++k) H[STB_HIST_TRANSFORM + k] = Tn[k];
-    H[STB_HIST_OK] = 1.0;
+  warp_se3_exp(x, E, lane);
+  warp_compose(E, T, Tn, lane);
+  if (lane < 16) {
+    S->T[lane] = Tn[lane];
+    R[STB_RES_TRANSFORM + lane] = Tn[lane];
+    if (H) H[STB_HIST_TRANSFORM + lane] = Tn[lane];
+  }
+  for (int k = lane; k < 36; k += 32) R[STB_RES_JTJ + k] = A[k];
+  if (lane < 12) S->pose.rt[lane] = __double2float_rn(Tn[lane]);
+  __syncwarp();
+  if (lane == 0) {
+    unsigned st = S->status;
+    bool finite = true;
+    for (int k = 0; k < 6; ++k) finite &= isfinite(x[k]);
+    if (!finite) st |= STB_ST_NAN;
+    if (count == 0.0) st |= STB_ST_NO_MATCHES;
+    S->status = st;
+    inverse_transpose(S->pose.rt, S->pose.nm);
+    S->iters_done += 1;
+    R[STB_RES_RESIDUAL] = tot[kR2] / count;
+    R[STB_RES_MATCHES] = count;
+    R[STB_RES_ITERS] = (double)S->iters_done;
+    R[STB_RES_STATUS] = (double)st;
+    if (H) H[STB_HIST_OK] = 1.0;
   }
 }
+
+// Pixels of one thread per round of the reduction loop; all their loads
+// that do not depend on the correspondence are issued together.
+constexpr int kRP = kPixelsPerThread;
 
 template <typename FT, bool kGeom, bool kFeat>
 __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict__ J,
                                                            int epoch) {
   __shared__ Pose32 P;
   __shared__ int skip;
-  __shared__ float ws[kReduceThreads / 32][kAccs][2];
+  __shared__ float red[kAccs][kReduceThreads];
   __shared__ float bs[kAccs], bc[kAccs];
   __shared__ int is_last;
   __shared__ double tot[kAccs];
@@ -307,9 +342,12 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
   __syncthreads();
   if (skip) return;
 
-  CSum acc[kAccs];
+  // per-thread partials are plain float32: a thread adds kRP pixels per
+  // round and few rounds, so its rounding stays below ~1e-6 of the sum of
+  // magnitudes; compensation (TwoSum) starts at the block level
+  float acc[kAccs];
 #pragma unroll
-  for (int a = 0; a < kAccs; ++a) acc[a] = {0.f, 0.f};
+  for (int a = 0; a < kAccs; ++a) acc[a] = 0.f;
 
   const int H = J->H, W = J->W;
   const int64_t npix = (int64_t)H * W;
@@ -319,70 +357,95 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
   const float *__restrict__ tp = J->tp;
   const float *__restrict__ tn = J->tn;
   const float wg1 = J->wg1, wg2 = J->wg2, wf1 = J->wf1, wf2 = J->wf2;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t pix = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; pix < npix;
-       pix += stride) {
-    const unsigned long long key = keys[pix];
-    if ((unsigned)(key >> 56) != tag) continue;
-    const int64_t i = (int64_t)(key & 0xffffffull);
-    const float3 Tp = transform_point(P.rt, sp[3 * i], sp[3 * i + 1], sp[3 * i + 2]);
-    if (kGeom) {
-      // r = (q - Tp).n, J = [n; Tp x n] (icp_jacobian_geometric.cu:82,
-      // icp_jacobian_common.hpp:41-48)
-      const float nx = tn[3 * pix], ny = tn[3 * pix + 1], nz = tn[3 * pix + 2];
-      const float r = dot3(fsub(tp[3 * pix], Tp.x), fsub(tp[3 * pix + 1], Tp.y),
-                           fsub(tp[3 * pix + 2], Tp.z), nx, ny, nz);
-      const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
-                           fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
-                           fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
-      accumulate_se3(acc, Jv, r, wg1, wg2);
-      csum_add(acc[kR2], wg1 * (r * r));
-      csum_add(acc[kCountGeom], 1.f);
-    }
-    if (kFeat) {
-      // FeatureJacobianKernel (icp_jacobian_feature.cu:65-108): the gate
-      // sum_c r_c^2 > thresh^2 is decided on the reference's float32 values.
-      const FT *__restrict__ tf = static_cast<const FT *>(J->tf);
-      const FT *__restrict__ sf = static_cast<const FT *>(J->sf);
-      const int C = J->C;
-      const long long n = J->n;
-      const int64_t plane = npix;
-      float u, v;
-      project(P, Tp, u, v);
-      float sq = 0.f;
-      for (int c = 0; c < C; ++c) {
-        const float r = fsub(bilinear(tf + c * plane, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
-        sq = fadd(sq, fmul(r, r));
+  const int64_t per_block = (int64_t)kReduceThreads * kRP;
+  for (int64_t base = blockIdx.x * per_block; base < npix;
+       base += (int64_t)gridDim.x * per_block) {
+    unsigned long long key[kRP];
+    float tq[kRP][3], tnm[kRP][3];
+#pragma unroll
+    for (int k = 0; k < kRP; ++k) {
+      const int64_t pix = base + k * kReduceThreads + threadIdx.x;
+      const int64_t pc = pix < npix ? pix : 0;
+      key[k] = pix < npix ? keys[pix] : 0ull;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        tq[k][d] = kGeom ? tp[3 * pc + d] : 0.f;
+        tnm[k][d] = kGeom ? tn[3 * pc + d] : 0.f;
       }
-      if (!(sq > J->feat_thr2)) {
-        const float h = 0.05f;
-        const float div = fdiv(1.f, fmul(2.f, h));
-        const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
-        const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
-        const float zz = fmul(Tp.z, Tp.z);
-        const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
-        const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
-        const int c0 = (J->channel_mode == 0) ? C - 1 : 0;
-        for (int c = c0; c < C; ++c) {
-          const FT *fc = tf + c * plane;
-          const float r = fsub(bilinear(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
-          const float du = fmul(fsub(bilinear(fc, H, W, uu0, v), bilinear(fc, H, W, uu1, v)), div);
-          const float dv = fmul(fsub(bilinear(fc, H, W, u, vv0), bilinear(fc, H, W, u, vv1)), div);
-          const float gx = fmul(du, j00), gy = fmul(dv, j11),
-                      gz = fadd(fmul(du, j02), fmul(dv, j12));
-          const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
-                               fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
-                               fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
-          // J^T r enters with -w_f (icp.py:222)
-          accumulate_se3(acc, Jv, r, -wf1, wf2);
+    }
+    float spt[kRP][3];
+#pragma unroll
+    for (int k = 0; k < kRP; ++k) {
+      const int64_t i = ((unsigned)(key[k] >> 56) == tag) ? (int64_t)(key[k] & 0xffffffull) : 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) spt[k][d] = sp[3 * i + d];
+    }
+#pragma unroll
+    for (int k = 0; k < kRP; ++k) {
+      if ((unsigned)(key[k] >> 56) != tag) continue;
+      const int64_t i = (int64_t)(key[k] & 0xffffffull);
+      const float3 Tp = transform_point(P.rt, spt[k][0], spt[k][1], spt[k][2]);
+      if (kGeom) {
+        // r = (q - Tp).n, J = [n; Tp x n] (icp_jacobian_geometric.cu:82,
+        // icp_jacobian_common.hpp:41-48)
+        const float nx = tnm[k][0], ny = tnm[k][1], nz = tnm[k][2];
+        const float r = dot3(fsub(tq[k][0], Tp.x), fsub(tq[k][1], Tp.y),
+                             fsub(tq[k][2], Tp.z), nx, ny, nz);
+        const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
+                             fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
+                             fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
+        accumulate_se3(acc, Jv, r, wg1, wg2);
+        acc[kR2] += wg1 * (r * r);
+        acc[kCountGeom] += 1.f;
+      }
+      if (kFeat) {
+        // FeatureJacobianKernel (icp_jacobian_feature.cu:65-108): the gate
+        // sum_c r_c^2 > thresh^2 is decided on the reference's float32 values.
+        const FT *__restrict__ tf = static_cast<const FT *>(J->tf);
+        const FT *__restrict__ sf = static_cast<const FT *>(J->sf);
+        const int C = J->C;
+        const long long n = J->n;
+        const int64_t plane = npix;
+        float u, v;
+        project(P, Tp, u, v);
+        float sq = 0.f;
+        for (int c = 0; c < C; ++c) {
+          const float r =
+              fsub(bilinear(tf + c * plane, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+          sq = fadd(sq, fmul(r, r));
         }
-        csum_add(acc[kR2], wf1 * sq);
-        csum_add(acc[kCountFeat], 1.f);
+        if (!(sq > J->feat_thr2)) {
+          const float h = 0.05f;
+          const float div = fdiv(1.f, fmul(2.f, h));
+          const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
+          const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
+          const float zz = fmul(Tp.z, Tp.z);
+          const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
+          const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
+          const int c0 = (J->channel_mode == 0) ? C - 1 : 0;
+          for (int c = c0; c < C; ++c) {
+            const FT *fc = tf + c * plane;
+            const float r = fsub(bilinear(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+            const float du =
+                fmul(fsub(bilinear(fc, H, W, uu0, v), bilinear(fc, H, W, uu1, v)), div);
+            const float dv =
+                fmul(fsub(bilinear(fc, H, W, u, vv0), bilinear(fc, H, W, u, vv1)), div);
+            const float gx = fmul(du, j00), gy = fmul(dv, j11),
+                        gz = fadd(fmul(du, j02), fmul(dv, j12));
+            const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
+                                 fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
+                                 fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
+            // J^T r enters with -w_f (icp.py:222)
+            accumulate_se3(acc, Jv, r, -wf1, wf2);
+          }
+          acc[kR2] += wf1 * sq;
+          acc[kCountFeat] += 1.f;
+        }
       }
     }
   }
 
-  block_reduce<kAccs>(acc, ws, bs, bc);
+  block_reduce<kAccs>(acc, red, bs, bc);
   const int nb = gridDim.x;
   if (threadIdx.x < kAccs) {
     J->part_s[threadIdx.x * nb + blockIdx.x] = bs[threadIdx.x];
@@ -396,9 +459,9 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
   __threadfence();
   grid_totals<kAccs>(J->part_s, J->part_c, nb, tot);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    S->ticket = 0;
-    gn_step(J, tot, epoch);
+  if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) S->ticket = 0;
+    gn_step_warp(J, tot, epoch);
   }
 }
 
@@ -406,14 +469,14 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
 // (icp_jacobian_geometric.cu:141-151), summed as icp.py:108.
 __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__ J,
                                                          int epoch) {
-  __shared__ float ws[kReduceThreads / 32][kInfoAccs][2];
+  __shared__ float red[kInfoAccs][kReduceThreads];
   __shared__ float bs[kInfoAccs], bc[kInfoAccs];
   __shared__ int is_last;
   __shared__ double tot[kInfoAccs];
   State *S = J->state;
-  CSum acc[kInfoAccs];
+  float acc[kInfoAccs];
 #pragma unroll
-  for (int a = 0; a < kInfoAccs; ++a) acc[a] = {0.f, 0.f};
+  for (int a = 0; a < kInfoAccs; ++a) acc[a] = 0.f;
   const int64_t npix = (int64_t)J->H * J->W;
   const unsigned tag = tag_of(epoch);
   const unsigned long long *__restrict__ keys = J->keys;
@@ -430,9 +493,9 @@ __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__
     for (int a = 0; a < 6; ++a)
 #pragma unroll
       for (int b = a; b < 6; ++b)
-        csum_add(acc[upper_index(a, b)], G0[a] * G0[b] + G1[a] * G1[b] + G2[a] * G2[b]);
+        acc[upper_index(a, b)] += G0[a] * G0[b] + G1[a] * G1[b] + G2[a] * G2[b];
   }
-  block_reduce<kInfoAccs>(acc, ws, bs, bc);
+  block_reduce<kInfoAccs>(acc, red, bs, bc);
   const int nb = gridDim.x;
   if (threadIdx.x < kInfoAccs) {
     J->part_s[threadIdx.x * nb + blockIdx.x] = bs[threadIdx.x];

@@ -1,6 +1,15 @@
 // Differentiable point-to-plane loss for batches of frame pairs, with a
 // hand-written adjoint.
 //
+// Layout: every field is one dense device array over the batch, pair p at
+// offset p * H * W pixels: source depth (float32, metres), source normals
+// (float32 xyz), source mask (uint8), target points / normals (float32
+// xyz), target mask (uint8); all pairs share the size and the intrinsics.
+// Source points are back-projected in the kernels exactly as
+// stb_depth_to_points does (x = ((u - cx) z) / fx, slamtb/camera.py:127-149),
+// so the loss reads 4 bytes of depth per source pixel instead of 12 of
+// points and the depth gradient needs no chain through a points tensor.
+//
 // Forward (per pair p, pose T_p): the ICPOdometry association at the float32
 // cast of T_p (64-bit atomicMin z-buffer, the reference's gates) and
 // L_p = sum over the correspondences of r^2, r = (q - T_p s).n
@@ -8,8 +17,7 @@
 // Adjoint (correspondences frozen): dL/dxi = -2 sum r J with J = [n; Tp x n]
 // for T <- exp(xi) T_p (the sign convention of icp_jacobian_common.hpp:41-48,
 // J = -dr/dxi), and dL/dz_i = -2 r_i (R^T n) . d_i for the source depth z_i,
-// s_i = z_i d_i, d_i = ((u_i - cx)/fx, (v_i - cy)/fy, 1) (the back-projection
-// of slamtb/camera.py:127-149).
+// s_i = z_i d_i, d_i = ((u_i - cx)/fx, (v_i - cy)/fy, 1).
 //
 // Grid: x = work items of a pair, y = pair.  Per-pair totals use per-block
 // partials and a last-block ticket (deterministic order).
@@ -31,72 +39,81 @@ constexpr int kItem = kT * 4;        // pixels per block
 constexpr int kMaxBlocksX = 1024;    // blocks per pair (grid-stride beyond)
 constexpr unsigned kTag = 254u;
 
-struct GradLayout {
-  size_t err, tickets, part, keys, total;
+struct LossArgs {
+  const float *depth, *sn;
+  const uint8_t *sm;
+  const float *tp, *tn;
+  const uint8_t *tm;
+  int B, H, W;
+  float fx, fy, cx, cy;
+  const double *poses;
 };
 
-inline int blocks_x(int64_t max_px) {
-  int64_t b = (max_px + kItem - 1) / kItem;
+struct GradLayout {
+  size_t tickets, part, keys, total;
+};
+
+inline int blocks_x(int64_t px) {
+  int64_t b = (px + kItem - 1) / kItem;
   return (int)(b < 1 ? 1 : (b > kMaxBlocksX ? kMaxBlocksX : b));
 }
 
 inline size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
-inline GradLayout grad_layout(int B, int64_t max_px) {
+inline GradLayout grad_layout(int B, int64_t px) {
   GradLayout g;
   size_t o = 0;
-  g.err = o;
-  o += 256;
   g.tickets = o;
   o += al(sizeof(unsigned) * (size_t)B);
   g.part = o;
-  o += al(sizeof(float) * 16 * (size_t)B * blocks_x(max_px));
+  o += al(sizeof(float) * 16 * (size_t)B * blocks_x(px));
   g.keys = o;
-  o += al(sizeof(unsigned long long) * (size_t)B * max_px);
+  o += al(sizeof(unsigned long long) * (size_t)B * px);
   g.total = o;
   return g;
 }
 
-// Level descriptor and float32 pose of pair blockIdx.y, into shared memory.
-__device__ __forceinline__ void pair_setup(const stb_level *levels, const double *poses,
-                                           stb_level &lv, Pose32 &P) {
+// float32 pose of pair blockIdx.y, into shared memory.
+__device__ __forceinline__ void pair_pose(const LossArgs &a, Pose32 &P) {
   if (threadIdx.x == 0) {
-    lv = levels[blockIdx.y];
     double T[16];
-    for (int k = 0; k < 16; ++k) T[k] = poses[blockIdx.y * 16 + k];
-    P.fx = lv.fx;
-    P.fy = lv.fy;
-    P.cx = lv.cx;
-    P.cy = lv.cy;
+    for (int k = 0; k < 16; ++k) T[k] = a.poses[blockIdx.y * 16 + k];
+    P.fx = a.fx;
+    P.fy = a.fy;
+    P.cx = a.cx;
+    P.cy = a.cy;
     refresh_pose32(P, T);
   }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kT) k_g_assoc(const stb_level *levels, const double *poses,
-                                                int64_t max_px, unsigned long long *keys_all,
-                                                float thr2, float cos_max, unsigned *err) {
-  __shared__ stb_level lv;
+// Source point i of a pair from its depth (stb_depth_to_points' arithmetic).
+__device__ __forceinline__ float3 source_point(const LossArgs &a, float z, int64_t i) {
+  const float u = (float)(i % a.W), v = (float)(i / a.W);
+  return make_float3(fdiv(fmul(fsub(u, a.cx), z), a.fx), fdiv(fmul(fsub(v, a.cy), z), a.fy), z);
+}
+
+__global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long long *keys_all,
+                                                float thr2, float cos_max) {
   __shared__ Pose32 P;
-  pair_setup(levels, poses, lv, P);
-  const int H = lv.height, W = lv.width;
-  if ((int64_t)H * W > max_px) {
-    if (threadIdx.x == 0) atomicOr(err, 2u);
-    return;
-  }
-  unsigned long long *keys = keys_all + (size_t)blockIdx.y * max_px;
-  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < lv.num_source;
+  pair_pose(a, P);
+  const int H = a.H, W = a.W;
+  const int64_t npix = (int64_t)H * W;
+  const size_t po = (size_t)blockIdx.y * npix;
+  unsigned long long *keys = keys_all + po;
+  const float *tp = a.tp + 3 * po, *tn = a.tn + 3 * po, *sn = a.sn + 3 * po;
+  const uint8_t *tm = a.tm + po;
+  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < npix;
        i += (int64_t)gridDim.x * kT) {
-    if (!lv.src_mask[i]) continue;
-    const float3 Tp = transform_point(P.rt, lv.src_points[3 * i], lv.src_points[3 * i + 1],
-                                      lv.src_points[3 * i + 2]);
+    if (!a.sm[po + i]) continue;
+    const float3 s = source_point(a, a.depth[po + i], i);
+    const float3 Tp = transform_point(P.rt, s.x, s.y, s.z);
     float u, v;
     project(P, Tp, u, v);
     int ui, vi;
     if (!round_in(u, W, ui) || !round_in(v, H, vi)) continue;
     const int64_t pix = (int64_t)vi * W + ui;
-    if (!lv.tgt_mask[pix]) continue;
-    const float *tp = lv.tgt_points, *tn = lv.tgt_normals, *sn = lv.src_normals;
+    if (!tm[pix]) continue;
     const float dx = fsub(tp[3 * pix], Tp.x), dy = fsub(tp[3 * pix + 1], Tp.y),
                 dz = fsub(tp[3 * pix + 2], Tp.z);
     const float sq = dot3(dx, dy, dz, dx, dy, dz);
@@ -157,89 +174,78 @@ __device__ bool pair_fold(CSum *acc, float *part_all, unsigned *tickets, double 
   return true;
 }
 
-__global__ void __launch_bounds__(kT) k_g_loss(const stb_level *levels, const double *poses,
-                                               int64_t max_px, const unsigned long long *keys_all,
-                                               float *part, unsigned *tickets, double *loss) {
-  __shared__ stb_level lv;
+// Residual at target pixel pix of the pair (offset po) and its
+// correspondence i; returns r and the transformed source point and normal.
+__device__ __forceinline__ float residual(const LossArgs &a, const Pose32 &P, size_t po,
+                                          int64_t pix, int64_t i, float3 &Tp, float3 &n) {
+  const float3 s = source_point(a, a.depth[po + i], i);
+  Tp = transform_point(P.rt, s.x, s.y, s.z);
+  const float *tp = a.tp + 3 * (po + pix), *tn = a.tn + 3 * (po + pix);
+  n = make_float3(tn[0], tn[1], tn[2]);
+  return dot3(fsub(tp[0], Tp.x), fsub(tp[1], Tp.y), fsub(tp[2], Tp.z), n.x, n.y, n.z);
+}
+
+__global__ void __launch_bounds__(kT) k_g_loss(const LossArgs a,
+                                               const unsigned long long *keys_all, float *part,
+                                               unsigned *tickets, double *loss) {
   __shared__ Pose32 P;
   __shared__ double tot[8];
-  pair_setup(levels, poses, lv, P);
-  const int64_t npix = (int64_t)lv.height * lv.width;
-  const unsigned long long *keys = keys_all + (size_t)blockIdx.y * max_px;
+  pair_pose(a, P);
+  const int64_t npix = (int64_t)a.H * a.W;
+  const size_t po = (size_t)blockIdx.y * npix;
+  const unsigned long long *keys = keys_all + po;
   CSum acc[1] = {{0.f, 0.f}};
-  if (npix <= max_px) {
-    for (int64_t pix = blockIdx.x * (int64_t)kT + threadIdx.x; pix < npix;
-         pix += (int64_t)gridDim.x * kT) {
-      const unsigned long long key = __ldcg(keys + pix);
-      if ((unsigned)(key >> 56) != kTag) continue;
-      const int64_t i = (int64_t)(key & 0xffffffull);
-      const float3 Tp = transform_point(P.rt, lv.src_points[3 * i], lv.src_points[3 * i + 1],
-                                        lv.src_points[3 * i + 2]);
-      const float *tp = lv.tgt_points + 3 * pix, *tn = lv.tgt_normals + 3 * pix;
-      const float r = dot3(fsub(tp[0], Tp.x), fsub(tp[1], Tp.y), fsub(tp[2], Tp.z), tn[0], tn[1],
-                           tn[2]);
-      csum_add(acc[0], r * r);
-    }
+  for (int64_t pix = blockIdx.x * (int64_t)kT + threadIdx.x; pix < npix;
+       pix += (int64_t)gridDim.x * kT) {
+    const unsigned long long key = __ldcg(keys + pix);
+    if ((unsigned)(key >> 56) != kTag) continue;
+    float3 Tp, n;
+    const float r = residual(a, P, po, pix, (int64_t)(key & 0xffffffull), Tp, n);
+    csum_add(acc[0], r * r);
   }
   if (pair_fold<1>(acc, part, tickets, tot) && threadIdx.x == 0) loss[blockIdx.y] = tot[0];
 }
 
-__global__ void __launch_bounds__(kT) k_g_adjoint(const stb_level *levels, const double *poses,
-                                                  int64_t max_px,
+__global__ void __launch_bounds__(kT) k_g_adjoint(const LossArgs a,
                                                   const unsigned long long *keys_all,
                                                   const double *grad_loss, float *part,
-                                                  unsigned *tickets, double *grad_twist,
-                                                  float *const *grad_depth) {
-  __shared__ stb_level lv;
+                                                  unsigned *tickets, double *grad_tangent,
+                                                  float *grad_depth) {
   __shared__ Pose32 P;
   __shared__ double tot[8];
-  pair_setup(levels, poses, lv, P);
-  const int H = lv.height, W = lv.width;
-  const int64_t npix = (int64_t)H * W;
-  const unsigned long long *keys = keys_all + (size_t)blockIdx.y * max_px;
+  pair_pose(a, P);
+  const int64_t npix = (int64_t)a.H * a.W;
+  const size_t po = (size_t)blockIdx.y * npix;
+  const unsigned long long *keys = keys_all + po;
   const float g = (float)grad_loss[blockIdx.y];
-  float *gz = grad_depth ? grad_depth[blockIdx.y] : nullptr;
+  float *gz = grad_depth ? grad_depth + po : nullptr;
   CSum acc[6];
 #pragma unroll
-  for (int a = 0; a < 6; ++a) acc[a] = {0.f, 0.f};
-  if (npix <= max_px) {
-    for (int64_t pix = blockIdx.x * (int64_t)kT + threadIdx.x; pix < npix;
-         pix += (int64_t)gridDim.x * kT) {
-      const unsigned long long key = __ldcg(keys + pix);
-      if ((unsigned)(key >> 56) != kTag) continue;
-      const int64_t i = (int64_t)(key & 0xffffffull);
-      const float3 Tp = transform_point(P.rt, lv.src_points[3 * i], lv.src_points[3 * i + 1],
-                                        lv.src_points[3 * i + 2]);
-      const float *tp = lv.tgt_points + 3 * pix, *tn = lv.tgt_normals + 3 * pix;
-      const float nx = tn[0], ny = tn[1], nz = tn[2];
-      const float r = dot3(fsub(tp[0], Tp.x), fsub(tp[1], Tp.y), fsub(tp[2], Tp.z), nx, ny, nz);
-      const float Jv[6] = {nx, ny, nz, Tp.y * nz - Tp.z * ny, Tp.z * nx - Tp.x * nz,
-                           Tp.x * ny - Tp.y * nx};
-      const float s = -2.f * g * r;
+  for (int k = 0; k < 6; ++k) acc[k] = {0.f, 0.f};
+  for (int64_t pix = blockIdx.x * (int64_t)kT + threadIdx.x; pix < npix;
+       pix += (int64_t)gridDim.x * kT) {
+    const unsigned long long key = __ldcg(keys + pix);
+    if ((unsigned)(key >> 56) != kTag) continue;
+    const int64_t i = (int64_t)(key & 0xffffffull);
+    float3 Tp, n;
+    const float r = residual(a, P, po, pix, i, Tp, n);
+    const float Jv[6] = {n.x, n.y, n.z, Tp.y * n.z - Tp.z * n.y, Tp.z * n.x - Tp.x * n.z,
+                         Tp.x * n.y - Tp.y * n.x};
+    const float s = -2.f * g * r;
 #pragma unroll
-      for (int a = 0; a < 6; ++a) csum_add(acc[a], s * Jv[a]);
-      if (gz) {
-        // R^T n, with R the float32 rotation of the pose
-        const float *R = P.rt;
-        const float rn0 = R[0] * nx + R[4] * ny + R[8] * nz;
-        const float rn1 = R[1] * nx + R[5] * ny + R[9] * nz;
-        const float rn2 = R[2] * nx + R[6] * ny + R[10] * nz;
-        const float u = (float)(i % W), v = (float)(i / W);
-        const float d0 = (u - P.cx) / P.fx, d1 = (v - P.cy) / P.fy;
-        gz[i] = s * (rn0 * d0 + rn1 * d1 + rn2);
-      }
+    for (int k = 0; k < 6; ++k) csum_add(acc[k], s * Jv[k]);
+    if (gz) {
+      // R^T n, with R the float32 rotation of the pose
+      const float *R = P.rt;
+      const float rn0 = R[0] * n.x + R[4] * n.y + R[8] * n.z;
+      const float rn1 = R[1] * n.x + R[5] * n.y + R[9] * n.z;
+      const float rn2 = R[2] * n.x + R[6] * n.y + R[10] * n.z;
+      const float d0 = ((float)(i % a.W) - P.cx) / P.fx, d1 = ((float)(i / a.W) - P.cy) / P.fy;
+      gz[i] = s * (rn0 * d0 + rn1 * d1 + rn2);
     }
   }
-  if (pair_fold<6>(acc, part, tickets, tot) && grad_twist && threadIdx.x < 6)
-    grad_twist[blockIdx.y * 6 + threadIdx.x] = tot[threadIdx.x];
-}
-
-__global__ void k_zero_depth_grads(const stb_level *levels, float *const *grad_depth) {
-  float *gz = grad_depth[blockIdx.y];
-  const int64_t n = levels[blockIdx.y].num_source;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    gz[i] = 0.f;
+  if (pair_fold<6>(acc, part, tickets, tot) && grad_tangent && threadIdx.x < 6)
+    grad_tangent[blockIdx.y * 6 + threadIdx.x] = tot[threadIdx.x];
 }
 
 __global__ void k_se3_exp_compose(const double *twist, const double *base, double *out, int B) {
@@ -303,19 +309,48 @@ __global__ void k_se3_twist_grad(const double *twist, const double *g_in, double
   }
 }
 
-int check_loss_args(const stb_level *levels, int B, const double *poses, int64_t max_px,
-                    void *workspace, size_t ws_bytes) {
-  if (B <= 0) return fail(STB_EINVAL, "Check failed: num_pairs must be positive");
-  if (max_px <= 0) return fail(STB_EINVAL, "Check failed: max_target_pixels must be positive");
-  const GradLayout g = grad_layout(B, max_px);
+int check_loss_args(const LossArgs &a, void *workspace, size_t ws_bytes) {
+  if (a.B <= 0) return fail(STB_EINVAL, "Check failed: num_pairs must be positive");
+  if (a.H <= 0 || a.W <= 0)
+    return fail(STB_EINVAL, "Check failed: frame size must be positive, got %dx%d", a.H, a.W);
+  if ((int64_t)a.H * a.W >= (1ll << 24))
+    return fail(STB_EINVAL, "Check failed: frames must have fewer than 2^24 pixels");
+  const GradLayout g = grad_layout(a.B, (int64_t)a.H * a.W);
   if (ws_bytes < g.total)
     return fail(STB_EINVAL, "Check failed: workspace of %zu bytes, %zu needed", ws_bytes, g.total);
   if (((uintptr_t)workspace & 255) != 0)
     return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
-  STB_TRY(check_device_ptr(levels, "levels"));
-  STB_TRY(check_device_ptr(poses, "poses"));
+  STB_TRY(check_device_ptr(a.depth, "source_depth"));
+  STB_TRY(check_device_ptr(a.sn, "source_normals"));
+  STB_TRY(check_device_ptr(a.sm, "source_mask"));
+  STB_TRY(check_device_ptr(a.tp, "target_points"));
+  STB_TRY(check_device_ptr(a.tn, "target_normals"));
+  STB_TRY(check_device_ptr(a.tm, "target_mask"));
+  STB_TRY(check_device_ptr(a.poses, "poses"));
   STB_TRY(check_device_ptr(workspace, "workspace"));
   return STB_OK;
+}
+
+LossArgs loss_args(const float *src_depth, const float *src_normals, const uint8_t *src_mask,
+                   const float *tgt_points, const float *tgt_normals, const uint8_t *tgt_mask,
+                   int32_t num_pairs, int32_t height, int32_t width, float fx, float fy,
+                   float cx, float cy, const double *poses) {
+  LossArgs a;
+  a.depth = src_depth;
+  a.sn = src_normals;
+  a.sm = src_mask;
+  a.tp = tgt_points;
+  a.tn = tgt_normals;
+  a.tm = tgt_mask;
+  a.B = num_pairs;
+  a.H = height;
+  a.W = width;
+  a.fx = fx;
+  a.fy = fy;
+  a.cx = cx;
+  a.cy = cy;
+  a.poses = poses;
+  return a;
 }
 
 }  // namespace
@@ -347,58 +382,64 @@ extern "C" int stb_se3_twist_grad(const double *twist, const double *grad_tangen
   return check_launch("stb_se3_twist_grad");
 }
 
-extern "C" size_t stb_icp_loss_workspace_bytes(int32_t num_pairs, int64_t max_target_pixels) {
-  if (num_pairs <= 0 || max_target_pixels <= 0) return 0;
-  return grad_layout(num_pairs, max_target_pixels).total;
+extern "C" size_t stb_icp_loss_workspace_bytes(int32_t num_pairs, int32_t height,
+                                               int32_t width) {
+  if (num_pairs <= 0 || height <= 0 || width <= 0) return 0;
+  return grad_layout(num_pairs, (int64_t)height * width).total;
 }
 
-extern "C" int stb_icp_loss_forward(const stb_level *levels, int32_t num_pairs,
-                                    const double *poses, double distance_thresh,
-                                    double normal_angle_thresh, int64_t max_target_pixels,
+extern "C" int stb_icp_loss_forward(const float *src_depth, const float *src_normals,
+                                    const uint8_t *src_mask, const float *tgt_points,
+                                    const float *tgt_normals, const uint8_t *tgt_mask,
+                                    int32_t num_pairs, int32_t height, int32_t width, float fx,
+                                    float fy, float cx, float cy, const double *poses,
+                                    double distance_thresh, double normal_angle_thresh,
                                     void *workspace, size_t workspace_bytes, double *loss,
                                     void *stream) {
   clear_error();
-  STB_TRY(check_loss_args(levels, num_pairs, poses, max_target_pixels, workspace,
-                          workspace_bytes));
+  const LossArgs a = loss_args(src_depth, src_normals, src_mask, tgt_points, tgt_normals,
+                               tgt_mask, num_pairs, height, width, fx, fy, cx, cy, poses);
+  STB_TRY(check_loss_args(a, workspace, workspace_bytes));
   STB_TRY(check_device_ptr(loss, "loss"));
-  const GradLayout g = grad_layout(num_pairs, max_target_pixels);
+  const int64_t npix = (int64_t)height * width;
+  const GradLayout g = grad_layout(num_pairs, npix);
   char *ws = static_cast<char *>(workspace);
   const cudaStream_t st = as_stream(stream);
-  unsigned *err = reinterpret_cast<unsigned *>(ws + g.err);
-  unsigned *tickets = reinterpret_cast<unsigned *>(ws + g.tickets);
   unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + g.keys);
-  cudaMemsetAsync(ws, 0, g.part, st);  // error word and tickets
-  cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * (size_t)num_pairs * max_target_pixels,
-                  st);
-  const dim3 grid(blocks_x(max_target_pixels), num_pairs);
-  k_g_assoc<<<grid, kT, 0, st>>>(levels, poses, max_target_pixels, keys,
-                                 distance_thresh_sq(distance_thresh),
-                                 angle_cos_max(normal_angle_thresh), err);
-  k_g_loss<<<grid, kT, 0, st>>>(levels, poses, max_target_pixels, keys,
-                                reinterpret_cast<float *>(ws + g.part), tickets, loss);
+  cudaMemsetAsync(ws + g.tickets, 0, sizeof(unsigned) * (size_t)num_pairs, st);
+  cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * (size_t)num_pairs * npix, st);
+  const dim3 grid(blocks_x(npix), num_pairs);
+  k_g_assoc<<<grid, kT, 0, st>>>(a, keys, distance_thresh_sq(distance_thresh),
+                                 angle_cos_max(normal_angle_thresh));
+  k_g_loss<<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
+                                reinterpret_cast<unsigned *>(ws + g.tickets), loss);
   return check_launch("stb_icp_loss_forward");
 }
 
-extern "C" int stb_icp_loss_backward(const stb_level *levels, int32_t num_pairs,
-                                     const double *poses, const double *grad_loss,
-                                     int64_t max_target_pixels, void *workspace,
-                                     size_t workspace_bytes, double *grad_twist,
-                                     float *const *grad_depth, void *stream) {
+extern "C" int stb_icp_loss_backward(const float *src_depth, const float *src_normals,
+                                     const uint8_t *src_mask, const float *tgt_points,
+                                     const float *tgt_normals, const uint8_t *tgt_mask,
+                                     int32_t num_pairs, int32_t height, int32_t width, float fx,
+                                     float fy, float cx, float cy, const double *poses,
+                                     const double *grad_loss, void *workspace,
+                                     size_t workspace_bytes, double *grad_tangent,
+                                     float *grad_depth, void *stream) {
   clear_error();
-  STB_TRY(check_loss_args(levels, num_pairs, poses, max_target_pixels, workspace,
-                          workspace_bytes));
+  const LossArgs a = loss_args(src_depth, src_normals, src_mask, tgt_points, tgt_normals,
+                               tgt_mask, num_pairs, height, width, fx, fy, cx, cy, poses);
+  STB_TRY(check_loss_args(a, workspace, workspace_bytes));
   STB_TRY(check_device_ptr(grad_loss, "grad_loss"));
-  STB_TRY(check_device_ptr(grad_twist, "grad_twist", true));
+  STB_TRY(check_device_ptr(grad_tangent, "grad_tangent", true));
   STB_TRY(check_device_ptr(grad_depth, "grad_depth", true));
-  const GradLayout g = grad_layout(num_pairs, max_target_pixels);
+  const int64_t npix = (int64_t)height * width;
+  const GradLayout g = grad_layout(num_pairs, npix);
   char *ws = static_cast<char *>(workspace);
   const cudaStream_t st = as_stream(stream);
-  const dim3 grid(blocks_x(max_target_pixels), num_pairs);
-  if (grad_depth) k_zero_depth_grads<<<grid, kT, 0, st>>>(levels, grad_depth);
-  k_g_adjoint<<<grid, kT, 0, st>>>(levels, poses, max_target_pixels,
-                                   reinterpret_cast<const unsigned long long *>(ws + g.keys),
+  if (grad_depth) cudaMemsetAsync(grad_depth, 0, sizeof(float) * (size_t)num_pairs * npix, st);
+  const dim3 grid(blocks_x(npix), num_pairs);
+  k_g_adjoint<<<grid, kT, 0, st>>>(a, reinterpret_cast<const unsigned long long *>(ws + g.keys),
                                    grad_loss, reinterpret_cast<float *>(ws + g.part),
-                                   reinterpret_cast<unsigned *>(ws + g.tickets), grad_twist,
+                                   reinterpret_cast<unsigned *>(ws + g.tickets), grad_tangent,
                                    grad_depth);
   return check_launch("stb_icp_loss_backward");
 }

@@ -3,27 +3,21 @@
 ``PointToPlaneLoss`` is a ``torch.autograd.Function`` over a batch of frame
 pairs: forward = the ICP association at ``exp(twist) @ pose`` and
 ``L_p = sum r^2`` (``stb_icp_loss_forward``); backward = the adjoint kernel
-(``stb_icp_loss_backward``) giving dL/dtwist (left perturbation, twist
-ordered [translation; rotation]) and dL/d(source depth) per pixel, with the
-correspondences of the forward pass held fixed.  Source normals only gate
-the association and get no gradient.
+(``stb_icp_loss_backward``) giving dL/d(source depth) per pixel and the
+gradient with respect to the left perturbation of the pose, which
+``stb_se3_twist_grad`` maps through the SE(3) left Jacobian to dL/dtwist
+(twist ordered [translation; rotation]).  The correspondences of the forward
+pass are held fixed; source normals only gate the association and get no
+gradient.
 
 The reference differentiates its registration through PyTorch ops and a
 custom matcher (``slamtb/registration/autogradicp.py:145-239``,
 ``src/fpcl_matcher.cu:197-229``); here the whole loss and its adjoint are
-two kernels per direction for the batch.
-
-The kernels differentiate with respect to the left perturbation
-``exp(e) @ exp(twist) @ pose`` at e = 0; ``stb_se3_twist_grad`` maps that
-to the gradient with respect to ``twist`` itself through the SE(3) left
-Jacobian (the identity at twist = 0).
+two kernels per direction for the batch, reading dense (B, H, W) arrays.
 """
-import ctypes
-
 import torch
 
 from .. import _native as N
-from .. import processing
 
 
 def se3_exp_compose(twist, base):
@@ -38,20 +32,16 @@ def se3_exp_compose(twist, base):
     return out
 
 
-class _State:
-    def __init__(self):
-        self.ws = None
+def _f32(name, t, shape):
+    if t.dtype != torch.float32 or t.device.type != "cuda" or tuple(t.shape) != shape:
+        raise RuntimeError(f"Check failed: {name} must be a float32 CUDA tensor of shape {shape}")
+    return t.contiguous()
 
 
-def _levels(points, normals, smask, tpoints, tnormals, tmask, kcam):
-    B, H, W = tmask.shape
-    fx, fy, cx, cy = kcam
-    arr = (N.StbLevel * B)()
-    for p in range(B):
-        arr[p] = N.StbLevel(points[p].data_ptr(), normals[p].data_ptr(), smask[p].data_ptr(),
-                            H * W, None, tpoints[p].data_ptr(), tnormals[p].data_ptr(),
-                            tmask[p].data_ptr(), H, W, None, fx, fy, cx, cy)
-    return torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(tmask.device)
+def _mask(name, t, shape):
+    if t.device.type != "cuda" or tuple(t.shape) != shape:
+        raise RuntimeError(f"Check failed: {name} must be a CUDA tensor of shape {shape}")
+    return t.to(torch.bool).contiguous()
 
 
 class PointToPlaneLoss(torch.autograd.Function):
@@ -61,53 +51,48 @@ class PointToPlaneLoss(torch.autograd.Function):
 
     twist: (B, 6) float64; source_depth: (B, H, W) float32 (metres);
     source_normals / target_points / target_normals: (B, H, W, 3) float32;
-    masks: (B, H, W) bool; kcam: (fx, fy, cx, cy) shared by source and
-    target; poses: (B, 4, 4) float64, the loss is evaluated at
-    exp(twist) @ poses."""
+    masks: (B, H, W) bool; kcam: (fx, fy, cx, cy) shared by every frame;
+    poses: (B, 4, 4) float64, the loss is evaluated at exp(twist) @ poses."""
 
     @staticmethod
     def forward(ctx, twist, source_depth, source_normals, source_mask, target_points,
                 target_normals, target_mask, kcam, poses, distance_threshold,
                 normals_angle_thresh):
-        dev = source_depth.device
         B, H, W = source_depth.shape
-        T = se3_exp_compose(twist, poses)
-        kmat = torch.tensor([[kcam[0], 0, kcam[2]], [0, kcam[1], kcam[3]], [0, 0, 1]],
-                            dtype=torch.float32)
-        pts = torch.stack([processing.depth_to_points(source_depth[p].detach(), kmat)[0]
-                           for p in range(B)]).contiguous()
-        keep = [pts, source_normals.contiguous(), source_mask.to(torch.bool).contiguous(),
-                target_points.contiguous(), target_normals.contiguous(),
-                target_mask.to(torch.bool).contiguous()]
-        levels = _levels(*keep, kcam)
-        need = int(N.lib().stb_icp_loss_workspace_bytes(B, H * W))
+        dev = source_depth.device
+        ins = [_f32("source_depth", source_depth.detach(), (B, H, W)),
+               _f32("source_normals", source_normals, (B, H, W, 3)),
+               _mask("source_mask", source_mask, (B, H, W)),
+               _f32("target_points", target_points, (B, H, W, 3)),
+               _f32("target_normals", target_normals, (B, H, W, 3)),
+               _mask("target_mask", target_mask, (B, H, W))]
+        tw = twist.detach().to(device=dev, dtype=torch.float64).contiguous()
+        T = se3_exp_compose(tw, poses)
+        need = int(N.lib().stb_icp_loss_workspace_bytes(B, H, W))
         ws = torch.empty(need, dtype=torch.uint8, device=dev)
         loss = torch.empty(B, dtype=torch.float64, device=dev)
+        k = tuple(float(x) for x in kcam)
         with torch.cuda.device(dev):
             N.check(N.lib().stb_icp_loss_forward(
-                N.ptr(levels), B, N.ptr(T), float(distance_threshold),
-                float(normals_angle_thresh), H * W, N.ptr(ws), need, N.ptr(loss),
-                N.stream_of(dev)))
-        ctx.keep = keep + [levels, ws, T, twist.detach().to(torch.float64).contiguous()]
-        ctx.shape = (B, H, W)
+                *[N.ptr(t) for t in ins], B, H, W, *k, N.ptr(T), float(distance_threshold),
+                float(normals_angle_thresh), N.ptr(ws), need, N.ptr(loss), N.stream_of(dev)))
+        ctx.keep = (ins, ws, T, tw, k)
         return loss
 
     @staticmethod
     def backward(ctx, grad_loss):
-        B, H, W = ctx.shape
-        levels, ws, T, twist = ctx.keep[-4:]
+        ins, ws, T, tw, k = ctx.keep
+        B, H, W = ins[0].shape
         dev = ws.device
         g = grad_loss.detach().to(device=dev, dtype=torch.float64).contiguous()
         grad_tangent = torch.empty(B, 6, dtype=torch.float64, device=dev)
         grad_twist = torch.empty(B, 6, dtype=torch.float64, device=dev)
         grad_depth = torch.empty(B, H, W, dtype=torch.float32, device=dev)
-        ptrs = torch.tensor([grad_depth[p].data_ptr() for p in range(B)], dtype=torch.int64,
-                            device=dev)
         with torch.cuda.device(dev):
             N.check(N.lib().stb_icp_loss_backward(
-                N.ptr(levels), B, N.ptr(T), N.ptr(g), H * W, N.ptr(ws), ws.numel(),
-                N.ptr(grad_tangent), N.ptr(ptrs), N.stream_of(dev)))
-            N.check(N.lib().stb_se3_twist_grad(N.ptr(twist), N.ptr(grad_tangent),
+                *[N.ptr(t) for t in ins], B, H, W, *k, N.ptr(T), N.ptr(g), N.ptr(ws),
+                ws.numel(), N.ptr(grad_tangent), N.ptr(grad_depth), N.stream_of(dev)))
+            N.check(N.lib().stb_se3_twist_grad(N.ptr(tw), N.ptr(grad_tangent),
                                                N.ptr(grad_twist), B, N.stream_of(dev)))
         return (grad_twist, grad_depth) + (None,) * 9
 

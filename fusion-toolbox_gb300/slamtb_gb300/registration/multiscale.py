@@ -37,6 +37,16 @@ class MultiscaleRegistration:
             src_feat_pyr = feature_pyramid(source_feats.to(device), scales)
         if target_feats is not None:
             tgt_feat_pyr = feature_pyramid(target_feats.to(device), scales)
+        return self.estimate_pyramid(source_pyr, target_pyr, src_feat_pyr, tgt_feat_pyr,
+                                     transform, device)
+
+    def estimate_pyramid(self, source_pyr, target_pyr, src_feat_pyr=None, tgt_feat_pyr=None,
+                         transform=None, device=None):
+        """The level loop of ``estimate_frame`` on prepared pyramids
+        (``FramePointCloud`` levels and feature maps, coarsest first)."""
+        n = len(self.estimators)
+        src_feat_pyr = src_feat_pyr or [None] * n
+        tgt_feat_pyr = tgt_feat_pyr or [None] * n
         curr_result = None
         for ((_, estimator), source, src_feats, target, tgt_feats) in zip(
                 self.estimators[::-1], source_pyr, src_feat_pyr, target_pyr, tgt_feat_pyr):

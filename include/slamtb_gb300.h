@@ -324,48 +324,56 @@ STB_API int stb_se3_exp_compose(const double *twist, const double *base,
 STB_API int stb_se3_twist_grad(const double *twist, const double *grad_tangent,
                                double *grad_twist, int32_t num_pairs, void *stream);
 
-/* Workspace bytes of stb_icp_loss_forward / _backward. */
-STB_API size_t stb_icp_loss_workspace_bytes(int32_t num_pairs,
-                                            int64_t max_target_pixels);
+/* Workspace bytes of stb_icp_loss_forward / _backward for num_pairs pairs
+ * of height x width frames. */
+STB_API size_t stb_icp_loss_workspace_bytes(int32_t num_pairs, int32_t height,
+                                            int32_t width);
 
 /*
  * Point-to-plane loss L_p = sum over correspondences of ((q - T_p s).n)^2
- * for each pair p at pose T_p (device float64 [num_pairs][16]): the
- * association of ICPOdometry (thresholds as stb_icp_estimate) at the float32
- * cast of T_p, then the residuals of the geometric term
- * (icp_jacobian_geometric.cu:82) summed in compensated float32 into
- * loss[p] (device float64 [num_pairs]).  levels: device stb_level
- * [num_pairs] (one level per pair; feature fields ignored); every pair's
- * height * width must be <= max_target_pixels.  The correspondences stay
- * in the workspace for stb_icp_loss_backward.  No counterpart in the
- * reference (its autograd ICP differentiates through PyTorch ops,
+ * for each pair p of a batch at pose T_p (device float64 [num_pairs][16]).
+ * Inputs are dense device arrays over the batch, pair p at pixel offset
+ * p * height * width: src_depth float32 [B][H][W] (metres), src_normals
+ * float32 [B][H][W][3], src_mask uint8 [B][H][W], tgt_points / tgt_normals
+ * float32 [B][H][W][3], tgt_mask uint8 [B][H][W]; fx, fy, cx, cy are the
+ * intrinsics of every frame.  Source points are the back-projection of
+ * stb_depth_to_points (scale 1, bias 0) computed in the kernels.  The
+ * association of ICPOdometry (thresholds as stb_icp_estimate) runs at the
+ * float32 cast of T_p, then the residuals of the geometric term
+ * (icp_jacobian_geometric.cu:82) are summed in compensated float32 into
+ * loss[p] (device float64 [num_pairs]).  The correspondences stay in the
+ * workspace for stb_icp_loss_backward.  No counterpart in the reference
+ * (its autograd ICP differentiates through PyTorch ops,
  * slamtb/registration/autogradicp.py:145-239).
  */
-STB_API int stb_icp_loss_forward(const stb_level *levels, int32_t num_pairs,
+STB_API int stb_icp_loss_forward(const float *src_depth, const float *src_normals,
+                                 const uint8_t *src_mask, const float *tgt_points,
+                                 const float *tgt_normals, const uint8_t *tgt_mask,
+                                 int32_t num_pairs, int32_t height, int32_t width,
+                                 float fx, float fy, float cx, float cy,
                                  const double *poses, double distance_thresh,
-                                 double normal_angle_thresh,
-                                 int64_t max_target_pixels, void *workspace,
-                                 size_t workspace_bytes, double *loss,
-                                 void *stream);
+                                 double normal_angle_thresh, void *workspace,
+                                 size_t workspace_bytes, double *loss, void *stream);
 
 /*
  * Adjoint of stb_icp_loss_forward at the correspondences it found (same
- * levels, poses and workspace): with g = grad_loss[p],
- *   grad_twist[p] = g * dL_p/dxi = -2 g sum r J,  J = [n; Tp x n], for the
- *     left perturbation T <- exp(xi) T_p (device float64 [num_pairs][6]),
+ * inputs, poses and workspace): with g = grad_loss[p],
+ *   grad_tangent[p] = g * dL_p/de = -2 g sum r J,  J = [n; Tp x n], for the
+ *     left perturbation T <- exp(e) T_p (device float64 [num_pairs][6]),
  *   grad_depth[p][i] = g * dL_p/dz_i = -2 g r_i (R^T n).((u_i - cx)/fx,
- *     (v_i - cy)/fy, 1) for the source pixel i = v_i * width + u_i (the
- *     source grid has the target's size and intrinsics), 0 where source
- *     pixel i has no correspondence (device float32 array per pair:
- *     grad_depth is a device array [num_pairs] of pointers).
+ *     (v_i - cy)/fy, 1) for source pixel i = v_i * width + u_i, 0 where
+ *     source pixel i has no correspondence (device float32 [B][H][W]).
  * Either output may be NULL.  Source normals only gate the association and
  * get no gradient.
  */
-STB_API int stb_icp_loss_backward(const stb_level *levels, int32_t num_pairs,
+STB_API int stb_icp_loss_backward(const float *src_depth, const float *src_normals,
+                                  const uint8_t *src_mask, const float *tgt_points,
+                                  const float *tgt_normals, const uint8_t *tgt_mask,
+                                  int32_t num_pairs, int32_t height, int32_t width,
+                                  float fx, float fy, float cx, float cy,
                                   const double *poses, const double *grad_loss,
-                                  int64_t max_target_pixels, void *workspace,
-                                  size_t workspace_bytes, double *grad_twist,
-                                  float *const *grad_depth, void *stream);
+                                  void *workspace, size_t workspace_bytes,
+                                  double *grad_tangent, float *grad_depth, void *stream);
 
 /*
  * stb_icp_estimate without any allocation.  No counterpart in the reference:

@@ -23,14 +23,14 @@ SCALES = [1.0, 0.5, 0.5]
 ITERS = [6, 4, 3]  # finest first
 
 
-def _kw(n, wf):
-    return dict(num_iters=n, geom_weight=1.0, feat_weight=wf, distance_threshold=0.1,
+def _kw(n, wf, wg=1.0):
+    return dict(num_iters=n, geom_weight=wg, feat_weight=wf, distance_threshold=0.1,
                 normals_angle_thresh=math.radians(20))
 
 
-def _estimators(wf, iters=ITERS, scales=SCALES):
+def _estimators(wf, iters=ITERS, scales=SCALES, wg=1.0):
     from slamtb_gb300.registration import ICPOdometry
-    return [(s, ICPOdometry(n, **{k: v for k, v in _kw(n, wf).items() if k != "num_iters"}))
+    return [(s, ICPOdometry(n, **{k: v for k, v in _kw(n, wf, wg).items() if k != "num_iters"}))
             for s, n in zip(scales, iters)]
 
 
@@ -44,20 +44,21 @@ def _device_levels(cuda, pyr):
     return out
 
 
-def _pair(cuda, seed, w, h, feats, scales=SCALES):
+def _pair(cuda, seed, w, h, feats, scales=SCALES, channels=0, dtype=torch.float32, **kw):
     from slamtb_gb300.processing import feature_pyramid
-    p = synthetic.make_pair(seed, width=w, height=h, feature_channels=0 if feats else None)
+    p = synthetic.make_pair(seed, width=w, height=h, feature_channels=channels if feats else None,
+                            **kw)
     spyr = fp.FramePointCloud.from_depth(p["source_depth"], p["kcam"]).pyramid(scales)
     tpyr = fp.FramePointCloud.from_depth(p["target_depth"], p["kcam"]).pyramid(scales)
     out = dict(spyr=spyr, tpyr=tpyr, src=_device_levels(cuda, spyr),
                tgt=_device_levels(cuda, tpyr))
     if feats:
-        out["sf"] = feature_pyramid(torch.from_numpy(p["source_feats"]).to(cuda), scales)
-        out["tf"] = feature_pyramid(torch.from_numpy(p["target_feats"]).to(cuda), scales)
+        out["sf"] = feature_pyramid(torch.from_numpy(p["source_feats"]).to(cuda, dtype), scales)
+        out["tf"] = feature_pyramid(torch.from_numpy(p["target_feats"]).to(cuda, dtype), scales)
     return out
 
 
-def _check_pair(hist, pair, wf, iters=ITERS, init=None):
+def _check_pair(hist, pair, wf, iters=ITERS, init=None, channel_mode="last", wg=1.0):
     """Teacher-forced check of one pair's history, level by level."""
     from slamtb_gb300 import _native as N
     off = 0
@@ -72,7 +73,7 @@ def _check_pair(hist, pair, wf, iters=ITERS, init=None):
                      tf=pair["tf"][level])
         h = hist[off:off + n]
         ok = h[:, N.HIST_OK].numpy()
-        compare_forced(h, d, x, _kw(n, wf), init=T)
+        compare_forced(h, d, x, _kw(n, wf, wg), init=T, channel_mode=channel_mode)
         done = int(ok.sum()) if ok.all() else int(np.argmin(ok))
         if done > 0:
             T = h[done - 1, N.HIST_TRANSFORM:N.HIST_TRANSFORM + 16].view(4, 4).numpy()
@@ -141,3 +142,28 @@ def test_level_handover_after_failed_first_iteration(cuda):
     br = BatchRegistration(_estimators(0.0), record_history=True)
     br.estimate_pyramids([pair["src"]], [pair["tgt"]], transforms=[torch.from_numpy(init)])
     _check_pair(br.last_history[0], pair, 0.0, init=init)
+
+
+@pytest.mark.parametrize("mode", ["last", "sum"])
+def test_bf16_sixteen_channel_four_level_batch(cuda, mode):
+    """The high-resolution feature workload at reduced size: 16:9 pairs
+    (480x270), 16 BF16 feature channels normalised per pixel, 4 levels
+    with iterations [10, 8, 5, 3], rotation up to 10 degrees and
+    translation up to 10 cm; the oracle sees the same BF16 values as
+    float32.  Weights are the reference preset's (geometric 10, feature 1,
+    slamtb/registration/preset.py:10): with 16 channels a feature weight of
+    0.1 makes the reference's weighting (J^T r by w, J^T J by w^2) overshoot
+    and the normal equations ill-conditioned (the FP64 oracle's own
+    Cholesky fails), where no float32 pose can meet a 1e-5 gate."""
+    from slamtb_gb300.registration import BatchRegistration
+    scales, iters = [1.0, 0.5, 0.5, 0.5], [10, 8, 5, 3]
+    pairs = [_pair(cuda, 60 + k, 480, 270, True, scales=scales, channels=16,
+                   dtype=torch.bfloat16, max_rot_deg=10.0, max_trans=0.1) for k in range(2)]
+    assert pairs[0]["tf"][0].dtype == torch.bfloat16 and pairs[0]["tf"][0].size(0) == 16
+    br = BatchRegistration(_estimators(1.0, iters=iters, scales=scales, wg=10.0),
+                           feat_channel_mode=mode, record_history=True)
+    res = br.estimate_pyramids([p["src"] for p in pairs], [p["tgt"] for p in pairs],
+                               [p["sf"] for p in pairs], [p["tf"] for p in pairs])
+    for k, pair in enumerate(pairs):
+        assert res[k].transform is not None
+        _check_pair(br.last_history[k], pair, 1.0, iters=iters, channel_mode=mode, wg=10.0)
