@@ -12,6 +12,21 @@ Metric: Gauss-Newton iterations per second (whole job, all ranks).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+Secondary workloads (rank 0, N = 1, reported under "secondary"; skip with
+--no-secondary):
+  multiscale_hybrid_640x480  3 levels 640x480/320x240/160x120, iterations
+      [10, 5, 3], geometric 1.0 + greyscale feature 0.1, one pair,
+      MultiscaleRegistration and the one-pair batch kernel;
+  loss_grad_32x640x480       PointToPlaneLoss forward + backward on 32 pairs
+      at the poses of 5 Gauss-Newton iterations;
+  batch_uneven_256           256 pairs with sizes drawn from 160x120 ...
+      1280x720, 3 levels [10, 5, 3]: BatchRegistration (autotuned tile) vs
+      the plain path (MultiscaleRegistration pair by pair, CUDA graph per
+      level);
+  feature_1080p_16ch_bf16    16 pairs 1920x1080, 16 BF16 feature channels,
+      4 levels [10, 8, 5, 3], weights geometric 10 / feature 1 (the
+      reference preset), BatchRegistration vs the plain path.
+
 Under torchrun each rank registers its own pair (seeded by rank), no
 collective touches the data path (weak scaling); a barrier and a max over
 ranks bracket the timed region.
@@ -54,6 +69,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     return ap.parse_args()
 
 
@@ -211,6 +227,273 @@ def cpu_baseline(x_host):
             "sample": f"{n} registrations (10 GN iterations each) of the 640x480 pair, "
                       f"{el:.1f} s, C/OpenMP restatement of the reference CPU path"}
 
+# ---------------------------------------------------------------------------
+# secondary workloads
+# ---------------------------------------------------------------------------
+
+def device_pair(seed, w, h, device, feature_channels=None, feat_dtype=None, **kw):
+    """A seeded pair rendered on the device and prepared by the product's
+    kernels: (source FramePointCloud, target FramePointCloud, source feats,
+    target feats, ground truth)."""
+    import torch
+    from slamtb_gb300 import synthetic
+    from slamtb_gb300.frame import Frame, FrameInfo, FramePointCloud, KCamera
+    p = synthetic.make_pair(seed, width=w, height=h, feature_channels=feature_channels,
+                            device=device, **kw)
+    k = KCamera(p["kcam"])
+    src = FramePointCloud.from_frame(Frame(FrameInfo(k), p["source_depth"]), device)
+    tgt = FramePointCloud.from_frame(Frame(FrameInfo(k), p["target_depth"]), device)
+    src.normals, tgt.normals  # computed now, outside any timed region
+    sf = tf = None
+    if feature_channels is not None:
+        dt = feat_dtype or torch.float32
+        sf = torch.from_numpy(p["source_feats"]).to(device=device, dtype=dt)
+        tf = torch.from_numpy(p["target_feats"]).to(device=device, dtype=dt)
+    return src, tgt, sf, tf, p["gt"]
+
+
+def _estimators(iters, scales, wg, wf):
+    from slamtb_gb300.registration.icp import ICPOdometry
+    return [(s, ICPOdometry(n, geom_weight=wg, feat_weight=wf, distance_threshold=DIST,
+                            normals_angle_thresh=ANGLE, use_graph=True))
+            for s, n in zip(scales, iters)]
+
+
+def _pyramids(pairs, scales):
+    from slamtb_gb300.processing import feature_pyramid
+    out = []
+    for src, tgt, sf, tf, _ in pairs:
+        out.append((src.pyramid(scales), tgt.pyramid(scales),
+                    None if sf is None else feature_pyramid(sf, scales),
+                    None if tf is None else feature_pyramid(tf, scales)))
+    return out
+
+
+def _rel_pose(a, b):
+    """||log(b^-1 a)|| over max(||log b||, 1e-3), by the rotation angle and
+    translation of b^-1 a (no oracle involved)."""
+    import numpy as np
+    D = np.linalg.inv(b) @ a
+    ang = math.acos(min(1.0, max(-1.0, (np.trace(D[:3, :3]) - 1.0) / 2.0)))
+    Bb = b
+    angb = math.acos(min(1.0, max(-1.0, (np.trace(Bb[:3, :3]) - 1.0) / 2.0)))
+    return math.hypot(ang, np.linalg.norm(D[:3, 3])) / max(
+        math.hypot(angb, np.linalg.norm(Bb[:3, 3])), 1e-3)
+
+
+def _alg_bytes_batch(pyrs, iters, feat_bytes=0):
+    """Algorithmic bytes of one batch run: per level and iteration, the
+    association reads 66 B per source pixel and the reduction 45 B (+ the
+    source and target feature bytes per pixel) per target pixel; the final
+    information pass 66 + 33 B per finest pixel."""
+    total = 0
+    for spyr, tpyr, _, _ in pyrs:
+        for lv, n in zip(range(len(spyr)), iters[::-1]):
+            npx = spyr[lv].mask.numel()
+            total += n * npx * (ALG_BYTES["association"] + ALG_BYTES["reduction+solve"]
+                                + 2 * feat_bytes)
+        total += spyr[-1].mask.numel() * (ALG_BYTES["association"] + 33)
+    return total
+
+
+def _time_plain(ms, pyrs, reps):
+    """Plain path: MultiscaleRegistration.estimate_pyramid pair by pair (one
+    CUDA graph per level, the result read back per level as the reference
+    API returns it).  Returns (seconds per pass, transforms)."""
+    import torch
+    for spyr, tpyr, sfp, tfp in pyrs[:min(len(pyrs), 8)]:
+        ms.estimate_pyramid(spyr, tpyr, sfp, tfp)
+    torch.cuda.synchronize()
+    best, Ts = None, None
+    for _ in range(reps):
+        t = time.perf_counter()
+        Ts = [ms.estimate_pyramid(spyr, tpyr, sfp, tfp).transform for spyr, tpyr, sfp, tfp in pyrs]
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t
+        best = el if best is None else min(best, el)
+    return best, Ts
+
+
+def _time_batch(br, plan, reps, device):
+    import torch
+    stream = torch.cuda.current_stream(device)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(reps)]
+    for a, b in ev:
+        a.record(stream)
+        br.run(plan)
+        b.record(stream)
+    torch.cuda.synchronize(device)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    return statistics.median(ms) / 1e3
+
+
+def _compare(batch_res, plain_T):
+    worst = 0.0
+    for r, T in zip(batch_res, plain_T):
+        if r.transform is None or T is None:
+            continue
+        worst = max(worst, _rel_pose(r.transform.numpy(), T.numpy()))
+    return worst
+
+
+def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps_plain,
+                    feat_bytes=0, mode="last"):
+    from slamtb_gb300.registration import BatchRegistration, MultiscaleRegistration
+    ests = _estimators(iters, scales, wg, wf)
+    pyrs = _pyramids(pairs, scales)
+    feats = pyrs[0][2] is not None
+    br = BatchRegistration(ests, feat_channel_mode=mode)
+    plan = br.prepare([p[0] for p in pyrs], [p[1] for p in pyrs],
+                      [p[2] for p in pyrs] if feats else None,
+                      [p[3] for p in pyrs] if feats else None)
+    tune = br.autotune(plan)
+    t_batch = _time_batch(br, plan, reps_batch, device)
+    res = br.results(plan)
+    for _, est in ests:
+        est.feat_channel_mode = mode
+    t_plain, plain_T = _time_plain(MultiscaleRegistration(ests), pyrs, reps_plain)
+    B = len(pairs)
+    alg = _alg_bytes_batch(pyrs, iters, feat_bytes)
+    peak, kind = measured_peak()
+    gt_err = [_rel_pose(r.transform.numpy(), p[4]) if r.transform is not None else None
+              for r, p in zip(res, pairs)]
+    return {
+        "workload": name, "pairs": B, "iters": iters, "scales": scales,
+        "weights": {"geometric": wg, "feature": wf},
+        "batch": {"pairs_per_s": B / t_batch, "ms_per_run": t_batch * 1e3,
+                  "tile_config": br.tile_config,
+                  "autotune_ms": {str(k): v for k, v in tune.items()},
+                  "launches_per_run": 3},
+        "plain": {"pairs_per_s": B / t_plain, "ms_per_pass": t_plain * 1e3,
+                  "path": "MultiscaleRegistration.estimate_pyramid pair by pair"},
+        "speedup_batch_vs_plain": t_plain / t_batch,
+        "max_rel_pose_diff_batch_vs_plain": _compare(res, plain_T),
+        "median_rel_pose_err_vs_ground_truth": statistics.median(
+            [e for e in gt_err if e is not None]) if any(e is not None for e in gt_err) else None,
+        "roofline": {"bound": "hbm", "kernel": "k_batch (whole run)",
+                     "alg_bytes_per_run": alg, "achieved": alg / t_batch / 1e9,
+                     "peak": peak, "peak_source": kind, "unit": "GB/s",
+                     "frac": alg / t_batch / 1e9 / peak},
+    }
+
+
+def secondary_multiscale(device, seed):
+    import torch
+    from slamtb_gb300.registration import BatchRegistration, MultiscaleRegistration
+    pair = device_pair(seed, 640, 480, device, feature_channels=0)
+    iters, scales = [10, 5, 3], [1.0, 0.5, 0.5]
+    ests = _estimators(iters, scales, 1.0, 0.1)
+    pyrs = _pyramids([pair], scales)
+    t_plain, Ts = _time_plain(MultiscaleRegistration(ests), pyrs * 50, 3)
+    br = BatchRegistration(ests)
+    plan = br.prepare([pyrs[0][0]], [pyrs[0][1]], [pyrs[0][2]], [pyrs[0][3]])
+    br.autotune(plan)
+    t_b = _time_batch(br, plan, 100, device)
+    res = br.results(plan)
+    return {"workload": "multiscale hybrid ICP 640x480/320x240/160x120 [10, 5, 3], "
+                        "geometric 1.0 + greyscale feature 0.1, 1 pair",
+            "plain": {"registrations_per_s": 50 / t_plain,
+                      "gn_iters_per_s": 50 * sum(iters) / t_plain,
+                      "path": "MultiscaleRegistration (CUDA graph per level, result read "
+                              "back per level)"},
+            "batch_kernel_one_pair": {"registrations_per_s": 1.0 / t_b,
+                                      "gn_iters_per_s": sum(iters) / t_b,
+                                      "tile_config": br.tile_config},
+            "max_rel_pose_diff_batch_vs_plain": _rel_pose(res[0].transform.numpy(),
+                                                          Ts[0].numpy()),
+            "rel_pose_err_vs_ground_truth": _rel_pose(res[0].transform.numpy(), pair[4])}
+
+
+def secondary_loss(device, seed, B=32):
+    import torch
+    from slamtb_gb300.registration import BatchRegistration, point_to_plane_loss
+    pairs = [device_pair(seed + 100 + k, W, H, device) for k in range(B)]
+    ests = _estimators([5], [1.0], 1.0, 0.0)
+    br = BatchRegistration(ests)
+    res = br.estimate_pyramids([[p[0]] for p in pairs], [[p[1]] for p in pairs])
+    poses = torch.stack([r.transform.to(torch.float64) for r in res]).to(device)
+    src_depth = torch.stack([p[0].points[..., 2] for p in pairs]).contiguous()
+    sn = torch.stack([p[0].normals for p in pairs]).contiguous()
+    sm = torch.stack([p[0].mask for p in pairs]).contiguous()
+    tp = torch.stack([p[1].points for p in pairs]).contiguous()
+    tn = torch.stack([p[1].normals for p in pairs]).contiguous()
+    tm = torch.stack([p[1].mask for p in pairs]).contiguous()
+    kcam = pairs[0][0].kcam.params()
+    twist = torch.zeros(B, 6, dtype=torch.float64, device=device, requires_grad=True)
+    depth = src_depth.clone().requires_grad_(True)
+
+    def step():
+        twist.grad = None
+        depth.grad = None
+        loss = point_to_plane_loss(twist, depth, sn, sm, tp, tn, tm, kcam, poses,
+                                   DIST, ANGLE)
+        loss.sum().backward()
+    for _ in range(3):
+        step()
+    stream = torch.cuda.current_stream(device)
+    reps = 50
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    a.record(stream)
+    for _ in range(reps):
+        step()
+    b.record(stream)
+    torch.cuda.synchronize(device)
+    t = a.elapsed_time(b) / 1e3 / reps
+    npx = B * H * W
+    # forward: assoc 50 B/px (depth, normal, masks, target point+normal,
+    # key) + key init 8 + loss 36; backward: 36 + depth-gradient init and
+    # write 8
+    alg = npx * (50 + 8 + 36 + 44)
+    peak, kind = measured_peak()
+    return {"workload": f"point-to-plane loss forward + backward, {B} pairs 640x480 at the "
+                        "poses of 5 GN iterations", "pairs": B,
+            "pairs_per_s": B / t, "ms_per_step": t * 1e3,
+            "launches_per_step": 8,
+            "roofline": {"bound": "hbm", "alg_bytes_per_step": alg,
+                         "achieved": alg / t / 1e9, "peak": peak, "peak_source": kind,
+                         "unit": "GB/s", "frac": alg / t / 1e9 / peak}}
+
+
+def secondary_batch_uneven(device, seed, B=256):
+    import numpy as np
+    rng = np.random.default_rng(seed + 7)
+    sizes = [(160, 120), (320, 240), (640, 480), (848, 480), (1280, 720)]
+    pick = rng.integers(0, len(sizes), size=B)
+    pairs = [device_pair(seed + 1000 + k, *sizes[i], device) for k, i in enumerate(pick)]
+    out = _batch_vs_plain("batched uneven ICP, 256 pairs from {160x120 ... 1280x720}, "
+                          "3 levels [10, 5, 3], geometric", pairs, [10, 5, 3],
+                          [1.0, 0.5, 0.5], 1.0, 0.0, device, 10, 2)
+    out["size_histogram"] = {f"{w}x{h}": int((pick == i).sum()) for i, (w, h) in enumerate(sizes)}
+    return out
+
+
+def secondary_feature_1080p(device, seed, B=16):
+    import torch
+    pairs = [device_pair(seed + 2000 + k, 1920, 1080, device, feature_channels=16,
+                         feat_dtype=torch.bfloat16, max_rot_deg=10.0, max_trans=0.1)
+             for k in range(B)]
+    return _batch_vs_plain("high-resolution feature ICP, 16 pairs 1920x1080, 16 BF16 channels, "
+                           "4 levels [10, 8, 5, 3]", pairs, [10, 8, 5, 3],
+                           [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, device, 5, 1, feat_bytes=32)
+
+
+def run_secondary(device, seed):
+    out = {}
+    for name, fn in (("multiscale_hybrid_640x480", secondary_multiscale),
+                     ("loss_grad_32x640x480", secondary_loss),
+                     ("batch_uneven_256", secondary_batch_uneven),
+                     ("feature_1080p_16ch_bf16", secondary_feature_1080p)):
+        t = time.perf_counter()
+        try:
+            out[name] = fn(device, seed)
+        except Exception as exc:  # reported, never hidden
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+        out[name]["wall_s"] = time.perf_counter() - t
+    return out
+
+
 
 def main():
     args = parse()
@@ -327,6 +610,9 @@ def main():
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(host)
+    secondary = None
+    if rank == 0 and world == 1 and not args.no_secondary:
+        secondary = run_secondary(device, args.seed)
 
     if rank == 0:
         launches_per_step = 1 + 2 * ITERS + 2
@@ -352,6 +638,7 @@ def main():
                     "d2h_bytes_per_step": N.RES_SIZE * 8, "steps": e2e_steps},
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clock_info,
+            "secondary": secondary,
         }))
     if world > 1:
         dist.destroy_process_group()

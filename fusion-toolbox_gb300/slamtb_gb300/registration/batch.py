@@ -18,6 +18,11 @@ from .icp import ICPOdometry
 from .result import RegistrationResult
 
 
+class BatchPlan:
+    """A prepared batch (``BatchRegistration.prepare``): device level table,
+    parameters, initial transforms, workspace and outputs."""
+
+
 class BatchRegistration:
     """Args:
         estimators (list of (float, ICPOdometry)): scale and estimator per
@@ -42,7 +47,6 @@ class BatchRegistration:
         self.record_history = record_history
         self.last_history = None
         self.tile_config = 0  # largest pixels per work item: 0 -> 8192; 1..5 -> 512 ... 8192
-        self._ws = None
 
     @property
     def scales(self):
@@ -58,12 +62,15 @@ class BatchRegistration:
                                       float(est.feat_residual_thresh))
         return arr, sum(est.num_iters for est in levels)
 
-    def launch(self, sources, targets, source_feats=None, target_feats=None,
-               transforms=None):
-        """Enqueue the batch; ``sources`` / ``targets``: per pair, the list of
-        level ``FramePointCloud`` (coarsest first), ``*_feats``: per pair the
-        list of (C, H, W) maps or None.  Returns (results (B, 96) device
-        tensor, history or None, keep-alive list)."""
+    def prepare(self, sources, targets, source_feats=None, target_feats=None,
+                transforms=None):
+        """Device description of a batch (``BatchPlan``): the level table,
+        the initial transforms, the workspace and the result buffers.
+        ``sources`` / ``targets``: per pair, the list of level
+        ``FramePointCloud`` (coarsest first); ``*_feats``: per pair the list
+        of (C, H, W) maps or None.  ``run(plan)`` launches it; the plan can
+        be launched again while its tensors hold new data of the same
+        shapes."""
         B, L = len(sources), len(self.estimators)
         if B == 0 or len(targets) != B:
             raise ValueError("sources and targets must be non-empty lists of equal length")
@@ -104,49 +111,86 @@ class BatchRegistration:
                     fx, fy, cx, cy)
                 biggest = max(biggest, h * w)
             total_px += biggest
-        levels_dev = torch.frombuffer(bytearray(bytes(lv)), dtype=torch.uint8).to(device)
-        keep.append(levels_dev)
-        params, total_iters = self._params()
-        init = None
+        plan = BatchPlan()
+        plan.B, plan.L, plan.device = B, L, device
+        plan.levels = torch.frombuffer(bytearray(bytes(lv)), dtype=torch.uint8).to(device)
+        plan.params, plan.total_iters = self._params()
+        plan.channels, plan.code, plan.total_px = channels, code, total_px
+        plan.init = None
         if transforms is not None:
-            init = torch.stack([torch.eye(4, dtype=torch.float64) if t is None else
-                                torch.as_tensor(t, dtype=torch.float64).cpu()
-                                for t in transforms]).to(device).contiguous()
-            keep.append(init)
+            plan.init = torch.stack([torch.eye(4, dtype=torch.float64) if t is None else
+                                     torch.as_tensor(t, dtype=torch.float64).cpu()
+                                     for t in transforms]).to(device).contiguous()
         need = int(N.lib().stb_icp_batch_workspace_bytes(B, total_px))
-        if self._ws is None or self._ws.device != device or self._ws.numel() < need:
-            self._ws = torch.empty(need, dtype=torch.uint8, device=device)
-        results = torch.empty(B, N.RES_SIZE, dtype=torch.float64, device=device)
-        hist = None
+        plan.ws = torch.empty(need, dtype=torch.uint8, device=device)
+        plan.results = torch.empty(B, N.RES_SIZE, dtype=torch.float64, device=device)
+        plan.history = None
         if self.record_history:
-            hist = torch.zeros(B, max(total_iters, 1), N.HIST_SIZE, dtype=torch.float64,
-                               device=device)
-        with torch.cuda.device(device):
-            N.check(N.lib().stb_icp_estimate_batch(
-                N.ptr(levels_dev), B, L, ctypes.cast(params, ctypes.c_void_p), channels, code,
-                0 if self.feat_channel_mode == "last" else 1, N.ptr(init), total_px,
-                N.ptr(self._ws), self._ws.numel(), N.ptr(results), N.ptr(hist),
-                int(self.tile_config), N.stream_of(device)))
-        return results, hist, keep
+            plan.history = torch.zeros(B, max(plan.total_iters, 1), N.HIST_SIZE,
+                                       dtype=torch.float64, device=device)
+        plan.num_source = [sources[p][-1].mask.numel() for p in range(B)]
+        plan.keep = keep
+        plan.mode = 0 if self.feat_channel_mode == "last" else 1
+        return plan
 
-    def estimate_pyramids(self, sources, targets, source_feats=None, target_feats=None,
-                          transforms=None):
-        """Register every pair; returns a list of ``RegistrationResult``
-        (the finest level's, as ``MultiscaleRegistration``)."""
-        results, hist, _ = self.launch(sources, targets, source_feats, target_feats,
-                                       transforms)
-        out = results.cpu()
-        if hist is not None:
-            self.last_history = hist.cpu()
-        res = []
-        for p in range(len(sources)):
-            n = sources[p][-1].mask.numel()
-            res.append(ICPOdometry._result(out[p], n, torch.float32))
+    def run(self, plan, tile_config=None):
+        """Enqueue ``plan`` on the current stream (one cooperative launch);
+        returns (results (B, 96) device tensor, history or None)."""
+        cfg = self.tile_config if tile_config is None else tile_config
+        with torch.cuda.device(plan.device):
+            N.check(N.lib().stb_icp_estimate_batch(
+                N.ptr(plan.levels), plan.B, plan.L, ctypes.cast(plan.params, ctypes.c_void_p),
+                plan.channels, plan.code, plan.mode, N.ptr(plan.init), plan.total_px,
+                N.ptr(plan.ws), plan.ws.numel(), N.ptr(plan.results), N.ptr(plan.history),
+                int(cfg), N.stream_of(plan.device)))
+        return plan.results, plan.history
+
+    def autotune(self, plan, configs=(0, 1, 2, 3, 4, 5), reps=3):
+        """Times ``plan`` under each tile configuration (largest pixels per
+        work item: 0 -> 8192, 1..5 -> 512 ... 8192) with CUDA events and
+        keeps the fastest in ``self.tile_config``.  Returns {config: ms}."""
+        stream = torch.cuda.current_stream(plan.device)
+        times = {}
+        for cfg in configs:
+            self.run(plan, cfg)  # warm-up
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record(stream)
+            for _ in range(reps):
+                self.run(plan, cfg)
+            ev[1].record(stream)
+            ev[1].synchronize()
+            times[cfg] = ev[0].elapsed_time(ev[1]) / reps
+        self.tile_config = min(times, key=times.get)
+        return times
+
+    def launch(self, sources, targets, source_feats=None, target_feats=None,
+               transforms=None):
+        """``prepare`` + ``run``: returns (results (B, 96) device tensor,
+        history or None, the plan, which keeps the inputs alive)."""
+        plan = self.prepare(sources, targets, source_feats, target_feats, transforms)
+        results, hist = self.run(plan)
+        return results, hist, plan
+
+    def results(self, plan):
+        """Host ``RegistrationResult`` list of a launched plan (synchronises);
+        raises when the kernel stopped early."""
+        out = plan.results.cpu()
+        if plan.history is not None:
+            self.last_history = plan.history.cpu()
+        res = [ICPOdometry._result(out[p], plan.num_source[p], torch.float32)
+               for p in range(plan.B)]
         status = out[:, N.RES_STATUS].to(torch.int64)
         if bool(((status & (N.ST_TIMEOUT | N.ST_CAPACITY)) != 0).any()):
             raise RuntimeError("stb_icp_estimate_batch stopped early "
                                f"(status bits {int(status.max())})")
         return res
+
+    def estimate_pyramids(self, sources, targets, source_feats=None, target_feats=None,
+                          transforms=None):
+        """Register every pair; returns a list of ``RegistrationResult``
+        (the finest level's, as ``MultiscaleRegistration``)."""
+        _, _, plan = self.launch(sources, targets, source_feats, target_feats, transforms)
+        return self.results(plan)
 
     def pyramids(self, frames, device=None):
         """Device pyramids (coarsest first) of a list of ``Frame`` or
