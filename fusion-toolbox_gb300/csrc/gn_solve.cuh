@@ -160,125 +160,161 @@ __host__ __device__ constexpr int upper_index(int a, int b) {
 }  // namespace stb
 
 // ---------------------------------------------------------------------------
-// Warp-parallel FP64 Gauss-Newton step.  FP64 latency is ~66 cycles per
-// dependent operation on this part, so the step is laid out to keep the
-// dependent chain short: lanes 0..5 hold the rows of the 6x6 system
-// (right-looking Cholesky, pivot reciprocals by Newton-Raphson on the
-// float32 rsqrt), divisions by constants are multiplications by
-// reciprocals, and matrix products run one entry per lane.
+// Warp-parallel FP64 Gauss-Newton step.  On this part every FP64 warp
+// instruction occupies the FP64 pipe of its SM sub-partition for ~64
+// cycles, however many lanes are active and whether or not it depends on
+// the previous one, so the cost of the step is its FP64 instruction count.
+// The layout therefore makes each FP64 instruction do the work of many
+// lanes: one lane per entry of the 6x6 lower triangle plus one per
+// right-hand side entry, an LDL^T factorisation (no square roots) whose
+// column step is one multiply and one FMA for all entries, pivot
+// reciprocals from the hardware approximation refined by one Newton-Raphson
+// step, the three exponential coefficients evaluated at once on three lane
+// groups (Estrin's scheme), and sign tests on the integer bits.  ~50 FP64
+// instructions per step.
 // ---------------------------------------------------------------------------
 namespace stb {
 
-// 1/sqrt(d) for d > 0: float32 seed (relative error < 2^-22), one
-// Newton-Raphson step in FP64 (y <- y + y/2 (1 - d y^2)), which squares the
-// error to below 2^-43 (~1e-13): the pivots of the 6x6 factorisation carry
-// 13 significant digits, the Gauss-Newton update needs fewer than 8.  Seeds
-// outside the float32 range fall back to the library call.
-__device__ __forceinline__ double rsqrt_fp64(double d) {
-  const float f = (float)d;
-  if (!(f > 1e-37f && f < 1e37f)) return 1.0 / sqrt(d);
-  const double y = (double)rsqrtf(f);
-  const double e = fma(-d, y * y, 1.0);
-  return fma(0.5 * y, e, y);
+// 1/d for d > 0: rcp.approx.ftz.f64 (relative error below 2^-22) and one
+// Newton-Raphson step y <- y + y (1 - d y), which squares the error to below
+// 2^-44 (~6e-14).  A subnormal d flushes to an infinite reciprocal, which
+// turns the solution into NaN (flagged by the caller).
+__device__ __forceinline__ double rcp_fp64(double d) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+  const double e = fma(-d, y, 1.0);
+  return fma(y, e, y);
 }
 
-// SE(3) exponential like se3_exp, entries spread over the warp: lanes 0..8
-// hold R, lanes 16..24 hold V = I + B W + C W^2, lanes 0..2 then form
-// t = V v.  All lanes call it with the same xi; E (16 doubles, shared
-// memory) receives the row-major 4x4.
-__device__ inline void warp_se3_exp(const double *xi, double *E, int lane) {
+// d > 0 (false for +-0, negatives and NaN; +inf passes, as the comparison
+// does) on the integer bits, off the FP64 pipe.
+__device__ __forceinline__ bool positive_bits(double d) {
+  const long long b = __double_as_longlong(d);
+  return b > 0 && b <= 0x7ff0000000000000ll;
+}
+
+// Lane of entry (i, k), k <= i, of the 6x6 lower triangle stored column by
+// column (column k starts at 6k - k(k-1)/2); right-hand side entry i is on
+// lane 21 + i.
+__host__ __device__ constexpr int tri_lane(int i, int k) { return 6 * k - k * (k - 1) / 2 + (i - k); }
+
+// Maclaurin coefficient n (in t^2) of A = sin t / t (which = 0),
+// B = (1 - cos t) / t^2 (1) or C = (t - sin t) / t^3 (2): (-1)^n / (2n + 1 +
+// which)!, n < 8 (the series of se3_coeffs).  n is a compile-time constant,
+// which a per-lane select.
+template <int n>
+__device__ __forceinline__ double se3_series_coeff(int which) {
+  constexpr double f[18] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0,
+                            3628800.0, 39916800.0, 479001600.0, 6227020800.0, 87178291200.0,
+                            1307674368000.0, 20922789888000.0, 355687428096000.0};
+  constexpr double s = (n & 1) ? -1.0 : 1.0;
+  constexpr double ca = s / f[2 * n + 1], cb = s / f[2 * n + 2], cc = s / f[2 * n + 3];
+  return which == 0 ? ca : (which == 1 ? cb : cc);
+}
+
+// One Gauss-Newton update by one warp (all 32 lanes call it).
+//   up: the 21 packed upper-triangle entries of J^T J (shared, FP64),
+//   bv: J^T r (6), T: the current pose (16, row-major), all shared.
+// Solves J^T J x = J^T r by LDL^T with the failure rule of LAPACK potrf
+// (a pivot that is not > 0, or NaN, fails: the LDL^T pivots are the squares
+// of the Cholesky pivots), then Tn = exp(x) T.  Returns the verdict
+// (uniform); on success lanes 0..15 hold Tn's entries in tn_out (lane k ->
+// entry k), and every lane holds x in xs.
+__device__ inline bool warp_gn_update(const double *up, const double *bv, const double *T,
+                                      double *xs, double &tn_out, int lane) {
   const unsigned full = 0xffffffffu;
-  const double wx = xi[3], wy = xi[4], wz = xi[5];
-  const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
-  double A, B, C;
-  se3_coeffs(t2, A, B, C);
-  // entry (i, j) of the 3x3 blocks: lanes 0..8 -> R, lanes 16..24 -> V
-  const int e = lane & 15;
-  const int i = e / 3, j = e % 3;
-  const double w[3] = {wx, wy, wz};
-  double val = 0.0;
-  if (e < 9) {
-    // W = hat(w): W[i][j] = -w[(i+2)%3] if j == (i+1)%3, w[(i+1)%3] if j == (i+2)%3
-    const double Wij = (i == j) ? 0.0 : ((j == (i + 1) % 3) ? -w[(i + 2) % 3] : w[(i + 1) % 3]);
-    const double W2ij = fma(w[i], w[j], (i == j) ? -t2 : 0.0);  // W^2 = w w^T - |w|^2 I
-    const double c1 = (lane < 16) ? A : B, c2 = (lane < 16) ? B : C;
-    val = fma(c1, Wij, fma(c2, W2ij, (i == j) ? 1.0 : 0.0));
+  // this lane's entry (i, k); k == 6 marks the right-hand side
+  int ei = 0, ek = 0;
+  if (lane < 21) {
+    int k = 0, first = 0;
+    while (lane >= first + (6 - k)) {
+      first += 6 - k;
+      ++k;
+    }
+    ek = k;
+    ei = k + (lane - first);
+  } else if (lane < 27) {
+    ei = lane - 21;
+    ek = 6;
   }
-  if (lane < 9) E[i * 4 + j] = val;
-  // t_i = sum_k V[i][k] v_k, V[i][k] on lane 16 + 3 i + k
-  const double v0 = __shfl_sync(full, val, 16 + 3 * (lane % 3) + 0);
-  const double v1 = __shfl_sync(full, val, 16 + 3 * (lane % 3) + 1);
-  const double v2 = __shfl_sync(full, val, 16 + 3 * (lane % 3) + 2);
-  if (lane < 3) E[lane * 4 + 3] = fma(v0, xi[0], fma(v1, xi[1], v2 * xi[2]));
-  if (lane >= 12 && lane < 16) E[lane] = (lane == 15) ? 1.0 : 0.0;
-  __syncwarp();
-}
-
-// 6x6 Cholesky solve A x = b by one warp.  A: 36 doubles (row-major, full
-// symmetric), b: 6 doubles, x: 6 doubles out; all in shared memory.  Lane i
-// holds row i; the forward substitution L y = b runs inside the
-// factorisation loop.  Returns the LAPACK potrf verdict (false when a pivot
-// is not > 0 or NaN), uniform across the warp.
-__device__ inline bool warp_cholesky_solve6(const double *A, const double *b, double *x,
-                                            double *L /* 36 doubles scratch */, int lane) {
-  const unsigned full = 0xffffffffu;
-  const int i = lane < 6 ? lane : 5;
-  double row[6];
-#pragma unroll
-  for (int k = 0; k < 6; ++k) row[k] = A[i * 6 + k];
-  double yi = (lane < 6) ? b[lane] : 0.0;
-  double my_inv = 0.0;
+  const bool is_rhs = (lane >= 21 && lane < 27);
+  const bool is_tri = lane < 21;
+  double v = 0.0;
+  if (is_tri) v = up[upper_index(ek, ei)];
+  if (is_rhs) v = bv[ei];
   bool ok = true;
+  // forward: LDL^T factorisation with L z = b and y = D^-1 z fused in
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    const double d = __shfl_sync(full, row[j], j);
-    ok = ok && (d > 0.0);
-    if (!ok) break;
-    const double inv = rsqrt_fp64(d);
-    if (lane == j) my_inv = inv;
-    // column j of L and y_j
-    if (i >= j) row[j] *= inv;
-    const double yj = __shfl_sync(full, yi * inv, j);
-    if (lane == j) yi = yj;
-    if (lane > j && lane < 6) yi = fma(-row[j], yj, yi);
-    // trailing update A'[i][k] -= L[i][j] L[k][j] for k > j
-#pragma unroll
-    for (int k = j + 1; k < 6; ++k) {
-      const double lkj = __shfl_sync(full, row[j], k);
-      if (i >= k) row[k] = fma(-row[j], lkj, row[k]);
-    }
+    const double piv = __shfl_sync(full, v, tri_lane(j, j));
+    ok = ok && positive_bits(piv);
+    const double inv = rcp_fp64(piv);
+    const int src_i = (ei >= j) ? tri_lane(ei, j) : 0;
+    const int src_k = is_rhs ? 21 + j : ((ek >= j && ek < 6) ? tri_lane(ek, j) : 0);
+    const double aij = __shfl_sync(full, v, src_i);
+    const double akj = __shfl_sync(full, v, src_k);
+    const bool own_y = is_rhs && ei == j;
+    const double t = (own_y ? v : aij) * inv;  // L_ij, or y_j on the rhs lane j
+    const bool upd = (is_tri && ek > j && ei >= ek) || (is_rhs && ei > j);
+    const double nv = fma(-t, akj, v);
+    if (upd) v = nv;
+    if ((is_tri && ek == j && ei > j) || own_y) v = t;
   }
   if (!ok) return false;
-  if (lane < 6) {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) L[lane * 6 + k] = (k <= lane) ? row[k] : 0.0;
-  }
-  __syncwarp();
-  // backward: L^T x = y
-  double xi = yi;
+  // backward: L^T x = y; rhs lane i ends with x_i
 #pragma unroll
   for (int j = 5; j >= 0; --j) {
-    const double xj = __shfl_sync(full, xi * my_inv, j);
-    if (lane == j) xi = xj;
-    if (lane < j) xi = fma(-L[j * 6 + lane], xj, xi);
+    const double xj = __shfl_sync(full, v, 21 + j);
+    xs[j] = xj;
+    if (j > 0) {
+      const int src = (is_rhs && ei < j) ? tri_lane(j, ei) : 0;
+      const double lji = __shfl_sync(full, v, src);
+      const double nv = fma(-lji, xj, v);
+      if (is_rhs && ei < j) v = nv;
+    }
   }
-  if (lane < 6) x[lane] = xi;
-  __syncwarp();
+  // exp(x): coefficients A (lanes 0..9), B (10..19), C (20..31) at once
+  const double wx = xs[3], wy = xs[4], wz = xs[5];
+  const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
+  double A, B, C;
+  if (t2 < 0.25) {
+    const int which = lane < 10 ? 0 : (lane < 20 ? 1 : 2);
+    const double u2 = t2 * t2, u4 = u2 * u2;
+    const double a01 = fma(se3_series_coeff<1>(which), t2, se3_series_coeff<0>(which));
+    const double a23 = fma(se3_series_coeff<3>(which), t2, se3_series_coeff<2>(which));
+    const double a45 = fma(se3_series_coeff<5>(which), t2, se3_series_coeff<4>(which));
+    const double a67 = fma(se3_series_coeff<7>(which), t2, se3_series_coeff<6>(which));
+    const double coef = fma(u4, fma(u2, a67, a45), fma(u2, a23, a01));
+    A = __shfl_sync(full, coef, 0);
+    B = __shfl_sync(full, coef, 10);
+    C = __shfl_sync(full, coef, 20);
+  } else {
+    se3_coeffs(t2, A, B, C);
+  }
+  // lanes 0..8 hold R_ac = I + A W + B W^2, lanes 9..17 V_ac = I + B W + C W^2
+  const int e = lane < 9 ? lane : (lane < 18 ? lane - 9 : 0);
+  const int ea = e / 3, ec = e % 3;
+  const double wa = ea == 0 ? wx : (ea == 1 ? wy : wz);
+  const double wc = ec == 0 ? wx : (ec == 1 ? wy : wz);
+  // W = hat(w): W_01 = -wz, W_02 = wy, W_10 = wz, W_12 = -wx, W_20 = -wy, W_21 = wx
+  const double Wac = e == 1 ? -wz : e == 2 ? wy : e == 3 ? wz : e == 5 ? -wx : e == 6 ? -wy
+                   : e == 7 ? wx : 0.0;
+  const bool diag = (ea == ec);
+  const double W2ac = fma(wa, wc, diag ? -t2 : 0.0);  // W^2 = w w^T - |w|^2 I
+  const bool isR = lane < 9;
+  const double val = fma(isR ? A : B, Wac, fma(isR ? B : C, W2ac, diag ? 1.0 : 0.0));
+  // t_a = sum_c V_ac x_c (V row a on lanes 9 + 3a ...)
+  const double v0 = __shfl_sync(full, val, 9 + 3 * ea), v1 = __shfl_sync(full, val, 10 + 3 * ea),
+               v2 = __shfl_sync(full, val, 11 + 3 * ea);
+  const double ta = fma(v0, xs[0], fma(v1, xs[1], v2 * xs[2]));
+  // Tn = [R t] T: lane q = 4 row + col < 12
+  const int row = lane < 12 ? (lane >> 2) : 0, col = lane & 3;
+  const double r0 = __shfl_sync(full, val, 3 * row), r1 = __shfl_sync(full, val, 3 * row + 1),
+               r2 = __shfl_sync(full, val, 3 * row + 2), tr = __shfl_sync(full, ta, 3 * row);
+  double tn = fma(r0, T[col], fma(r1, T[4 + col], fma(r2, T[8 + col], col == 3 ? tr : 0.0)));
+  if (lane >= 12) tn = (lane == 15) ? 1.0 : 0.0;
+  tn_out = tn;
   return true;
-}
-
-// Out = E * T (rigid 4x4, row-major) by one warp: lane = entry of the 3x4.
-__device__ inline void warp_compose(const double *E, const double *T, double *Out, int lane) {
-  if (lane < 12) {
-    const int i = lane >> 2, j = lane & 3;
-    double s = fma(E[i * 4 + 0], T[0 * 4 + j],
-                   fma(E[i * 4 + 1], T[1 * 4 + j], E[i * 4 + 2] * T[2 * 4 + j]));
-    if (j == 3) s += E[i * 4 + 3];
-    Out[lane] = s;
-  } else if (lane < 16) {
-    Out[lane] = (lane == 15) ? 1.0 : 0.0;
-  }
-  __syncwarp();
 }
 
 }  // namespace stb

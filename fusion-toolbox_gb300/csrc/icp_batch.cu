@@ -55,6 +55,7 @@ struct LevelP {
 struct PairState {
   double T[16];
   Pose32 pose;
+  double last_r2, last_count;  // of the level's last successful step
   unsigned stopped, status;
   int level_iters, iters_done;
 };
@@ -399,6 +400,7 @@ __device__ __forceinline__ void load_pose(Pose32 &P, const PairState *ps) {
 struct TileCache {
   stb_level lv;
   Pose32 P;
+  double T[16];  // the pair's FP64 pose (read by the pair's last block in its step)
   int p, skip;
 };
 
@@ -428,6 +430,7 @@ __device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *o
   __syncthreads();
   if (s_new && !tc.skip) {
     load_pose(tc.P, a.ps + tc.p);
+    if (threadIdx.x >= 32 && threadIdx.x < 48) tc.T[threadIdx.x - 32] = __ldcg(a.ps[tc.p].T + threadIdx.x - 32);
     __syncthreads();
   }
   return tc.p;
@@ -513,32 +516,29 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
 // ---------------------------------------------------------------------------
 // per-pair FP64 step by warp 0 (totals in smem)
 // ---------------------------------------------------------------------------
-__device__ void pair_step(const BatchArgs &a, int p, int level, int s, const double *tot) {
-  __shared__ double A[36], b[6], x[6], L[36], E[16], T[16], Tn[16];
+__device__ void pair_step(const BatchArgs &a, int p, int level, int s, const double *tot,
+                          const double *T) {
   const int lane = threadIdx.x & 31;
   PairState *ps = a.ps + p;
   const LevelP &q = a.lp[level];
-  for (int k = lane; k < 36; k += 32) {
-    const int r = k / 6, c = k % 6;
-    A[k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
-  }
-  if (lane < 6) b[lane] = tot[kJrB + lane];
-  if (lane < 16) T[lane] = __ldcg(ps->T + lane);
-  __syncwarp();
   const double cg = tot[kCountGeomB], cf = tot[kCountFeatB];
   const double count = q.use_geom ? fmax(cg, cf) : cf;
   double *H = a.history ? a.history + ((size_t)p * a.total_iters + s) * STB_HIST_SIZE : nullptr;
-  if (H) {
-    for (int k = lane; k < 36; k += 32) H[STB_HIST_JTJ + k] = A[k];
-    if (lane < 6) H[STB_HIST_JR + lane] = b[lane];
-    if (lane == 0) {
-      H[STB_HIST_R2] = tot[kR2B];
-      H[STB_HIST_GEOM_COUNT] = cg;
-      H[STB_HIST_FEAT_COUNT] = cf;
-    }
-  }
-  const bool ok = warp_cholesky_solve6(A, b, x, L, lane);
+  double xs[6], tn;
+  const bool ok = warp_gn_update(tot, tot + kJrB, T, xs, tn, lane);
   double *R = a.results + (size_t)p * STB_RES_SIZE;
+  for (int k = lane; k < 36; k += 32) {
+    const int r = k / 6, c = k % 6;
+    const double v = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
+    if (H) H[STB_HIST_JTJ + k] = v;
+    if (ok) R[STB_RES_JTJ + k] = v;
+  }
+  if (H && lane < 6) H[STB_HIST_JR + lane] = tot[kJrB + lane];
+  if (H && lane == 0) {
+    H[STB_HIST_R2] = tot[kR2B];
+    H[STB_HIST_GEOM_COUNT] = cg;
+    H[STB_HIST_FEAT_COUNT] = cf;
+  }
   if (!ok) {
     if (lane == 0) {
       unsigned st = __ldcg(&ps->status) | STB_ST_NOT_PD;
@@ -550,32 +550,32 @@ __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const dou
     }
     return;
   }
-  warp_se3_exp(x, E, lane);
-  warp_compose(E, T, Tn, lane);
-  if (lane < 16) {
-    ps->T[lane] = Tn[lane];
-    R[STB_RES_TRANSFORM + lane] = Tn[lane];
-    if (H) H[STB_HIST_TRANSFORM + lane] = Tn[lane];
+  __shared__ float rt32[12];
+  if (lane < 12) {
+    rt32[lane] = __double2float_rn(tn);
+    ps->pose.rt[lane] = rt32[lane];
   }
-  for (int k = lane; k < 36; k += 32) R[STB_RES_JTJ + k] = A[k];
+  if (lane < 16) {
+    ps->T[lane] = tn;
+    R[STB_RES_TRANSFORM + lane] = tn;
+    if (H) H[STB_HIST_TRANSFORM + lane] = tn;
+  }
+  __syncwarp();
   if (lane == 0) {
     unsigned st = __ldcg(&ps->status);
     bool finite = true;
-    for (int k = 0; k < 6; ++k) finite &= isfinite(x[k]);
+    for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
     if (!finite) st |= STB_ST_NAN;
     if (count == 0.0) st |= STB_ST_NO_MATCHES;
     ps->status = st;
-    Pose32 P;
-    P.fx = __ldcg(&ps->pose.fx);
-    P.fy = __ldcg(&ps->pose.fy);
-    P.cx = __ldcg(&ps->pose.cx);
-    P.cy = __ldcg(&ps->pose.cy);
-    refresh_pose32(P, Tn);
-    ps->pose = P;
+    float nm[9];
+    inverse_transpose(rt32, nm);
+    for (int k = 0; k < 9; ++k) ps->pose.nm[k] = nm[k];
     const int li = __ldcg(&ps->level_iters) + 1;
     ps->level_iters = li;
     ps->iters_done = __ldcg(&ps->iters_done) + 1;
-    R[STB_RES_RESIDUAL] = tot[kR2B] / count;
+    ps->last_r2 = tot[kR2B];
+    ps->last_count = count;
     R[STB_RES_MATCHES] = count;
     R[STB_RES_ITERS] = (double)li;
     R[STB_RES_STATUS] = (double)st;
@@ -756,8 +756,13 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
       const int r = k / 6, c = k % 6;
       R[STB_RES_INFO + k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
     }
+    if (threadIdx.x == 0) {
+      // residual r2 / count of the finest level's last successful step (icp.py:251)
+      const double n = __ldcg(&a.ps[p].last_count);
+      R[STB_RES_RESIDUAL] = n > 0.0 ? __ldcg(&a.ps[p].last_r2) / n : INFINITY;
+    }
   } else if (threadIdx.x < 32) {
-    pair_step(a, p, level, s, tot);
+    pair_step(a, p, level, s, tot, tc.T);
   }
   __syncthreads();
 }
@@ -785,6 +790,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
     ps->status = 0;
     ps->level_iters = 0;
     ps->iters_done = 0;
+    ps->last_r2 = 0.0;
+    ps->last_count = 0.0;
     a.pair_ticket[p] = 0;
     double *R = a.results + p * STB_RES_SIZE;
     for (int k = 0; k < STB_RES_SIZE; ++k) R[k] = 0.0;
@@ -808,6 +815,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
       for (int k = 0; k < 16; ++k) ps->T[k] = T[k];
       ps->stopped = 0;
       ps->level_iters = 0;
+      ps->last_r2 = 0.0;
+      ps->last_count = 0.0;
       const stb_level lv = a.levels[p * a.L + level];
       Pose32 P;
       P.fx = lv.fx;

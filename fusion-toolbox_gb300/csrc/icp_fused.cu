@@ -54,6 +54,7 @@ constexpr int kJr = 21, kR2 = 27, kCountGeom = 28, kCountFeat = 29;
 struct State {
   double T[16];  // current pose, FP64
   Pose32 pose;   // its float32 view + intrinsics
+  double last_r2, last_count;  // of the last successful step (residual = r2 / count)
   unsigned ticket;
   unsigned stopped;
   unsigned status;
@@ -78,7 +79,7 @@ struct Job {
   float thr2, cos_max, feat_thr2;
   double *result, *history;
   unsigned long long *keys;
-  float *part_s, *part_c;
+  float2 *part;  // per block: kSlotAccs (sum, compensation) pairs
   int nblocks;
   State *state;
 };
@@ -95,10 +96,13 @@ inline int reduce_blocks(int64_t pixels) {
   return (int)b;
 }
 
-// Workspace: [Job slot][State slot][partials s, c: kAccs x nblocks][keys H*W]
+constexpr int kSlotAccs = 32;  // accumulator pairs per block slot (>= kAccs)
+
+// Workspace: [Job slot][State slot][block slots: nblocks x kSlotAccs float2]
+// [keys H*W]
 inline size_t workspace_bytes(int64_t pixels) {
   const int nb = reduce_blocks(pixels);
-  return 2 * kSlot + 2 * align256(sizeof(float) * kAccs * nb) +
+  return 2 * kSlot + align256(sizeof(float2) * kSlotAccs * nb) +
          align256(sizeof(unsigned long long) * pixels);
 }
 
@@ -127,6 +131,8 @@ __global__ void k_begin(Job job, Job *dst) {
   S->stopped = 0;
   S->status = 0;
   S->iters_done = 0;
+  S->last_r2 = 0.0;
+  S->last_count = 0.0;
   for (int k = 0; k < STB_RES_SIZE; ++k) job.result[k] = 0.0;
   job.result[STB_RES_RESIDUAL] = INFINITY;
 }
@@ -205,121 +211,179 @@ __device__ __forceinline__ void accumulate_se3(float *acc, const float *Jv, floa
 // Block-level compensated reduction of kN per-thread float32 partials,
 // transposed through shared memory: thread t stores its partial a at
 // red[a][t]; warp w then sums accumulators w, w + 8, ... (each lane eight
-// of the block's threads with TwoSum, then the warp's lanes by shuffles).
-// This costs ~kN / 8 warp reductions per warp instead of kN.  Threads
-// 0..kN-1 of the block end with the totals in out_s / out_c (shared).
+// of the block's threads with TwoSum, then the warp's lanes by shuffles),
+// its accumulators interleaved so that their dependent chains overlap.
+// Threads 0..kN-1 of the block end with the totals in out (shared).
 template <int kN>
 __device__ __forceinline__ void block_reduce(const float *acc, float (*red)[kReduceThreads],
-                                             float *out_s, float *out_c) {
+                                             float2 *out) {
+  constexpr int kW = kReduceThreads / 32;
+  constexpr int kPer = (kN + kW - 1) / kW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int a = 0; a < kN; ++a) red[a][threadIdx.x] = acc[a];
   __syncthreads();
-  for (int a = warp; a < kN; a += kReduceThreads / 32) {
-    float v[kReduceThreads / 32];
+  CSum t[kPer];
 #pragma unroll
-    for (int j = 0; j < kReduceThreads / 32; ++j) v[j] = red[a][lane + 32 * j];
-    CSum t = {v[0], 0.f};
+  for (int q = 0; q < kPer; ++q) {
+    const int a = warp + q * kW;
+    float v[kW];
 #pragma unroll
-    for (int j = 1; j < kReduceThreads / 32; ++j) csum_add(t, v[j]);
-    csum_warp_reduce(t);
-    if (lane == 0) {
-      out_s[a] = t.s;
-      out_c[a] = t.c;
+    for (int j = 0; j < kW; ++j) v[j] = (a < kN) ? red[a < kN ? a : 0][lane + 32 * j] : 0.f;
+    t[q] = {v[0], 0.f};
+#pragma unroll
+    for (int j = 1; j < kW; ++j) csum_add(t[q], v[j]);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      const float s2 = __shfl_down_sync(0xffffffffu, t[q].s, off);
+      const float c2 = __shfl_down_sync(0xffffffffu, t[q].c, off);
+      csum_merge(t[q], s2, c2);
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      const int a = warp + q * kW;
+      if (a < kN) out[a] = make_float2(t[q].s, t[q].c);
     }
   }
   __syncthreads();
 }
 
-// Last block: FP64 totals of kN accumulators from all block partials.  Every
-// load of a lane is issued before its additions (up to kFoldLoads slots per
-// lane per round), so the fold costs a few L2 round trips, not one per slot.
-constexpr int kFoldLoads = 8;
+// Writes the block's totals to its slot and takes a ticket; true in the
+// last block to finish (which then sees every slot).
 template <int kN>
-__device__ __forceinline__ void grid_totals(const float *part_s, const float *part_c,
-                                            int nblocks, double *tot) {
+__device__ __forceinline__ bool publish_slot(const float2 *bsum, float2 *part, unsigned *ticket,
+                                             int *is_last) {
+  if (threadIdx.x < kN) part[(size_t)blockIdx.x * kSlotAccs + threadIdx.x] = bsum[threadIdx.x];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) *is_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!*is_last) return false;
+  __threadfence();
+  return true;
+}
+
+// Last block: FP64 totals of kN accumulators from all block slots.  Warp w
+// folds slots w, w + 8, ... with lane = accumulator; every load of a round
+// (kFoldLoads slots) is issued before its additions, so 300 slots cost two
+// L2 round trips.  The eight warp results are merged through shared memory.
+constexpr int kFoldLoads = 24;
+template <int kN>
+__device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, double *tot) {
+  __shared__ float2 wsum[kReduceThreads / 32][32];
+  constexpr int kW = kReduceThreads / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
-  for (int a = warp; a < kN; a += nw) {
-    CSum t = {0.f, 0.f};
-    for (int b0 = 0; b0 < nblocks; b0 += 32 * kFoldLoads) {
-      float vs[kFoldLoads], vc[kFoldLoads];
+  CSum t = {0.f, 0.f};
+  for (int b0 = warp; b0 < nblocks; b0 += kW * kFoldLoads) {
+    float2 v[kFoldLoads];
 #pragma unroll
-      for (int k = 0; k < kFoldLoads; ++k) {
-        const int b = b0 + lane + 32 * k;
-        vs[k] = (b < nblocks) ? __ldcg(part_s + a * nblocks + b) : 0.f;
-        vc[k] = (b < nblocks) ? __ldcg(part_c + a * nblocks + b) : 0.f;
-      }
-#pragma unroll
-      for (int k = 0; k < kFoldLoads; ++k) csum_merge(t, vs[k], vc[k]);
+    for (int k = 0; k < kFoldLoads; ++k) {
+      const int b = b0 + k * kW;
+      v[k] = (b < nblocks && lane < kN) ? __ldcg(part + (size_t)b * kSlotAccs + lane)
+                                        : make_float2(0.f, 0.f);
     }
-    csum_warp_reduce(t);
-    if (lane == 0) tot[a] = (double)t.s + (double)t.c;
+#pragma unroll
+    for (int k = 0; k < kFoldLoads; ++k) csum_merge(t, v[k].x, v[k].y);
   }
+  wsum[warp][lane] = make_float2(t.s, t.c);
+  __syncthreads();
+  if (threadIdx.x < kN) {
+    CSum u = {0.f, 0.f};
+#pragma unroll
+    for (int w = 0; w < kW; ++w) csum_merge(u, wsum[w][threadIdx.x].x, wsum[w][threadIdx.x].y);
+    tot[threadIdx.x] = (double)u.s + (double)u.c;
+  }
+  __syncthreads();
+}
+
+// Per-block copy of the loop state, loaded at kernel start (the last block
+// then finds it in shared memory instead of paying an L2 round trip in the
+// serial tail).
+struct StateView {
+  double T[16];
+  unsigned status;
+  int iters_done;
+};
+
+__device__ __forceinline__ void load_state_view(StateView &V, const State *S) {
+  if (threadIdx.x < 16) V.T[threadIdx.x] = S->T[threadIdx.x];
+  if (threadIdx.x == 16) V.status = S->status;
+  if (threadIdx.x == 17) V.iters_done = S->iters_done;
 }
 
 // One Gauss-Newton step from the FP64 totals in shared memory, by one warp
-// (the warp-parallel Cholesky, exponential and composition of gn_solve.cuh).
-__device__ void gn_step_warp(const Job *J, const double *tot, int iter) {
-  __shared__ double A[36], b[6], x[6], L[36], E[16], T[16], Tn[16];
+// (warp_gn_update of gn_solve.cuh).  The residual r2 / count is stored for
+// the information pass to divide.
+__device__ void gn_step_warp(const Job *J, const StateView &V, const double *tot, int iter) {
+  __shared__ float rt32[12];
   const int lane = threadIdx.x & 31;
   State *S = J->state;
-  for (int k = lane; k < 36; k += 32) {
-    const int r = k / 6, c = k % 6;
-    A[k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
-  }
-  if (lane < 6) b[lane] = tot[kJr + lane];
-  if (lane < 16) T[lane] = __ldcg(S->T + lane);
-  __syncwarp();
   const double cg = tot[kCountGeom], cf = tot[kCountFeat];
   const double count = J->use_geom ? fmax(cg, cf) : cf;
   double *H = J->history ? J->history + (size_t)iter * STB_HIST_SIZE : nullptr;
-  if (H) {
-    for (int k = lane; k < 36; k += 32) H[STB_HIST_JTJ + k] = A[k];
-    if (lane < 6) H[STB_HIST_JR + lane] = b[lane];
-    if (lane == 0) {
-      H[STB_HIST_R2] = tot[kR2];
-      H[STB_HIST_GEOM_COUNT] = cg;
-      H[STB_HIST_FEAT_COUNT] = cf;
-    }
-  }
-  const bool ok = warp_cholesky_solve6(A, b, x, L, lane);
+  double xs[6], tn;
+  const bool ok = warp_gn_update(tot, tot + kJr, V.T, xs, tn, lane);
   double *R = J->result;
+  for (int k = lane; k < 36; k += 32) {
+    const int r = k / 6, c = k % 6;
+    const double a = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
+    if (H) H[STB_HIST_JTJ + k] = a;
+    if (ok) R[STB_RES_JTJ + k] = a;
+  }
+  if (H && lane < 6) H[STB_HIST_JR + lane] = tot[kJr + lane];
   if (!ok) {
     if (lane == 0) {
-      unsigned st = S->status | STB_ST_NOT_PD;
+      unsigned st = V.status | STB_ST_NOT_PD;
       if (count == 0.0) st |= STB_ST_NO_MATCHES;
       S->status = st;
       S->stopped = 1;
       R[STB_RES_STATUS] = (double)st;
-      if (H) H[STB_HIST_OK] = 0.0;
+      if (H) {
+        H[STB_HIST_R2] = tot[kR2];
+        H[STB_HIST_GEOM_COUNT] = cg;
+        H[STB_HIST_FEAT_COUNT] = cf;
+        H[STB_HIST_OK] = 0.0;
+      }
     }
     return;
   }
-  warp_se3_exp(x, E, lane);
-  warp_compose(E, T, Tn, lane);
-  if (lane < 16) {
-    S->T[lane] = Tn[lane];
-    R[STB_RES_TRANSFORM + lane] = Tn[lane];
-    if (H) H[STB_HIST_TRANSFORM + lane] = Tn[lane];
+  if (lane < 12) {
+    rt32[lane] = __double2float_rn(tn);
+    S->pose.rt[lane] = rt32[lane];
   }
-  for (int k = lane; k < 36; k += 32) R[STB_RES_JTJ + k] = A[k];
-  if (lane < 12) S->pose.rt[lane] = __double2float_rn(Tn[lane]);
+  if (lane < 16) {
+    S->T[lane] = tn;
+    R[STB_RES_TRANSFORM + lane] = tn;
+    if (H) H[STB_HIST_TRANSFORM + lane] = tn;
+  }
   __syncwarp();
   if (lane == 0) {
-    unsigned st = S->status;
+    unsigned st = V.status;
     bool finite = true;
-    for (int k = 0; k < 6; ++k) finite &= isfinite(x[k]);
+    for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
     if (!finite) st |= STB_ST_NAN;
     if (count == 0.0) st |= STB_ST_NO_MATCHES;
     S->status = st;
-    inverse_transpose(S->pose.rt, S->pose.nm);
-    S->iters_done += 1;
-    R[STB_RES_RESIDUAL] = tot[kR2] / count;
+    float nm[9];
+    inverse_transpose(rt32, nm);
+    for (int k = 0; k < 9; ++k) S->pose.nm[k] = nm[k];
+    S->iters_done = V.iters_done + 1;
+    S->last_r2 = tot[kR2];
+    S->last_count = count;
     R[STB_RES_MATCHES] = count;
-    R[STB_RES_ITERS] = (double)S->iters_done;
+    R[STB_RES_ITERS] = (double)(V.iters_done + 1);
     R[STB_RES_STATUS] = (double)st;
-    if (H) H[STB_HIST_OK] = 1.0;
+    if (H) {
+      H[STB_HIST_R2] = tot[kR2];
+      H[STB_HIST_GEOM_COUNT] = cg;
+      H[STB_HIST_FEAT_COUNT] = cf;
+      H[STB_HIST_OK] = 1.0;
+    }
   }
 }
 
@@ -331,14 +395,16 @@ template <typename FT, bool kGeom, bool kFeat>
 __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict__ J,
                                                            int epoch) {
   __shared__ Pose32 P;
+  __shared__ StateView V;
   __shared__ int skip;
   __shared__ float red[kAccs][kReduceThreads];
-  __shared__ float bs[kAccs], bc[kAccs];
+  __shared__ float2 bsum[kAccs];
   __shared__ int is_last;
   __shared__ double tot[kAccs];
   State *S = J->state;
   if (threadIdx.x == 0) skip = S->stopped;
   load_shared_pose(P, S);
+  load_state_view(V, S);
   __syncthreads();
   if (skip) return;
 
@@ -445,23 +511,12 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
     }
   }
 
-  block_reduce<kAccs>(acc, red, bs, bc);
-  const int nb = gridDim.x;
-  if (threadIdx.x < kAccs) {
-    J->part_s[threadIdx.x * nb + blockIdx.x] = bs[threadIdx.x];
-    J->part_c[threadIdx.x * nb + blockIdx.x] = bc[threadIdx.x];
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) is_last = (atomicAdd(&S->ticket, 1u) == (unsigned)nb - 1);
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  grid_totals<kAccs>(J->part_s, J->part_c, nb, tot);
-  __syncthreads();
+  block_reduce<kAccs>(acc, red, bsum);
+  if (!publish_slot<kAccs>(bsum, J->part, &S->ticket, &is_last)) return;
+  grid_totals<kAccs>(J->part, gridDim.x, tot);
   if (threadIdx.x < 32) {
     if (threadIdx.x == 0) S->ticket = 0;
-    gn_step_warp(J, tot, epoch);
+    gn_step_warp(J, V, tot, epoch);
   }
 }
 
@@ -470,7 +525,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
 __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__ J,
                                                          int epoch) {
   __shared__ float red[kInfoAccs][kReduceThreads];
-  __shared__ float bs[kInfoAccs], bc[kInfoAccs];
+  __shared__ float2 bsum[kInfoAccs];
   __shared__ int is_last;
   __shared__ double tot[kInfoAccs];
   State *S = J->state;
@@ -495,26 +550,18 @@ __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__
       for (int b = a; b < 6; ++b)
         acc[upper_index(a, b)] += G0[a] * G0[b] + G1[a] * G1[b] + G2[a] * G2[b];
   }
-  block_reduce<kInfoAccs>(acc, red, bs, bc);
-  const int nb = gridDim.x;
-  if (threadIdx.x < kInfoAccs) {
-    J->part_s[threadIdx.x * nb + blockIdx.x] = bs[threadIdx.x];
-    J->part_c[threadIdx.x * nb + blockIdx.x] = bc[threadIdx.x];
+  block_reduce<kInfoAccs>(acc, red, bsum);
+  if (!publish_slot<kInfoAccs>(bsum, J->part, &S->ticket, &is_last)) return;
+  grid_totals<kInfoAccs>(J->part, gridDim.x, tot);
+  double *R = J->result;
+  for (int k = threadIdx.x; k < 36; k += blockDim.x) {
+    const int r = k / 6, c = k % 6;
+    R[STB_RES_INFO + k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
   }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) is_last = (atomicAdd(&S->ticket, 1u) == (unsigned)nb - 1);
-  __syncthreads();
-  if (!is_last) return;
-  __threadfence();
-  grid_totals<kInfoAccs>(J->part_s, J->part_c, nb, tot);
-  __syncthreads();
   if (threadIdx.x == 0) {
     S->ticket = 0;
-    double *R = J->result;
-    for (int a = 0; a < 6; ++a)
-      for (int b = a; b < 6; ++b)
-        R[STB_RES_INFO + a * 6 + b] = R[STB_RES_INFO + b * 6 + a] = tot[upper_index(a, b)];
+    // the residual of the last successful step, r2 / count (icp.py:251)
+    if (S->iters_done > 0) R[STB_RES_RESIDUAL] = S->last_r2 / S->last_count;
     R[STB_RES_STATUS] = (double)S->status;
   }
 }
@@ -804,10 +851,8 @@ extern "C" int stb_icp_estimate(
   job.history = history;
   size_t off = 2 * kSlot;
   job.state = reinterpret_cast<State *>(ws + kSlot);
-  job.part_s = reinterpret_cast<float *>(ws + off);
-  off += align256(sizeof(float) * kAccs * p.nblocks);
-  job.part_c = reinterpret_cast<float *>(ws + off);
-  off += align256(sizeof(float) * kAccs * p.nblocks);
+  job.part = reinterpret_cast<float2 *>(ws + off);
+  off += align256(sizeof(float2) * kSlotAccs * p.nblocks);
   job.keys = reinterpret_cast<unsigned long long *>(ws + off);
   job.nblocks = p.nblocks;
   p.keys = job.keys;
@@ -1013,10 +1058,8 @@ extern "C" int stb_icp_estimate_static(
   job.history = history;
   size_t off = 2 * kSlot;
   job.state = reinterpret_cast<State *>(ws + kSlot);
-  job.part_s = reinterpret_cast<float *>(ws + off);
-  off += align256(sizeof(float) * kAccs * p.nblocks);
-  job.part_c = reinterpret_cast<float *>(ws + off);
-  off += align256(sizeof(float) * kAccs * p.nblocks);
+  job.part = reinterpret_cast<float2 *>(ws + off);
+  off += align256(sizeof(float2) * kSlotAccs * p.nblocks);
   job.keys = reinterpret_cast<unsigned long long *>(ws + off);
   job.nblocks = p.nblocks;
   p.keys = job.keys;
