@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--profile-case", choices=["batch", "loss", "feature"], default=None,
+                    help="run only a small case of one secondary workload (for ncu captures)")
+    ap.add_argument("--pairs", type=int, default=8, help="pairs of the --profile-case")
     return ap.parse_args()
 
 
@@ -479,6 +482,57 @@ def secondary_feature_1080p(device, seed, B=16):
                            [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, device, 5, 1, feat_bytes=32)
 
 
+def profile_case(args, device):
+    """A small case of one secondary workload, --steps runs after --warmup,
+    for profiler captures (prints one JSON line; not a bench result)."""
+    import numpy as np
+    import torch
+    from slamtb_gb300.registration import BatchRegistration, point_to_plane_loss
+    B = args.pairs
+    if args.profile_case in ("batch", "feature"):
+        if args.profile_case == "batch":
+            rng = np.random.default_rng(args.seed + 7)
+            sizes = [(160, 120), (320, 240), (640, 480), (848, 480), (1280, 720)]
+            pairs = [device_pair(args.seed + 1000 + k, *sizes[i], device)
+                     for k, i in enumerate(rng.integers(0, len(sizes), size=B))]
+            iters, scales, wg, wf, feats = [10, 5, 3], [1.0, 0.5, 0.5], 1.0, 0.0, False
+        else:
+            pairs = [device_pair(args.seed + 2000 + k, 1920, 1080, device, feature_channels=16,
+                                 feat_dtype=torch.bfloat16, max_rot_deg=10.0, max_trans=0.1)
+                     for k in range(B)]
+            iters, scales, wg, wf, feats = [10, 8, 5, 3], [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, True
+        pyrs = _pyramids(pairs, scales)
+        br = BatchRegistration(_estimators(iters, scales, wg, wf))
+        plan = br.prepare([p[0] for p in pyrs], [p[1] for p in pyrs],
+                          [p[2] for p in pyrs] if feats else None,
+                          [p[3] for p in pyrs] if feats else None)
+        run = lambda: br.run(plan)  # noqa: E731
+    else:
+        pairs = [device_pair(args.seed + 100 + k, W, H, device) for k in range(B)]
+        br = BatchRegistration(_estimators([5], [1.0], 1.0, 0.0))
+        res = br.estimate_pyramids([[p[0]] for p in pairs], [[p[1]] for p in pairs])
+        poses = torch.stack([r.transform.to(torch.float64) for r in res]).to(device)
+        st = lambda f: torch.stack([f(p) for p in pairs]).contiguous()  # noqa: E731
+        depth = st(lambda p: p[0].points[..., 2]).requires_grad_(True)
+        sn, sm = st(lambda p: p[0].normals), st(lambda p: p[0].mask)
+        tp, tn, tm = st(lambda p: p[1].points), st(lambda p: p[1].normals), st(lambda p: p[1].mask)
+        twist = torch.zeros(B, 6, dtype=torch.float64, device=device, requires_grad=True)
+        kcam = pairs[0][0].kcam.params()
+
+        def run():
+            loss = point_to_plane_loss(twist, depth, sn, sm, tp, tn, tm, kcam, poses, DIST, ANGLE)
+            loss.sum().backward()
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize(device)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        run()
+    torch.cuda.synchronize(device)
+    print(json.dumps({"profile_case": args.profile_case, "pairs": B, "steps": args.steps,
+                      "ms_per_step": 1e3 * (time.perf_counter() - t) / args.steps}))
+
+
 def run_secondary(device, seed):
     out = {}
     for name, fn in (("multiscale_hybrid_640x480", secondary_multiscale),
@@ -512,6 +566,9 @@ def main():
     from slamtb_gb300.registration.icp import ICPOdometry
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
+    if args.profile_case:
+        profile_case(args, device)
+        return
     x, host = make_inputs(args.seed + rank, device)
     icp = ICPOdometry(ITERS, geom_weight=1.0, feat_weight=0.0, distance_threshold=DIST,
                       normals_angle_thresh=ANGLE, use_graph=True)

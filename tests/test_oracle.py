@@ -246,3 +246,20 @@ def test_loss_gradients_fd_vs_analytic():
     pix = m.idx[:16]
     g, r, dr = io.loss_depth_grad_fd(T, s["points"], m, d["kcam"], 80, pix)
     np.testing.assert_allclose(g, 2 * r * dr, rtol=1e-6, atol=1e-12)
+
+
+def test_registration_verifier_rules():
+    """RegistrationVerifier (slamtb/registration/result.py:49-95): a result
+    passes when its residual, the largest covariance eigenvalue (inverse of
+    the information matrix) and its match ratio are all within bounds."""
+    import torch
+    from slamtb_gb300.registration import RegistrationResult, RegistrationVerifier
+
+    def res(residual, info_scale, ratio):
+        return RegistrationResult(torch.eye(4, dtype=torch.float64),
+                                  torch.eye(6, dtype=torch.float32) * info_scale, residual, ratio)
+    v = RegistrationVerifier()
+    assert v(res(1e-5, 1e6, 0.9))
+    assert not v(res(1e-3, 1e6, 0.9))     # residual above 1e-4
+    assert not v(res(1e-5, 1e2, 0.9))     # covariance eigenvalue 1e-2 above 1e-4
+    assert not v(res(1e-5, 1e6, 0.1))     # match ratio below 0.6
