@@ -116,7 +116,9 @@ inline Layout layout(int B, long long total_pixels) {
   l.grp_part = o;
   o += al256(sizeof(float) * kSlotFloats * (size_t)l.groups_cap);
   l.keys = o;
-  o += al256(sizeof(unsigned long long) * (size_t)total_pixels);
+  // one key per pixel of each pair's largest level, each pair's map rounded
+  // up to an even count so that it starts on a 16-byte boundary (bulk copies)
+  o += al256(sizeof(unsigned long long) * (size_t)(total_pixels + B));
   l.total = o;
   return l;
 }
@@ -248,7 +250,7 @@ __device__ void build_offsets(const BatchArgs &a) {
             const stb_level lk = a.levels[(size_t)p * a.L + k];
             m = max(m, (long long)lk.height * lk.width);
           }
-          v[3] = m;
+          v[3] = (m + 1) & ~1ll;  // even: 16-byte aligned maps
         }
       }
       // inclusive warp scans
@@ -442,8 +444,157 @@ __device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *o
 constexpr int kChunk = 4;   // pixels per thread per pipelined reduction chunk
 constexpr int kChunkA = 4;  // points per thread per pipelined association chunk
 
+// ---------------------------------------------------------------------------
+// Bulk-copy staging of a tile's contiguous streams.  A tile is walked in
+// sub-chunks of kSub pixels; each sub-chunk's streams (reduction: keys,
+// target points, target normals; association: source points, normals,
+// mask) are copied into one of two shared-memory stages by cp.async.bulk
+// (issued by thread 0, completion counted on the stage's mbarrier) while the
+// block computes on the other stage.  This keeps ~32 KB per block in flight
+// independently of occupancy; only the true gathers (winners' source points,
+// projected target pixels, feature taps) remain per-thread loads.
+// A stream whose base is not 16-byte aligned, and the bytes of a stream past
+// its last 16-byte multiple, are copied by the threads with plain loads.
+// ---------------------------------------------------------------------------
+constexpr int kSub = kThreads * kChunk;  // pixels per staged sub-chunk (1024)
+constexpr int kStageBytes = kSub * 32;   // keys 8 + xyz 12 + normal 12 per pixel
+constexpr int kStageSmem = 2 * kStageBytes;
+
+struct StageCtl {
+  unsigned long long bar[2];  // mbarriers of the two stages
+  int failed;                 // a wait ran out: the block takes no further tiles
+};
+
+struct StageStream {
+  void *dst;
+  const void *src;
+  unsigned bytes;
+  unsigned elem;  // element size of the plain copy (1, 4 or 8)
+};
+
+extern __shared__ __align__(128) unsigned char s_stage[];
+
+__device__ __forceinline__ unsigned char *stage_buf(int st) { return s_stage + st * kStageBytes; }
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void stage_init(StageCtl &ctl) {
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 2; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&ctl.bar[k])));
+    ctl.failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// Copies the streams of one sub-chunk into stage st.  All threads call it
+// (after a __syncthreads that ends every read of the stage).
+__device__ __forceinline__ void stage_issue(const StageStream *ss, int count, int st,
+                                            StageCtl &ctl) {
+  unsigned bulk[3];
+  unsigned total = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    bulk[i] = 0;
+    if (i < count) {
+      const bool al = (((uintptr_t)ss[i].src | (uintptr_t)ss[i].dst) & 15) == 0;
+      bulk[i] = al ? (ss[i].bytes & ~15u) : 0u;
+      total += bulk[i];
+    }
+  }
+  if (threadIdx.x == 0) {
+    const unsigned bar = smem_addr(&ctl.bar[st]);
+    // order the block's earlier generic reads of the stage, and the grid's
+    // generic writes of the key map, before the async-proxy copies
+    asm volatile("fence.proxy.async;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(total)
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      if (i < count && bulk[i])
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+            "[%3];" ::"r"(smem_addr(ss[i].dst)),
+            "l"(ss[i].src), "r"(bulk[i]), "r"(bar)
+            : "memory");
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (i >= count) continue;
+    const unsigned e = ss[i].elem;
+    for (unsigned off = bulk[i] + threadIdx.x * e; off < ss[i].bytes; off += kThreads * e) {
+      const char *src = static_cast<const char *>(ss[i].src) + off;
+      char *dst = static_cast<char *>(ss[i].dst) + off;
+      if (e == 8)
+        *reinterpret_cast<unsigned long long *>(dst) =
+            __ldcg(reinterpret_cast<const unsigned long long *>(src));
+      else if (e == 4)
+        *reinterpret_cast<float *>(dst) = __ldg(reinterpret_cast<const float *>(src));
+      else
+        *dst = *src;
+    }
+  }
+}
+
+// Bounded wait for stage st's copies.  ph holds this thread's expected
+// parity of both stages (bit st) and flips on success; every thread waits,
+// so every thread's ph stays the same.  False after the limit (error bit 4).
+__device__ __forceinline__ bool stage_wait(int st, StageCtl &ctl, unsigned &ph, unsigned *err) {
+  const unsigned bar = smem_addr(&ctl.bar[st]);
+  const unsigned parity = (ph >> st) & 1u;
+  for (unsigned spins = 0; spins <= kSpinLimit; ++spins) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) {
+      ph ^= 1u << st;
+      return true;
+    }
+    __nanosleep(32);
+  }
+  atomicOr(err, 4u);
+  return false;
+}
+
+// Runs a tile of nsub sub-chunks: issue(c) stages sub-chunk c (all threads
+// call it), compute(c, st) consumes stage st.  Sub-chunk c + 1 is in flight
+// while c is computed.  After a wait that ran out, every thread (the
+// decision is a block vote) waits once more, bounded, for the copies still in
+// flight, marks the block failed and returns; grid barriers then see the
+// error bit and end the kernel.
+template <typename Issue, typename Compute>
+__device__ __forceinline__ void stage_pipeline(int nsub, StageCtl &ctl, unsigned &ph,
+                                               unsigned *err, Issue issue, Compute compute) {
+  if (nsub <= 0 || ctl.failed) return;
+  issue(0);
+  if (nsub > 1) issue(1);
+  bool ok = stage_wait(0, ctl, ph, err);
+  for (int c = 0;; ++c) {
+    if (__syncthreads_or(!ok)) {
+      stage_wait(0, ctl, ph, err);
+      if (nsub > 1) stage_wait(1, ctl, ph, err);
+      if (threadIdx.x == 0) ctl.failed = 1;
+      __syncthreads();
+      return;
+    }
+    if (c > 0 && c + 1 < nsub) issue(c + 1);
+    if (c >= nsub) return;
+    const int st = c & 1;
+    compute(c, st);
+    ok = (c + 1 < nsub) ? stage_wait(st ^ 1, ctl, ph, err) : true;
+  }
+}
+
 __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *off, int level,
-                                           long long t, int s, bool force, TileCache &tc) {
+                                           long long t, int s, bool force, TileCache &tc,
+                                           StageCtl &ctl, unsigned &ph) {
   const int p = cache_pair(a, off, level, t, !force, tc);
   if (tc.skip) return;
   const Pose32 &P = tc.P;
@@ -454,32 +605,36 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
   unsigned long long *keys = a.keys + __ldcg(a.key_off + p);
   const unsigned long long tag = (unsigned long long)btag(s) << 56;
   const long long tile = __ldcg(a.level_tile + level);
+  const long long start = lt * tile;
   const long long end = min((lt + 1) * tile, (long long)lv.num_source);
-  for (long long base = lt * tile; base < end; base += kThreads * kChunkA) {
-    // round 1: source loads
-    float px[kChunkA], py[kChunkA], pz[kChunkA], nx[kChunkA], ny[kChunkA], nz[kChunkA];
-    bool ok[kChunkA];
-    long long idx[kChunkA];
-#pragma unroll
-    for (int k = 0; k < kChunkA; ++k) {
-      idx[k] = base + k * kThreads + threadIdx.x;
-      ok[k] = idx[k] < end;
-      const long long i = ok[k] ? idx[k] : 0;
-      ok[k] = ok[k] && __ldg(lv.src_mask + i);
-      px[k] = __ldg(lv.src_points + 3 * i);
-      py[k] = __ldg(lv.src_points + 3 * i + 1);
-      pz[k] = __ldg(lv.src_points + 3 * i + 2);
-      nx[k] = __ldg(lv.src_normals + 3 * i);
-      ny[k] = __ldg(lv.src_normals + 3 * i + 1);
-      nz[k] = __ldg(lv.src_normals + 3 * i + 2);
-    }
-    // round 2: projection and target gathers
+  const int nsub = start < end ? (int)((end - start + kSub - 1) / kSub) : 0;
+  // stage layout: source xyz [kSub][3] | source normal [kSub][3] | mask [kSub]
+  auto issue = [&](int c) {
+    const long long b0 = start + (long long)c * kSub;
+    const unsigned n = (unsigned)min((long long)kSub, end - b0);
+    unsigned char *buf = stage_buf(c & 1);
+    const StageStream ss[3] = {{buf, lv.src_points + 3 * b0, 12u * n, 4},
+                               {buf + kSub * 12, lv.src_normals + 3 * b0, 12u * n, 4},
+                               {buf + kSub * 24, lv.src_mask + b0, n, 1}};
+    stage_issue(ss, 3, c & 1, ctl);
+  };
+  auto compute = [&](int c, int st) {
+    const long long b0 = start + (long long)c * kSub;
+    const int n = (int)min((long long)kSub, end - b0);
+    const float *sp = reinterpret_cast<const float *>(stage_buf(st));
+    const float *sn = sp + kSub * 3;
+    const unsigned char *sm = stage_buf(st) + kSub * 24;
+    // round 1: projection and target gathers
     float3 Tp[kChunkA];
     long long pix[kChunkA];
+    bool ok[kChunkA];
     float qx[kChunkA], qy[kChunkA], qz[kChunkA], mx[kChunkA], my[kChunkA], mz[kChunkA];
 #pragma unroll
     for (int k = 0; k < kChunkA; ++k) {
-      Tp[k] = transform_point(P.rt, px[k], py[k], pz[k]);
+      const int j = k * kThreads + threadIdx.x;
+      ok[k] = j < n && sm[j < n ? j : 0];
+      const int jj = ok[k] ? j : 0;
+      Tp[k] = transform_point(P.rt, sp[3 * jj], sp[3 * jj + 1], sp[3 * jj + 2]);
       float u, v;
       project(P, Tp[k], u, v);
       int ui = 0, vi = 0;
@@ -493,24 +648,26 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
       my[k] = __ldg(lv.tgt_normals + 3 * pix[k] + 1);
       mz[k] = __ldg(lv.tgt_normals + 3 * pix[k] + 2);
     }
-    // round 3: gates and the z-buffer
+    // round 2: gates and the z-buffer
 #pragma unroll
     for (int k = 0; k < kChunkA; ++k) {
       if (!ok[k]) continue;
+      const int j = k * kThreads + threadIdx.x;
       const float dx = fsub(qx[k], Tp[k].x), dy = fsub(qy[k], Tp[k].y),
                   dz = fsub(qz[k], Tp[k].z);
       const float sq = dot3(dx, dy, dz, dx, dy, dz);
       if (sq > q.thr2) continue;
-      const float3 Tn = transform_normal(P.nm, nx[k], ny[k], nz[k]);
-      const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, mx[k], my[k], mz[k]),
-                           fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
-                                __fsqrt_rn(dot3(mx[k], my[k], mz[k], mx[k], my[k], mz[k]))));
-      if (c >= -1.0f && c <= q.cos_max) continue;
+      const float3 Tn = transform_normal(P.nm, sn[3 * j], sn[3 * j + 1], sn[3 * j + 2]);
+      const float cs = fdiv(dot3(Tn.x, Tn.y, Tn.z, mx[k], my[k], mz[k]),
+                            fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
+                                 __fsqrt_rn(dot3(mx[k], my[k], mz[k], mx[k], my[k], mz[k]))));
+      if (cs >= -1.0f && cs <= q.cos_max) continue;
       const float dist = __fsqrt_rn(sq);
       atomicMin(keys + pix[k], tag | ((unsigned long long)__float_as_uint(dist) << 24) |
-                                   (unsigned long long)idx[k]);
+                                   (unsigned long long)(b0 + j));
     }
-  }
+  };
+  stage_pipeline(nsub, ctl, ph, a.sync + 2, issue, compute);
 }
 
 // ---------------------------------------------------------------------------
@@ -589,7 +746,8 @@ __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const dou
 // ---------------------------------------------------------------------------
 template <typename FT, bool kFeat, bool kInfo>
 __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long *off, int level,
-                                            long long t, int s, TileCache &tc) {
+                                            long long t, int s, TileCache &tc, StageCtl &ctl,
+                                            unsigned &ph) {
   constexpr int kN = kInfo ? 21 : kAccsB;
   __shared__ int s_last;
   __shared__ float bs[32], bc[32];
@@ -613,94 +771,107 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   for (int k = 0; k < kN; ++k) acc[k] = 0.f;
 
   const long long tile = __ldcg(a.level_tile + level);
+  const long long start = lt * tile;
   const long long end = min((lt + 1) * tile, npix);
-  for (long long base = lt * tile; base < end; base += kThreads * kChunk) {
-  // round 1: keys and the target point / normal of every pixel (their
-  // addresses do not depend on the key); round 2: the winners' source points
-  unsigned long long key[kChunk];
-  long long pixs[kChunk];
-  float tq[kChunk][3], tnm[kChunk][3];
-  constexpr int kP = kChunk;
+  const int nsub = start < end ? (int)((end - start + kSub - 1) / kSub) : 0;
+  const bool need_n = !kInfo && q.use_geom;
+  // stage layout: keys [kSub] | target xyz [kSub][3] | target normal [kSub][3]
+  auto issue = [&](int c) {
+    const long long b0 = start + (long long)c * kSub;
+    const unsigned n = (unsigned)min((long long)kSub, end - b0);
+    unsigned char *buf = stage_buf(c & 1);
+    const StageStream ss[3] = {{buf, keys + b0, 8u * n, 8},
+                               {buf + kSub * 8, lv.tgt_points + 3 * b0, 12u * n, 4},
+                               {buf + kSub * 20, lv.tgt_normals + 3 * b0, need_n ? 12u * n : 0u, 4}};
+    stage_issue(ss, 3, c & 1, ctl);
+  };
+  auto compute = [&](int c, int st) {
+    const long long b0 = start + (long long)c * kSub;
+    const int nn = (int)min((long long)kSub, end - b0);
+    const unsigned long long *skeys = reinterpret_cast<const unsigned long long *>(stage_buf(st));
+    const float *stq = reinterpret_cast<const float *>(stage_buf(st) + kSub * 8);
+    const float *stn = reinterpret_cast<const float *>(stage_buf(st) + kSub * 20);
+    // round 1: the winners' source points (the gathers that remain)
+    unsigned long long key[kChunk];
+    float spt[kChunk][3];
 #pragma unroll
-  for (int k = 0; k < kP; ++k) {
-    pixs[k] = base + k * kThreads + threadIdx.x;
-    const long long pc = (pixs[k] < end) ? pixs[k] : 0;
-    key[k] = (pixs[k] < end) ? __ldcg(keys + pixs[k]) : 0ull;
+    for (int k = 0; k < kChunk; ++k) {
+      const int j = k * kThreads + threadIdx.x;
+      key[k] = j < nn ? skeys[j] : 0ull;
+      const bool m = (unsigned)(key[k] >> 56) == tag;
+      const long long i = (m && !kInfo) ? (long long)(key[k] & 0xffffffull) : 0;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      tq[k][d] = __ldg(lv.tgt_points + 3 * pc + d);
-      tnm[k][d] = (kInfo || !q.use_geom) ? 0.f : __ldg(lv.tgt_normals + 3 * pc + d);
+      for (int d = 0; d < 3; ++d) spt[k][d] = kInfo ? 0.f : __ldg(lv.src_points + 3 * i + d);
     }
-  }
+    // round 2: residuals, Jacobians and the per-thread sums
 #pragma unroll
-  for (int k = 0; k < kP; ++k) {
-    if ((unsigned)(key[k] >> 56) != tag || pixs[k] >= end) continue;
-    const long long pix = pixs[k];
-    const float qx = tq[k][0], qy = tq[k][1], qz = tq[k][2];
-    if (kInfo) {
-      const float G0[6] = {0.f, qz, -qy, 1.f, 0.f, 0.f};
-      const float G1[6] = {-qz, 0.f, qx, 0.f, 1.f, 0.f};
-      const float G2[6] = {qy, -qx, 0.f, 0.f, 0.f, 1.f};
-#pragma unroll
-      for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int j = i; j < 6; ++j)
-          acc[upper_index(i, j)] += G0[i] * G0[j] + G1[i] * G1[j] + G2[i] * G2[j];
-      continue;
-    }
-    const long long i = (long long)(key[k] & 0xffffffull);
-    const float3 Tp = transform_point(P.rt, __ldg(lv.src_points + 3 * i),
-                                      __ldg(lv.src_points + 3 * i + 1),
-                                      __ldg(lv.src_points + 3 * i + 2));
-    if (q.use_geom) {
-      const float nx = tnm[k][0], ny = tnm[k][1], nz = tnm[k][2];
-      const float r = dot3(fsub(qx, Tp.x), fsub(qy, Tp.y), fsub(qz, Tp.z), nx, ny, nz);
-      const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
-                           fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
-                           fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
-      acc_se3(acc, Jv, r, q.wg1, q.wg2);
-      acc[kR2B] += q.wg1 * (r * r);
-      acc[kCountGeomB] += 1.f;
-    }
-    if (kFeat && q.use_feat) {
-      const FT *tf = static_cast<const FT *>(lv.tgt_feats);
-      const FT *sf = static_cast<const FT *>(lv.src_feats);
-      const int C = a.C;
-      const long long n = lv.num_source;
-      float u, v;
-      project(P, Tp, u, v);
-      float sq = 0.f;
-      for (int c = 0; c < C; ++c) {
-        const float r = fsub(bilin(tf + c * npix, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
-        sq = fadd(sq, fmul(r, r));
+    for (int k = 0; k < kChunk; ++k) {
+      if ((unsigned)(key[k] >> 56) != tag) continue;
+      const int j = k * kThreads + threadIdx.x;
+      const float qx = stq[3 * j], qy = stq[3 * j + 1], qz = stq[3 * j + 2];
+      if (kInfo) {
+        const float G0[6] = {0.f, qz, -qy, 1.f, 0.f, 0.f};
+        const float G1[6] = {-qz, 0.f, qx, 0.f, 1.f, 0.f};
+        const float G2[6] = {qy, -qx, 0.f, 0.f, 0.f, 1.f};
+  #pragma unroll
+        for (int i = 0; i < 6; ++i)
+  #pragma unroll
+          for (int j = i; j < 6; ++j)
+            acc[upper_index(i, j)] += G0[i] * G0[j] + G1[i] * G1[j] + G2[i] * G2[j];
+        continue;
       }
-      if (!(sq > q.feat_thr2)) {
-        const float h = 0.05f;
-        const float div = fdiv(1.f, fmul(2.f, h));
-        const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
-        const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
-        const float zz = fmul(Tp.z, Tp.z);
-        const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
-        const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
-        const int c0 = (a.mode == 0) ? C - 1 : 0;
-        for (int c = c0; c < C; ++c) {
-          const FT *fc = tf + c * npix;
-          const float r = fsub(bilin(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
-          const float du = fmul(fsub(bilin(fc, H, W, uu0, v), bilin(fc, H, W, uu1, v)), div);
-          const float dv = fmul(fsub(bilin(fc, H, W, u, vv0), bilin(fc, H, W, u, vv1)), div);
-          const float gx = fmul(du, j00), gy = fmul(dv, j11),
-                      gz = fadd(fmul(du, j02), fmul(dv, j12));
-          const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
-                               fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
-                               fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
-          acc_se3(acc, Jv, r, -q.wf1, q.wf2);
+      const long long i = (long long)(key[k] & 0xffffffull);
+      const float3 Tp = transform_point(P.rt, spt[k][0], spt[k][1], spt[k][2]);
+      if (q.use_geom) {
+        const float nx = stn[3 * j], ny = stn[3 * j + 1], nz = stn[3 * j + 2];
+        const float r = dot3(fsub(qx, Tp.x), fsub(qy, Tp.y), fsub(qz, Tp.z), nx, ny, nz);
+        const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
+                             fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
+                             fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
+        acc_se3(acc, Jv, r, q.wg1, q.wg2);
+        acc[kR2B] += q.wg1 * (r * r);
+        acc[kCountGeomB] += 1.f;
+      }
+      if (kFeat && q.use_feat) {
+        const FT *tf = static_cast<const FT *>(lv.tgt_feats);
+        const FT *sf = static_cast<const FT *>(lv.src_feats);
+        const int C = a.C;
+        const long long n = lv.num_source;
+        float u, v;
+        project(P, Tp, u, v);
+        float sq = 0.f;
+        for (int c = 0; c < C; ++c) {
+          const float r = fsub(bilin(tf + c * npix, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+          sq = fadd(sq, fmul(r, r));
         }
-        acc[kR2B] += q.wf1 * sq;
-        acc[kCountFeatB] += 1.f;
+        if (!(sq > q.feat_thr2)) {
+          const float h = 0.05f;
+          const float div = fdiv(1.f, fmul(2.f, h));
+          const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
+          const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
+          const float zz = fmul(Tp.z, Tp.z);
+          const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
+          const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
+          const int c0 = (a.mode == 0) ? C - 1 : 0;
+          for (int c = c0; c < C; ++c) {
+            const FT *fc = tf + c * npix;
+            const float r = fsub(bilin(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+            const float du = fmul(fsub(bilin(fc, H, W, uu0, v), bilin(fc, H, W, uu1, v)), div);
+            const float dv = fmul(fsub(bilin(fc, H, W, u, vv0), bilin(fc, H, W, u, vv1)), div);
+            const float gx = fmul(du, j00), gy = fmul(dv, j11),
+                        gz = fadd(fmul(du, j02), fmul(dv, j12));
+            const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
+                                 fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
+                                 fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
+            acc_se3(acc, Jv, r, -q.wf1, q.wf2);
+          }
+          acc[kR2B] += q.wf1 * sq;
+          acc[kCountFeatB] += 1.f;
+        }
       }
     }
-  }
-  }
+  };
+  stage_pipeline(nsub, ctl, ph, a.sync + 2, issue, compute);
 
   block_sum<kN>(acc, bs, bc);
   float *slot = a.tile_part + (size_t)t * kSlotFloats;
@@ -774,9 +945,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
   __shared__ BatchArgs a;
   __shared__ long long s_off[kStageOff];
   __shared__ TileCache tc;
+  __shared__ StageCtl ctl;
+  unsigned ph = 0;  // expected parities of the two staging barriers
   for (int k = threadIdx.x; k < (int)(sizeof(BatchArgs) / sizeof(int)); k += blockDim.x)
     reinterpret_cast<int *>(&a)[k] = reinterpret_cast<const int *>(&args)[k];
-  __syncthreads();
+  stage_init(ctl);
   // phase 0: offsets (block 0), then pair states, key map, tickets
   if (blockIdx.x == 0) build_offsets(a);
   if (!grid_sync(a.sync)) return;
@@ -837,12 +1010,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
       const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
       reset_cache(tc);
       for (long long t = blockIdx.x; t < src_tiles; t += gridDim.x)
-        assoc_tile(a, off, level, t, s, false, tc);
+        assoc_tile(a, off, level, t, s, false, tc, ctl, ph);
       if (!grid_sync(a.sync)) return;
       off = stage_offsets(a.tgt_off + row, a.B, s_off);
       reset_cache(tc);
       for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
-        reduce_tile<FT, kFeat, false>(a, off, level, t, s, tc);
+        reduce_tile<FT, kFeat, false>(a, off, level, t, s, tc, ctl, ph);
       if (!grid_sync(a.sync)) return;
     }
   }
@@ -854,12 +1027,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
   const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
   reset_cache(tc);
   for (long long t = blockIdx.x; t < src_tiles; t += gridDim.x)
-    assoc_tile(a, off, level, t, s, true, tc);
+    assoc_tile(a, off, level, t, s, true, tc, ctl, ph);
   if (!grid_sync(a.sync)) return;
   off = stage_offsets(a.tgt_off + row, a.B, s_off);
   reset_cache(tc);
   for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
-    reduce_tile<FT, false, true>(a, off, level, t, s, tc);
+    reduce_tile<FT, false, true>(a, off, level, t, s, tc, ctl, ph);
 }
 
 // Flags every pair's status when the persistent kernel stopped early:
@@ -880,12 +1053,15 @@ int launch_batch(const BatchArgs &args, cudaStream_t st) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0);
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageSmem) !=
+      cudaSuccess)
+    return check_launch("cudaFuncSetAttribute");
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, kStageSmem);
   if (per_sm < 1) return fail(STB_ECUDA, "Cuda call error stb_icp_estimate_batch: kernel does not fit an SM");
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(sms * per_sm);
   cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = kStageSmem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -1000,7 +1176,7 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   a.tile_part = reinterpret_cast<float *>(ws + lay.tile_part);
   a.grp_part = reinterpret_cast<float *>(ws + lay.grp_part);
   a.keys = reinterpret_cast<unsigned long long *>(ws + lay.keys);
-  a.keys_cap = total_target_pixels;
+  a.keys_cap = total_target_pixels + num_pairs;
   a.tiles_cap = lay.tiles_cap;
   a.groups_cap = lay.groups_cap;
 
