@@ -303,19 +303,6 @@ __device__ void build_offsets(const BatchArgs &a) {
   }
 }
 
-template <typename T>
-__device__ __forceinline__ float bilin(const T *__restrict__ f, int H, int W, float u, float v) {
-  const int ui = (int)u, vi = (int)v;
-  const float ur = fsub(u, (float)ui), vr = fsub(v, (float)vi);
-  const float v00 = load_feat(f + (int64_t)vi * W + ui);
-  const float v10 = (ui + 1 < W) ? load_feat(f + (int64_t)vi * W + ui + 1) : 0.f;
-  const float v01 = (vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui) : 0.f;
-  const float v11 =
-      (ui + 1 < W && vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui + 1) : 0.f;
-  const float a0 = fadd(fmul(v00, fsub(1.f, ur)), fmul(v10, ur));
-  const float a1 = fadd(fmul(v01, fsub(1.f, ur)), fmul(v11, ur));
-  return fadd(fmul(a0, fsub(1.f, vr)), fmul(a1, vr));
-}
 
 // Per-thread partial sums are plain float32: a thread adds at most
 // tile / 256 <= 16 pixels, so its rounding error stays below ~1e-6 of the
@@ -744,7 +731,7 @@ __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const dou
 // ---------------------------------------------------------------------------
 // phase B: reduction of one target tile (+ group / pair folds and the step)
 // ---------------------------------------------------------------------------
-template <typename FT, bool kFeat, bool kInfo>
+template <typename FT, bool kFeat, bool kInfo, bool kHWC>
 __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long *off, int level,
                                             long long t, int s, TileCache &tc, StageCtl &ctl,
                                             unsigned &ph) {
@@ -833,15 +820,14 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
         acc[kCountGeomB] += 1.f;
       }
       if (kFeat && q.use_feat) {
-        const FT *tf = static_cast<const FT *>(lv.tgt_feats);
-        const FT *sf = static_cast<const FT *>(lv.src_feats);
-        const int C = a.C;
-        const long long n = lv.num_source;
+        const FeatView<FT, kHWC> tf{static_cast<const FT *>(lv.tgt_feats), npix, a.C};
+        const FeatView<FT, kHWC> sf{static_cast<const FT *>(lv.src_feats), lv.num_source, a.C};
+            const int C = a.C;
         float u, v;
         project(P, Tp, u, v);
         float sq = 0.f;
         for (int c = 0; c < C; ++c) {
-          const float r = fsub(bilin(tf + c * npix, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+          const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
           sq = fadd(sq, fmul(r, r));
         }
         if (!(sq > q.feat_thr2)) {
@@ -854,10 +840,11 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
           const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
           const int c0 = (a.mode == 0) ? C - 1 : 0;
           for (int c = c0; c < C; ++c) {
-            const FT *fc = tf + c * npix;
-            const float r = fsub(bilin(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
-            const float du = fmul(fsub(bilin(fc, H, W, uu0, v), bilin(fc, H, W, uu1, v)), div);
-            const float dv = fmul(fsub(bilin(fc, H, W, u, vv0), bilin(fc, H, W, u, vv1)), div);
+                        const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
+            const float du =
+                fmul(fsub(bilin_c(tf, c, H, W, uu0, v), bilin_c(tf, c, H, W, uu1, v)), div);
+            const float dv =
+                fmul(fsub(bilin_c(tf, c, H, W, u, vv0), bilin_c(tf, c, H, W, u, vv1)), div);
             const float gx = fmul(du, j00), gy = fmul(dv, j11),
                         gz = fadd(fmul(du, j02), fmul(dv, j12));
             const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
@@ -938,7 +925,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   __syncthreads();
 }
 
-template <typename FT, bool kFeat>
+template <typename FT, bool kFeat, bool kHWC>
 __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
   // the argument block is staged in shared memory so that device functions
   // can take it by reference without a per-thread local copy
@@ -1015,7 +1002,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
       off = stage_offsets(a.tgt_off + row, a.B, s_off);
       reset_cache(tc);
       for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
-        reduce_tile<FT, kFeat, false>(a, off, level, t, s, tc, ctl, ph);
+        reduce_tile<FT, kFeat, false, kHWC>(a, off, level, t, s, tc, ctl, ph);
       if (!grid_sync(a.sync)) return;
     }
   }
@@ -1032,7 +1019,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
   off = stage_offsets(a.tgt_off + row, a.B, s_off);
   reset_cache(tc);
   for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
-    reduce_tile<FT, false, true>(a, off, level, t, s, tc, ctl, ph);
+    reduce_tile<FT, false, true, false>(a, off, level, t, s, tc, ctl, ph);
 }
 
 // Flags every pair's status when the persistent kernel stopped early:
@@ -1047,9 +1034,9 @@ __global__ void k_batch_status(const unsigned *sync, double *results, int B) {
         (double)((unsigned)results[(size_t)p * STB_RES_SIZE + STB_RES_STATUS] | bits);
 }
 
-template <typename FT, bool kFeat>
+template <typename FT, bool kFeat, bool kHWC>
 int launch_batch(const BatchArgs &args, cudaStream_t st) {
-  auto kern = k_batch<FT, kFeat>;
+  auto kern = k_batch<FT, kFeat, kHWC>;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1110,7 +1097,7 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   if (any_feat) {
     if (channels <= 0)
       return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
-    if (feat_dtype != STB_F32 && feat_dtype != STB_BF16)
+    if (feat_dtype < STB_F32 || feat_dtype > STB_BF16_HWC)
       return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
   }
   if (channel_mode != 0 && channel_mode != 1)
@@ -1184,7 +1171,11 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   // barrier counters start at zero for every launch
   if (cudaMemsetAsync(a.sync, 0, kSyncBytes, st) != cudaSuccess)
     return check_launch("cudaMemsetAsync");
-  if (!any_feat) return launch_batch<float, false>(a, st);
-  if (feat_dtype == STB_F32) return launch_batch<float, true>(a, st);
-  return launch_batch<__nv_bfloat16, true>(a, st);
+  if (!any_feat) return launch_batch<float, false, false>(a, st);
+  switch (feat_dtype) {
+    case STB_F32: return launch_batch<float, true, false>(a, st);
+    case STB_BF16: return launch_batch<__nv_bfloat16, true, false>(a, st);
+    case STB_F32_HWC: return launch_batch<float, true, true>(a, st);
+    default: return launch_batch<__nv_bfloat16, true, true>(a, st);
+  }
 }

@@ -180,24 +180,6 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(const Job *__restrict__
   atomicMin(J->keys + pix, key);
 }
 
-// ---------------------------------------------------------------------------
-// Feature sampling shared with the compat kernel's arithmetic
-// (BilinearInterp, feature_map.hpp:15-41).
-template <typename T>
-__device__ __forceinline__ float bilinear(const T *__restrict__ f, int H, int W, float u,
-                                          float v) {
-  const int ui = (int)u, vi = (int)v;
-  const float ur = fsub(u, (float)ui), vr = fsub(v, (float)vi);
-  const float v00 = load_feat(f + (int64_t)vi * W + ui);
-  const float v10 = (ui + 1 < W) ? load_feat(f + (int64_t)vi * W + ui + 1) : 0.f;
-  const float v01 = (vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui) : 0.f;
-  const float v11 =
-      (ui + 1 < W && vi + 1 < H) ? load_feat(f + (int64_t)(vi + 1) * W + ui + 1) : 0.f;
-  const float a0 = fadd(fmul(v00, fsub(1.f, ur)), fmul(v10, ur));
-  const float a1 = fadd(fmul(v01, fsub(1.f, ur)), fmul(v11, ur));
-  return fadd(fmul(a0, fsub(1.f, vr)), fmul(a1, vr));
-}
-
 __device__ __forceinline__ void accumulate_se3(float *acc, const float *Jv, float r, float w1,
                                                float w2) {
 #pragma unroll
@@ -391,7 +373,7 @@ __device__ void gn_step_warp(const Job *J, const StateView &V, const double *tot
 // that do not depend on the correspondence are issued together.
 constexpr int kRP = kPixelsPerThread;
 
-template <typename FT, bool kGeom, bool kFeat>
+template <typename FT, bool kGeom, bool kFeat, bool kHWC>
 __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict__ J,
                                                            int epoch) {
   __shared__ Pose32 P;
@@ -467,17 +449,14 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
       if (kFeat) {
         // FeatureJacobianKernel (icp_jacobian_feature.cu:65-108): the gate
         // sum_c r_c^2 > thresh^2 is decided on the reference's float32 values.
-        const FT *__restrict__ tf = static_cast<const FT *>(J->tf);
-        const FT *__restrict__ sf = static_cast<const FT *>(J->sf);
         const int C = J->C;
-        const long long n = J->n;
-        const int64_t plane = npix;
+        const FeatView<FT, kHWC> tf{static_cast<const FT *>(J->tf), npix, C};
+        const FeatView<FT, kHWC> sf{static_cast<const FT *>(J->sf), J->n, C};
         float u, v;
         project(P, Tp, u, v);
         float sq = 0.f;
         for (int c = 0; c < C; ++c) {
-          const float r =
-              fsub(bilinear(tf + c * plane, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+          const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
           sq = fadd(sq, fmul(r, r));
         }
         if (!(sq > J->feat_thr2)) {
@@ -490,12 +469,11 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
           const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
           const int c0 = (J->channel_mode == 0) ? C - 1 : 0;
           for (int c = c0; c < C; ++c) {
-            const FT *fc = tf + c * plane;
-            const float r = fsub(bilinear(fc, H, W, u, v), load_feat(sf + (int64_t)c * n + i));
+            const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
             const float du =
-                fmul(fsub(bilinear(fc, H, W, uu0, v), bilinear(fc, H, W, uu1, v)), div);
+                fmul(fsub(bilin_c(tf, c, H, W, uu0, v), bilin_c(tf, c, H, W, uu1, v)), div);
             const float dv =
-                fmul(fsub(bilinear(fc, H, W, u, vv0), bilinear(fc, H, W, u, vv1)), div);
+                fmul(fsub(bilin_c(tf, c, H, W, u, vv0), bilin_c(tf, c, H, W, u, vv1)), div);
             const float gx = fmul(du, j00), gy = fmul(dv, j11),
                         gz = fadd(fmul(du, j02), fmul(dv, j12));
             const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
@@ -625,12 +603,19 @@ struct Plan {
 
 using ReduceFn = void (*)(const Job *, int);
 
+template <typename FT, bool kHWC>
+ReduceFn pick_feat_reduce(bool use_geom) {
+  return use_geom ? k_reduce<FT, true, true, kHWC> : k_reduce<FT, false, true, kHWC>;
+}
+
 ReduceFn pick_reduce(const Plan &p) {
-  if (!p.use_feat) return k_reduce<float, true, false>;
-  if (p.dtype == STB_F32)
-    return p.use_geom ? k_reduce<float, true, true> : k_reduce<float, false, true>;
-  return p.use_geom ? k_reduce<__nv_bfloat16, true, true>
-                    : k_reduce<__nv_bfloat16, false, true>;
+  if (!p.use_feat) return k_reduce<float, true, false, false>;
+  switch (p.dtype) {
+    case STB_F32: return pick_feat_reduce<float, false>(p.use_geom);
+    case STB_BF16: return pick_feat_reduce<__nv_bfloat16, false>(p.use_geom);
+    case STB_F32_HWC: return pick_feat_reduce<float, true>(p.use_geom);
+    default: return pick_feat_reduce<__nv_bfloat16, true>(p.use_geom);
+  }
 }
 
 // Everything after k_begin; k_begin itself is launched by the caller so that
@@ -782,7 +767,7 @@ extern "C" int stb_icp_estimate(
   if (use_feat) {
     if (channels <= 0)
       return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
-    if (feat_dtype != STB_F32 && feat_dtype != STB_BF16)
+    if (feat_dtype < STB_F32 || feat_dtype > STB_BF16_HWC)
       return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
     if (channel_mode != 0 && channel_mode != 1)
       return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
@@ -988,7 +973,7 @@ extern "C" int stb_icp_estimate_static(
   if (use_feat) {
     if (channels <= 0)
       return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
-    if (feat_dtype != STB_F32 && feat_dtype != STB_BF16)
+    if (feat_dtype < STB_F32 || feat_dtype > STB_BF16_HWC)
       return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
     if (channel_mode != 0 && channel_mode != 1)
       return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");

@@ -241,6 +241,32 @@ int check_down(int H, int W, float scale, int DH, int DW) {
   return STB_OK;
 }
 
+// [C][n] -> [n][C] through a shared-memory tile of kTX pixels x up to kTC
+// channels: loads coalesced along pixels, stores coalesced along channels.
+constexpr int kTX = 32, kTC = 32;
+template <typename T>
+__global__ void k_interleave(const T *__restrict__ src, T *__restrict__ dst, int C, int64_t n) {
+  __shared__ T tile[kTC][kTX + 1];
+  const int64_t x0 = (int64_t)blockIdx.x * kTX;
+  for (int c0 = 0; c0 < C; c0 += kTC) {
+    // load: thread (tx, ty) reads channel c0 + ty, pixel x0 + tx
+    for (int ty = threadIdx.y; ty < kTC; ty += blockDim.y) {
+      const int c = c0 + ty;
+      const int64_t x = x0 + threadIdx.x;
+      if (c < C && x < n) tile[ty][threadIdx.x] = src[(int64_t)c * n + x];
+    }
+    __syncthreads();
+    // store: consecutive threads write consecutive channels of a pixel
+    const int cw = min(kTC, C - c0);
+    for (int k = threadIdx.y * kTX + threadIdx.x; k < kTX * cw; k += blockDim.x * blockDim.y) {
+      const int px = k / cw, c = k % cw;
+      const int64_t x = x0 + px;
+      if (x < n) dst[x * C + c0 + c] = tile[c][px];
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 }  // namespace stb
 
@@ -365,4 +391,25 @@ extern "C" int stb_gaussian_blur3(const void *feats, int32_t channels, int32_t h
   else
     return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
   return check_launch("stb_gaussian_blur3");
+}
+
+extern "C" int stb_feature_interleave(const void *src, void *dst, int32_t channels,
+                                      int64_t count, int32_t feat_dtype, void *stream) {
+  clear_error();
+  if (channels <= 0) return fail(STB_EINVAL, "Check failed: channels must be positive");
+  if (count <= 0) return fail(STB_EINVAL, "Check failed: count must be positive");
+  STB_TRY(check_device_ptr(src, "src"));
+  STB_TRY(check_device_ptr(dst, "dst"));
+  if (src == dst) return fail(STB_EINVAL, "Check failed: interleave cannot run in place");
+  const dim3 grid((unsigned)((count + kTX - 1) / kTX)), block(kTX, 8);
+  if (feat_dtype == STB_F32)
+    k_interleave<float><<<grid, block, 0, as_stream(stream)>>>(
+        static_cast<const float *>(src), static_cast<float *>(dst), channels, count);
+  else if (feat_dtype == STB_BF16)
+    k_interleave<__nv_bfloat16><<<grid, block, 0, as_stream(stream)>>>(
+        static_cast<const __nv_bfloat16 *>(src), static_cast<__nv_bfloat16 *>(dst), channels,
+        count);
+  else
+    return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
+  return check_launch("stb_feature_interleave");
 }

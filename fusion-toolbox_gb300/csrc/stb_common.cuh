@@ -117,6 +117,37 @@ __device__ __forceinline__ float load_feat<__nv_bfloat16>(const __nv_bfloat16 *p
   return __bfloat162float(*p);
 }
 
+// Feature maps of n pixels and C channels in the reference's planar layout
+// ([C][n], kHWC = false) or texel-major ([n][C], kHWC = true: the channels of
+// a pixel share cache lines, so sampling all channels at a pixel touches a
+// few lines instead of one per channel).
+template <typename T, bool kHWC>
+struct FeatView {
+  const T *p;
+  long long n;
+  int C;
+  __device__ __forceinline__ float at(int c, long long idx) const {
+    return load_feat(p + (kHWC ? idx * C + c : (long long)c * n + idx));
+  }
+};
+
+// Bilinear sample of channel c (BilinearInterp, feature_map.hpp:15-41):
+// truncated cell, taps past the right / bottom edge read 0.
+template <typename T, bool kHWC>
+__device__ __forceinline__ float bilin_c(const FeatView<T, kHWC> &f, int c, int H, int W,
+                                         float u, float v) {
+  const int ui = (int)u, vi = (int)v;
+  const float ur = __fsub_rn(u, (float)ui), vr = __fsub_rn(v, (float)vi);
+  const long long b = (long long)vi * W + ui;
+  const float v00 = f.at(c, b);
+  const float v10 = (ui + 1 < W) ? f.at(c, b + 1) : 0.f;
+  const float v01 = (vi + 1 < H) ? f.at(c, b + W) : 0.f;
+  const float v11 = (ui + 1 < W && vi + 1 < H) ? f.at(c, b + W + 1) : 0.f;
+  const float a0 = __fadd_rn(__fmul_rn(v00, __fsub_rn(1.f, ur)), __fmul_rn(v10, ur));
+  const float a1 = __fadd_rn(__fmul_rn(v01, __fsub_rn(1.f, ur)), __fmul_rn(v11, ur));
+  return __fadd_rn(__fmul_rn(a0, __fsub_rn(1.f, vr)), __fmul_rn(a1, vr));
+}
+
 // ---------------------------------------------------------------------------
 // Compensated float32 sums: a value is carried as (s, c) with the exact sum
 // s + c; TwoSum (Knuth) keeps the rounding error of every addition.

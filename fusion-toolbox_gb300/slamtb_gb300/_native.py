@@ -14,6 +14,8 @@ from . import _build
 STB_OK = 0
 STB_F32 = 0
 STB_BF16 = 1
+STB_F32_HWC = 2   # texel-major feature layout [count][channels]
+STB_BF16_HWC = 3
 
 # result block layout (doubles), see the header
 RES_TRANSFORM, RES_JTJ, RES_INFO = 0, 16, 52
@@ -50,6 +52,7 @@ _SIGNATURES = {
     "stb_icp_batch_workspace_bytes": (_sz, [_i32, _i64]),
     "stb_icp_estimate_batch": (ctypes.c_int, [
         _vp, _i32, _i32, _vp, _i32, _i32, _i32, _vp, _i64, _vp, _sz, _vp, _vp, _i32, _vp]),
+    "stb_feature_interleave": (ctypes.c_int, [_vp, _vp, _i32, _i64, _i32, _vp]),
     "stb_se3_exp_compose": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp]),
     "stb_se3_twist_grad": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp]),
     "stb_icp_loss_workspace_bytes": (_sz, [_i32, _i32, _i32]),

@@ -102,3 +102,15 @@ def feature_pyramid(feature_map, scales):
         pyr.append(f)
     pyr.reverse()
     return pyr
+
+
+def interleave_features(feats):
+    """(C, ...) feature maps -> (count, C): the texel-major layout the
+    registration kernels sample with all channels of a pixel adjacent
+    (``stb_feature_interleave``)."""
+    dev = _dev(feats)
+    f = feats.reshape(feats.size(0), -1).contiguous()
+    c, n = f.shape
+    out = torch.empty(n, c, dtype=f.dtype, device=dev)
+    _run(dev, N.lib().stb_feature_interleave, N.ptr(f), N.ptr(out), c, n, N.feat_dtype_code(f))
+    return out

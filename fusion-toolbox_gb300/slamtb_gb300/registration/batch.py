@@ -13,6 +13,7 @@ import torch
 
 from .. import _native as N
 from ..frame import Frame, FramePointCloud, resolve_device
+from .. import processing
 from ..processing import feature_pyramid
 from .icp import ICPOdometry
 from .result import RegistrationResult
@@ -47,6 +48,7 @@ class BatchRegistration:
         self.record_history = record_history
         self.last_history = None
         self.tile_config = 0  # largest pixels per work item: 0 -> 8192; 1..5 -> 512 ... 8192
+        self.feat_layout = "auto"  # "auto": texel-major feature copies when C > 1; "planar"
 
     @property
     def scales(self):
@@ -102,6 +104,11 @@ class BatchRegistration:
                     sf = source_feats[p][l].to(device).reshape(tf.size(0), -1).contiguous()
                     channels = tf.size(0)
                     code = N.feat_dtype_code(tf)
+                    if channels > 1 and self.feat_layout == "auto":
+                        # texel-major copies, kept alive by the plan
+                        tf = processing.interleave_features(tf)
+                        sf = processing.interleave_features(sf)
+                        code += N.STB_F32_HWC
                 keep += [sp, sn, sm, tp, tn, tm, sf, tf]
                 fx, fy, cx, cy = tgt.kcam.params()
                 lv[p * L + l] = N.StbLevel(

@@ -11,6 +11,7 @@ import math
 import torch
 
 from .. import _native as N
+from .. import processing
 from .result import RegistrationResult
 
 
@@ -64,6 +65,10 @@ class ICPOdometry:
         feat_channel_mode (str): "last" (reference behaviour: with several
             feature channels only the last channel's Jacobian enters J^T J
             and J^T r) or "sum" (all channels).
+        feat_layout (str): "auto" samples feature maps of several channels
+            from texel-major copies (all channels of a pixel adjacent, built
+            on the device per call); "planar" reads the (C, H, W) maps as
+            given.  Results are identical.
         use_graph (bool): replay the launch sequence as a CUDA graph.
         record_history (bool): keep per-iteration records in
             ``self.last_history`` (float64 (num_iters, 64) CPU tensor, layout
@@ -73,7 +78,7 @@ class ICPOdometry:
     def __init__(self, num_iters, geom_weight=1.0, feat_weight=1.0, so3=False,
                  distance_threshold=.5, normals_angle_thresh=math.pi / 4,
                  feat_residual_thresh=2.75, feat_channel_mode="last",
-                 use_graph=True, record_history=False):
+                 use_graph=True, record_history=False, feat_layout="auto"):
         if so3:
             raise NotImplementedError(
                 "so3=True is not supported: the reference's rotation-only path "
@@ -83,6 +88,8 @@ class ICPOdometry:
             raise ValueError("num_iters must be at most 254")
         if feat_channel_mode not in ("last", "sum"):
             raise ValueError("feat_channel_mode must be 'last' or 'sum'")
+        if feat_layout not in ("auto", "planar"):
+            raise ValueError("feat_layout must be 'auto' or 'planar'")
         self.num_iters = num_iters
         self.geom_weight = geom_weight
         self.feat_weight = feat_weight
@@ -91,6 +98,7 @@ class ICPOdometry:
         self.normals_angle_thresh = normals_angle_thresh
         self.feat_residual_thresh = feat_residual_thresh
         self.feat_channel_mode = feat_channel_mode
+        self.feat_layout = feat_layout
         self.use_graph = use_graph
         self.record_history = record_history
         self.last_history = None
@@ -171,6 +179,12 @@ class ICPOdometry:
             channels = tf.size(0)
             if tf.shape[1:] != (h, w) or sf.size(1) != n:
                 raise RuntimeError("Check failed: feature maps do not match the point grids")
+            if channels > 1 and self.feat_layout == "auto":
+                # texel-major copies: the kernels then read all channels of a
+                # pixel from adjacent bytes (same values, same results)
+                tf = processing.interleave_features(tf)
+                sf = processing.interleave_features(sf)
+                code += N.STB_F32_HWC
         init = None
         if transform is not None:
             init = torch.as_tensor(transform).to(device=device, dtype=torch.float64).contiguous()

@@ -56,6 +56,12 @@ extern "C" {
 /* ---- element types for feature maps ----------------------------------- */
 #define STB_F32 0
 #define STB_BF16 1
+/* Texel-major feature layout ([count][channels]: all channels of a pixel
+ * adjacent) of the same element types, accepted by stb_icp_estimate and
+ * stb_icp_estimate_batch; produce it with stb_feature_interleave.  The
+ * reference's layout ([channels][count]) is STB_F32 / STB_BF16. */
+#define STB_F32_HWC 2
+#define STB_BF16_HWC 3
 
 /* ---- per-registration status bits (result block, STB_RES_STATUS) ------- */
 #define STB_ST_NOT_PD 1u     /* 6x6 J^T J was not positive definite: stopped */
@@ -299,6 +305,17 @@ STB_API int stb_icp_estimate_batch(
     int32_t channel_mode, const double *init_transforms,
     int64_t total_target_pixels, void *workspace, size_t workspace_bytes,
     double *results, double *history, int32_t tile_config, void *stream);
+
+/*
+ * dst[k * channels + c] = src[c * count + k]: feature maps from the
+ * reference's planar layout [channels][count] to the texel-major layout
+ * [count][channels] (STB_F32_HWC / STB_BF16_HWC) that the registration
+ * kernels sample with all channels of a texel in adjacent bytes.
+ * feat_dtype: STB_F32 or STB_BF16 (the element type of both arrays).  No
+ * counterpart in the reference.
+ */
+STB_API int stb_feature_interleave(const void *src, void *dst, int32_t channels,
+                                   int64_t count, int32_t feat_dtype, void *stream);
 
 /* ======================================================================= *
  * Differentiable point-to-plane loss (hand-written adjoint)

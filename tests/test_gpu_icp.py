@@ -178,3 +178,30 @@ def test_sample2_known_answer(cuda):
     _, gt_r = pose_error(np.eye(4), d["gt"])
     err_t, err_r = pose_error(res.transform.numpy(), d["gt"])
     assert err_r < 0.1 * gt_r and err_t < 1e-3
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_texel_major_layout_is_bit_identical(cuda, dtype):
+    """feat_layout="auto" (texel-major copies) and "planar" (the reference's
+    (C, H, W) maps) compute the same numbers: histories equal bit for bit."""
+    from slamtb_gb300.registration.icp import ICPOdometry
+    d = synthetic_pair(4, width=320, height=240, feature_channels=5)
+    kw = dict(GEOM, num_iters=5, feat_weight=0.05)
+    x = _dev(d, cuda, dtype)
+    hs = []
+    for layout in ("planar", "auto"):
+        icp = ICPOdometry(record_history=True, feat_channel_mode="sum", feat_layout=layout, **kw)
+        _run_gpu(x, icp)
+        hs.append(icp.last_history.numpy())
+    np.testing.assert_array_equal(hs[0], hs[1])
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_interleave_features_is_a_transpose(cuda, dtype):
+    from slamtb_gb300.processing import interleave_features
+    g = torch.Generator().manual_seed(3)
+    for c, h, w in ((1, 7, 5), (3, 33, 17), (40, 9, 31)):
+        f = torch.randn(c, h, w, generator=g).to(cuda, dtype)
+        out = interleave_features(f)
+        assert out.shape == (h * w, c)
+        assert torch.equal(out, f.reshape(c, -1).t().contiguous())
