@@ -24,6 +24,7 @@
 // (slamtb/registration/icp.py:152-262) for each pair.
 #include <math.h>
 
+#include "feature_term.cuh"
 #include "gn_solve.cuh"
 #include "stb_common.cuh"
 #include "stb_host.hpp"
@@ -822,36 +823,8 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
       if (kFeat && q.use_feat) {
         const FeatView<FT, kHWC> tf{static_cast<const FT *>(lv.tgt_feats), npix, a.C};
         const FeatView<FT, kHWC> sf{static_cast<const FT *>(lv.src_feats), lv.num_source, a.C};
-            const int C = a.C;
-        float u, v;
-        project(P, Tp, u, v);
-        float sq = 0.f;
-        for (int c = 0; c < C; ++c) {
-          const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
-          sq = fadd(sq, fmul(r, r));
-        }
-        if (!(sq > q.feat_thr2)) {
-          const float h = 0.05f;
-          const float div = fdiv(1.f, fmul(2.f, h));
-          const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
-          const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
-          const float zz = fmul(Tp.z, Tp.z);
-          const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
-          const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
-          const int c0 = (a.mode == 0) ? C - 1 : 0;
-          for (int c = c0; c < C; ++c) {
-                        const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
-            const float du =
-                fmul(fsub(bilin_c(tf, c, H, W, uu0, v), bilin_c(tf, c, H, W, uu1, v)), div);
-            const float dv =
-                fmul(fsub(bilin_c(tf, c, H, W, u, vv0), bilin_c(tf, c, H, W, u, vv1)), div);
-            const float gx = fmul(du, j00), gy = fmul(dv, j11),
-                        gz = fadd(fmul(du, j02), fmul(dv, j12));
-            const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
-                                 fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
-                                 fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
-            acc_se3(acc, Jv, r, -q.wf1, q.wf2);
-          }
+        float sq;
+        if (feature_term(tf, sf, i, P, Tp, H, W, q.feat_thr2, a.mode, q.wf1, q.wf2, acc, sq)) {
           acc[kR2B] += q.wf1 * sq;
           acc[kCountFeatB] += 1.f;
         }

@@ -29,6 +29,7 @@
 #include <tuple>
 #include <vector>
 
+#include "feature_term.cuh"
 #include "gn_solve.cuh"
 #include "stb_common.cuh"
 #include "stb_host.hpp"
@@ -447,41 +448,12 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
         acc[kCountGeom] += 1.f;
       }
       if (kFeat) {
-        // FeatureJacobianKernel (icp_jacobian_feature.cu:65-108): the gate
-        // sum_c r_c^2 > thresh^2 is decided on the reference's float32 values.
-        const int C = J->C;
-        const FeatView<FT, kHWC> tf{static_cast<const FT *>(J->tf), npix, C};
-        const FeatView<FT, kHWC> sf{static_cast<const FT *>(J->sf), J->n, C};
-        float u, v;
-        project(P, Tp, u, v);
-        float sq = 0.f;
-        for (int c = 0; c < C; ++c) {
-          const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
-          sq = fadd(sq, fmul(r, r));
-        }
-        if (!(sq > J->feat_thr2)) {
-          const float h = 0.05f;
-          const float div = fdiv(1.f, fmul(2.f, h));
-          const float uu0 = fadd(u, h), uu1 = fmaxf(fsub(u, h), 0.f);
-          const float vv0 = fadd(v, h), vv1 = fmaxf(fsub(v, h), 0.f);
-          const float zz = fmul(Tp.z, Tp.z);
-          const float j00 = fdiv(P.fx, Tp.z), j02 = fdiv(fmul(-Tp.x, P.fx), zz);
-          const float j11 = fdiv(P.fy, Tp.z), j12 = fdiv(fmul(-Tp.y, P.fy), zz);
-          const int c0 = (J->channel_mode == 0) ? C - 1 : 0;
-          for (int c = c0; c < C; ++c) {
-            const float r = fsub(bilin_c(tf, c, H, W, u, v), sf.at(c, i));
-            const float du =
-                fmul(fsub(bilin_c(tf, c, H, W, uu0, v), bilin_c(tf, c, H, W, uu1, v)), div);
-            const float dv =
-                fmul(fsub(bilin_c(tf, c, H, W, u, vv0), bilin_c(tf, c, H, W, u, vv1)), div);
-            const float gx = fmul(du, j00), gy = fmul(dv, j11),
-                        gz = fadd(fmul(du, j02), fmul(dv, j12));
-            const float Jv[6] = {gx, gy, gz, fsub(fmul(Tp.y, gz), fmul(Tp.z, gy)),
-                                 fsub(fmul(Tp.z, gx), fmul(Tp.x, gz)),
-                                 fsub(fmul(Tp.x, gy), fmul(Tp.y, gx))};
-            // J^T r enters with -w_f (icp.py:222)
-            accumulate_se3(acc, Jv, r, -wf1, wf2);
-          }
+        // FeatureJacobianKernel (icp_jacobian_feature.cu:65-108)
+        const FeatView<FT, kHWC> tf{static_cast<const FT *>(J->tf), npix, J->C};
+        const FeatView<FT, kHWC> sf{static_cast<const FT *>(J->sf), J->n, J->C};
+        float sq;
+        if (feature_term(tf, sf, i, P, Tp, H, W, J->feat_thr2, J->channel_mode, wf1, wf2, acc,
+                         sq)) {
           acc[kR2] += wf1 * sq;
           acc[kCountFeat] += 1.f;
         }

@@ -118,9 +118,9 @@ __device__ __forceinline__ float load_feat<__nv_bfloat16>(const __nv_bfloat16 *p
 }
 
 // Feature maps of n pixels and C channels in the reference's planar layout
-// ([C][n], kHWC = false) or texel-major ([n][C], kHWC = true: the channels of
-// a pixel share cache lines, so sampling all channels at a pixel touches a
-// few lines instead of one per channel).
+// ([C][n], kHWC = false) or texel-major ([n][C], kHWC = true: the channels
+// of a pixel share cache lines, so sampling all channels at a pixel touches
+// a few lines instead of one per channel).
 template <typename T, bool kHWC>
 struct FeatView {
   const T *p;
