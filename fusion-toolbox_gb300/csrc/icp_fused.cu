@@ -139,22 +139,45 @@ __global__ void k_begin(Job job, Job *dst) {
 }
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch: a kernel launched with the attribute may
+// start while its predecessor in the stream still runs; it does work that
+// does not depend on the predecessor, then waits here for its completion
+// (and the visibility of its writes).  Without the attribute the wait
+// returns at once.
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+// Lets the next kernel of the stream be scheduled (it still waits for this
+// one to complete before reading what this one writes).
+__device__ __forceinline__ void grid_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(kAssocThreads) k_assoc(const Job *__restrict__ J,
                                                          int epoch, int force) {
   __shared__ Pose32 P;
   __shared__ int skip;
+  // pose-independent prologue: this thread's source point and normal (the
+  // inputs and the Job are not written by the preceding kernel)
+  const long long n = J->n;
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool in = i < n && J->sm[i];
+  const float *__restrict__ sp = J->sp;
+  const float *__restrict__ sn = J->sn;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f, n0 = 0.f, n1 = 0.f, n2 = 0.f;
+  if (in) {
+    s0 = sp[3 * i], s1 = sp[3 * i + 1], s2 = sp[3 * i + 2];
+    n0 = sn[3 * i], n1 = sn[3 * i + 1], n2 = sn[3 * i + 2];
+  }
+  grid_dependency_wait();  // the previous reduction has written the pose
+  grid_launch_dependents();
   const State *S = J->state;
   if (threadIdx.x == 0) skip = !force && S->stopped;
   load_shared_pose(P, S);
   __syncthreads();
-  if (skip) return;
-  const long long n = J->n;
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float *__restrict__ sp = J->sp;
-  if (!J->sm[i]) return;
+  if (skip || !in) return;
   const int H = J->H, W = J->W;
-  const float3 Tp = transform_point(P.rt, sp[3 * i], sp[3 * i + 1], sp[3 * i + 2]);
+  const float3 Tp = transform_point(P.rt, s0, s1, s2);
   float u, v;
   project(P, Tp, u, v);
   int ui, vi;
@@ -166,9 +189,8 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(const Job *__restrict__
               dz = fsub(tp[3 * pix + 2], Tp.z);
   const float sq = dot3(dx, dy, dz, dx, dy, dz);
   if (sq > J->thr2) return;
-  const float *__restrict__ sn = J->sn;
   const float *__restrict__ tn = J->tn;
-  const float3 Tn = transform_normal(P.nm, sn[3 * i], sn[3 * i + 1], sn[3 * i + 2]);
+  const float3 Tn = transform_normal(P.nm, n0, n1, n2);
   const float nx = tn[3 * pix], ny = tn[3 * pix + 1], nz = tn[3 * pix + 2];
   const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, nx, ny, nz),
                        fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
@@ -385,6 +407,8 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
   __shared__ int is_last;
   __shared__ double tot[kAccs];
   State *S = J->state;
+  grid_dependency_wait();  // the association has written the key map
+  grid_launch_dependents();
   if (threadIdx.x == 0) skip = S->stopped;
   load_shared_pose(P, S);
   load_state_view(V, S);
@@ -479,6 +503,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__
   __shared__ int is_last;
   __shared__ double tot[kInfoAccs];
   State *S = J->state;
+  grid_dependency_wait();
   float acc[kInfoAccs];
 #pragma unroll
   for (int a = 0; a < kInfoAccs; ++a) acc[a] = 0.f;
@@ -592,24 +617,48 @@ ReduceFn pick_reduce(const Plan &p) {
 
 // Everything after k_begin; k_begin itself is launched by the caller so that
 // a captured graph can take new Job parameters per call.
+// Launch with programmatic stream serialisation (the kernel may start while
+// its predecessor finishes; it waits in grid_dependency_wait).
+template <typename... Args>
+void launch_pdl(void (*kern)(Args...), unsigned grid, unsigned block, cudaStream_t st, bool pdl,
+                Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = pdl ? attr : nullptr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// Everything after k_begin; k_begin itself is launched by the caller so that
+// a captured graph can take new Job parameters per call.  The first
+// association follows k_begin (which writes the Job) without overlap; every
+// later kernel overlaps its predecessor's tail, except when profiling (event
+// records sit between the kernels).
 int launch_body(const Plan &p, cudaStream_t st, ProfSet *ps) {
   const unsigned agrid = blocks_for(p.n, kAssocThreads);
   const ReduceFn red = pick_reduce(p);
+  const bool pdl = ps == nullptr;
+  const Job *job = p.job_dev;
   for (int it = 0; it < p.iters; ++it) {
     if (p.n > 0) {
       Timed t(ps, kProfAssoc, st);
-      k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, it, 0);
+      launch_pdl(k_assoc, agrid, kAssocThreads, st, pdl && it > 0, job, it, 0);
     }
     Timed t(ps, kProfReduce, st);
-    red<<<p.nblocks, kReduceThreads, 0, st>>>(p.job_dev, it);
+    launch_pdl(red, p.nblocks, kReduceThreads, st, pdl && (p.n > 0 || it > 0), job, it);
   }
   if (p.n > 0) {
     Timed t(ps, kProfAssoc, st);
-    k_assoc<<<agrid, kAssocThreads, 0, st>>>(p.job_dev, p.iters, 1);
+    launch_pdl(k_assoc, agrid, kAssocThreads, st, pdl && p.iters > 0, job, p.iters, 1);
   }
   {
     Timed t(ps, kProfInfo, st);
-    k_info<<<p.nblocks, kReduceThreads, 0, st>>>(p.job_dev, p.iters);
+    launch_pdl(k_info, p.nblocks, kReduceThreads, st, pdl, job, p.iters);
   }
   return check_launch("stb_icp_estimate");
 }
