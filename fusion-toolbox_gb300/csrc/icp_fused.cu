@@ -89,8 +89,10 @@ constexpr size_t kSlot = 1024;
 
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-inline int reduce_blocks(int64_t pixels) {
-  const int64_t per_block = (int64_t)kReduceThreads * kPixelsPerThread;
+// Blocks of the reduction for `threads` threads of kPixelsPerThread pixels;
+// the workspace holds slots for the 256-thread count (the largest grid).
+inline int reduce_blocks(int64_t pixels, int threads = kReduceThreads) {
+  const int64_t per_block = (int64_t)threads * kPixelsPerThread;
   int64_t b = (pixels + per_block - 1) / per_block;
   if (b < 1) b = 1;
   if (b > kMaxReduceBlocks) b = kMaxReduceBlocks;
@@ -219,10 +221,9 @@ __device__ __forceinline__ void accumulate_se3(float *acc, const float *Jv, floa
 // of the block's threads with TwoSum, then the warp's lanes by shuffles),
 // its accumulators interleaved so that their dependent chains overlap.
 // Threads 0..kN-1 of the block end with the totals in out (shared).
-template <int kN>
-__device__ __forceinline__ void block_reduce(const float *acc, float (*red)[kReduceThreads],
-                                             float2 *out) {
-  constexpr int kW = kReduceThreads / 32;
+template <int kN, int kT>
+__device__ __forceinline__ void block_reduce(const float *acc, float (*red)[kT], float2 *out) {
+  constexpr int kW = kT / 32;
   constexpr int kPer = (kN + kW - 1) / kW;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -278,10 +279,10 @@ __device__ __forceinline__ bool publish_slot(const float2 *bsum, float2 *part, u
 // (kFoldLoads slots) is issued before its additions, so 300 slots cost two
 // L2 round trips.  The eight warp results are merged through shared memory.
 constexpr int kFoldLoads = 24;
-template <int kN>
+template <int kN, int kT>
 __device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, double *tot) {
-  __shared__ float2 wsum[kReduceThreads / 32][32];
-  constexpr int kW = kReduceThreads / 32;
+  __shared__ float2 wsum[kT / 32][32];
+  constexpr int kW = kT / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   CSum t = {0.f, 0.f};
   for (int b0 = warp; b0 < nblocks; b0 += kW * kFoldLoads) {
@@ -396,13 +397,16 @@ __device__ void gn_step_warp(const Job *J, const StateView &V, const double *tot
 // that do not depend on the correspondence are issued together.
 constexpr int kRP = kPixelsPerThread;
 
-template <typename FT, bool kGeom, bool kFeat, bool kHWC>
-__global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict__ J,
-                                                           int epoch) {
+// The transposed block sum of k_reduce lives in dynamic shared memory
+// (kAccs x kT floats: 60 KB at 512 threads).
+extern __shared__ __align__(16) float s_red[];
+
+template <typename FT, bool kGeom, bool kFeat, bool kHWC, int kT>
+__global__ void __launch_bounds__(kT) k_reduce(const Job *__restrict__ J, int epoch) {
   __shared__ Pose32 P;
   __shared__ StateView V;
   __shared__ int skip;
-  __shared__ float red[kAccs][kReduceThreads];
+  float(*red)[kT] = reinterpret_cast<float(*)[kT]>(s_red);
   __shared__ float2 bsum[kAccs];
   __shared__ int is_last;
   __shared__ double tot[kAccs];
@@ -430,14 +434,14 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
   const float *__restrict__ tp = J->tp;
   const float *__restrict__ tn = J->tn;
   const float wg1 = J->wg1, wg2 = J->wg2, wf1 = J->wf1, wf2 = J->wf2;
-  const int64_t per_block = (int64_t)kReduceThreads * kRP;
+  const int64_t per_block = (int64_t)kT * kRP;
   for (int64_t base = blockIdx.x * per_block; base < npix;
        base += (int64_t)gridDim.x * per_block) {
     unsigned long long key[kRP];
     float tq[kRP][3], tnm[kRP][3];
 #pragma unroll
     for (int k = 0; k < kRP; ++k) {
-      const int64_t pix = base + k * kReduceThreads + threadIdx.x;
+      const int64_t pix = base + k * kT + threadIdx.x;
       const int64_t pc = pix < npix ? pix : 0;
       key[k] = pix < npix ? keys[pix] : 0ull;
 #pragma unroll
@@ -485,9 +489,9 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce(const Job *__restrict
     }
   }
 
-  block_reduce<kAccs>(acc, red, bsum);
+  block_reduce<kAccs, kT>(acc, red, bsum);
   if (!publish_slot<kAccs>(bsum, J->part, &S->ticket, &is_last)) return;
-  grid_totals<kAccs>(J->part, gridDim.x, tot);
+  grid_totals<kAccs, kT>(J->part, gridDim.x, tot);
   if (threadIdx.x < 32) {
     if (threadIdx.x == 0) S->ticket = 0;
     gn_step_warp(J, V, tot, epoch);
@@ -525,9 +529,9 @@ __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__
       for (int b = a; b < 6; ++b)
         acc[upper_index(a, b)] += G0[a] * G0[b] + G1[a] * G1[b] + G2[a] * G2[b];
   }
-  block_reduce<kInfoAccs>(acc, red, bsum);
+  block_reduce<kInfoAccs, kReduceThreads>(acc, red, bsum);
   if (!publish_slot<kInfoAccs>(bsum, J->part, &S->ticket, &is_last)) return;
-  grid_totals<kInfoAccs>(J->part, gridDim.x, tot);
+  grid_totals<kInfoAccs, kReduceThreads>(J->part, gridDim.x, tot);
   double *R = J->result;
   for (int k = threadIdx.x; k < 36; k += blockDim.x) {
     const int r = k / 6, c = k % 6;
@@ -600,31 +604,64 @@ struct Plan {
 
 using ReduceFn = void (*)(const Job *, int);
 
-template <typename FT, bool kHWC>
-ReduceFn pick_feat_reduce(bool use_geom) {
-  return use_geom ? k_reduce<FT, true, true, kHWC> : k_reduce<FT, false, true, kHWC>;
+// The reduction kernel of a configuration with its block size and dynamic
+// shared memory: the geometric-only kernel runs 512 threads per block (one
+// block per SM at 640x480: half the block partials of 256, so the last
+// block's fold is one round of loads); the feature kernels, whose sampling
+// needs more registers, 256.
+struct ReduceLaunch {
+  ReduceFn fn;
+  int threads;
+  int smem;
+};
+
+template <typename FT, bool kGeom, bool kFeat, bool kHWC, int kT>
+ReduceLaunch reduce_launch() {
+  return ReduceLaunch{k_reduce<FT, kGeom, kFeat, kHWC, kT>, kT, (int)(sizeof(float) * kAccs * kT)};
 }
 
-ReduceFn pick_reduce(const Plan &p) {
-  if (!p.use_feat) return k_reduce<float, true, false, false>;
+// The 512-thread kernel needs more than the default 48 KB of dynamic shared
+// memory; allowed once per device, outside any stream capture.
+int prepare_reduce_kernels() {
+  static std::mutex m;
+  static unsigned long long done = 0;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("cudaGetDevice");
+  std::lock_guard<std::mutex> lock(m);
+  if (dev < 64 && (done >> dev) & 1ull) return STB_OK;
+  const ReduceLaunch r = reduce_launch<float, true, false, false, 512>();
+  if (cudaFuncSetAttribute(r.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, r.smem) !=
+      cudaSuccess)
+    return check_launch("cudaFuncSetAttribute");
+  if (dev < 64) done |= 1ull << dev;
+  return STB_OK;
+}
+
+template <typename FT, bool kHWC>
+ReduceLaunch feat_reduce(bool use_geom) {
+  return use_geom ? reduce_launch<FT, true, true, kHWC, 256>()
+                  : reduce_launch<FT, false, true, kHWC, 256>();
+}
+
+ReduceLaunch pick_reduce(const Plan &p) {
+  if (!p.use_feat) return reduce_launch<float, true, false, false, 512>();
   switch (p.dtype) {
-    case STB_F32: return pick_feat_reduce<float, false>(p.use_geom);
-    case STB_BF16: return pick_feat_reduce<__nv_bfloat16, false>(p.use_geom);
-    case STB_F32_HWC: return pick_feat_reduce<float, true>(p.use_geom);
-    default: return pick_feat_reduce<__nv_bfloat16, true>(p.use_geom);
+    case STB_F32: return feat_reduce<float, false>(p.use_geom);
+    case STB_BF16: return feat_reduce<__nv_bfloat16, false>(p.use_geom);
+    case STB_F32_HWC: return feat_reduce<float, true>(p.use_geom);
+    default: return feat_reduce<__nv_bfloat16, true>(p.use_geom);
   }
 }
 
-// Everything after k_begin; k_begin itself is launched by the caller so that
-// a captured graph can take new Job parameters per call.
 // Launch with programmatic stream serialisation (the kernel may start while
 // its predecessor finishes; it waits in grid_dependency_wait).
 template <typename... Args>
-void launch_pdl(void (*kern)(Args...), unsigned grid, unsigned block, cudaStream_t st, bool pdl,
-                Args... args) {
+void launch_pdl(void (*kern)(Args...), unsigned grid, unsigned block, size_t smem,
+                cudaStream_t st, bool pdl, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -641,24 +678,25 @@ void launch_pdl(void (*kern)(Args...), unsigned grid, unsigned block, cudaStream
 // records sit between the kernels).
 int launch_body(const Plan &p, cudaStream_t st, ProfSet *ps) {
   const unsigned agrid = blocks_for(p.n, kAssocThreads);
-  const ReduceFn red = pick_reduce(p);
+  const ReduceLaunch red = pick_reduce(p);
+  const unsigned rgrid = reduce_blocks((int64_t)p.H * p.W, red.threads);
   const bool pdl = ps == nullptr;
   const Job *job = p.job_dev;
   for (int it = 0; it < p.iters; ++it) {
     if (p.n > 0) {
       Timed t(ps, kProfAssoc, st);
-      launch_pdl(k_assoc, agrid, kAssocThreads, st, pdl && it > 0, job, it, 0);
+      launch_pdl(k_assoc, agrid, kAssocThreads, 0, st, pdl && it > 0, job, it, 0);
     }
     Timed t(ps, kProfReduce, st);
-    launch_pdl(red, p.nblocks, kReduceThreads, st, pdl && (p.n > 0 || it > 0), job, it);
+    launch_pdl(red.fn, rgrid, red.threads, red.smem, st, pdl && (p.n > 0 || it > 0), job, it);
   }
   if (p.n > 0) {
     Timed t(ps, kProfAssoc, st);
-    launch_pdl(k_assoc, agrid, kAssocThreads, st, pdl && p.iters > 0, job, p.iters, 1);
+    launch_pdl(k_assoc, agrid, kAssocThreads, 0, st, pdl && p.iters > 0, job, p.iters, 1);
   }
   {
     Timed t(ps, kProfInfo, st);
-    launch_pdl(k_info, p.nblocks, kReduceThreads, st, pdl, job, p.iters);
+    launch_pdl(k_info, p.nblocks, kReduceThreads, 0, st, pdl, job, p.iters);
   }
   return check_launch("stb_icp_estimate");
 }
@@ -808,6 +846,7 @@ extern "C" int stb_icp_estimate(
   STB_TRY(check_device_ptr(workspace, "workspace"));
   STB_TRY(check_device_ptr(result, "result"));
   STB_TRY(check_device_ptr(history, "history", true));
+  STB_TRY(prepare_reduce_kernels());
 
   char *ws = static_cast<char *>(workspace);
   Plan p;
@@ -1013,6 +1052,7 @@ extern "C" int stb_icp_estimate_static(
   STB_TRY(check_device_ptr(init_transform, "transform", true));
   STB_TRY(check_device_ptr(result, "result"));
   STB_TRY(check_device_ptr(history, "history", true));
+  STB_TRY(prepare_reduce_kernels());
   void *workspace = nullptr;
   STB_TRY(static_workspace(&workspace));
 
