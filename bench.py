@@ -83,6 +83,18 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, world, device=None):
+    """The slowest rank's value (the timed region is bracketed by a barrier;
+    the job's time is the maximum over ranks)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peak():
     path = ROOT / "MEASURED_PEAKS.json"
     if path.exists():
@@ -609,11 +621,7 @@ def main():
     barrier()
     clocks.mark("t1")
     clock_info = clocks.stop()
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms), world, device)
     value = world * args.steps * ITERS / (total_ms / 1e3)
 
     # per-kernel times: the same steps with CUDA events around every kernel
@@ -656,12 +664,8 @@ def main():
     for _ in range(3):
         e2e_step()
     barrier()
-    e2e_ms = sum(timed(min(args.steps, 500), e2e_step))
     e2e_steps = min(args.steps, 500)
-    if world > 1:
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(sum(timed(e2e_steps, e2e_step)), world, device)
     e2e_value = world * e2e_steps * ITERS / (e2e_ms / 1e3)
 
     base = None
