@@ -185,15 +185,18 @@ __global__ void __launch_bounds__(kAssocThreads) k_assoc(const Job *__restrict__
   int ui, vi;
   if (!round_in(u, W, ui) || !round_in(v, H, vi)) return;
   const int64_t pix = (int64_t)vi * W + ui;
-  if (!J->tm[pix]) return;
+  // the target pixel's mask, point and normal in one round trip (the point
+  // and normal of a masked-out pixel are read and discarded)
   const float *__restrict__ tp = J->tp;
-  const float dx = fsub(tp[3 * pix], Tp.x), dy = fsub(tp[3 * pix + 1], Tp.y),
-              dz = fsub(tp[3 * pix + 2], Tp.z);
+  const float *__restrict__ tn = J->tn;
+  const bool valid = J->tm[pix];
+  const float qx = tp[3 * pix], qy = tp[3 * pix + 1], qz = tp[3 * pix + 2];
+  const float nx = tn[3 * pix], ny = tn[3 * pix + 1], nz = tn[3 * pix + 2];
+  if (!valid) return;
+  const float dx = fsub(qx, Tp.x), dy = fsub(qy, Tp.y), dz = fsub(qz, Tp.z);
   const float sq = dot3(dx, dy, dz, dx, dy, dz);
   if (sq > J->thr2) return;
-  const float *__restrict__ tn = J->tn;
   const float3 Tn = transform_normal(P.nm, n0, n1, n2);
-  const float nx = tn[3 * pix], ny = tn[3 * pix + 1], nz = tn[3 * pix + 2];
   const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, nx, ny, nz),
                        fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
                             __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz))));
