@@ -18,11 +18,26 @@ int fail(int code, const char *fmt, ...) {
 
 void clear_error() { g_message[0] = '\0'; }
 
+// Recently validated device pointers of this thread (a tracker passes the
+// same buffers every frame): a hit skips the driver query.  Only pointers
+// that passed as device memory of the current device are remembered, so a
+// host pointer is always queried and refused.
+struct PtrCacheEntry {
+  const void *p;
+  int dev;
+};
+static thread_local PtrCacheEntry g_ptr_cache[32];
+static thread_local int g_ptr_next = 0;
+
 int check_device_ptr(const void *p, const char *name, bool allow_null) {
   if (p == nullptr) {
     if (allow_null) return STB_OK;
     return fail(STB_EINVAL, "Check failed: %s: null pointer", name);
   }
+  int dev = -1;
+  cudaGetDevice(&dev);
+  for (const PtrCacheEntry &e : g_ptr_cache)
+    if (e.p == p && e.dev == dev) return STB_OK;
   cudaPointerAttributes attr;
   const cudaError_t err = cudaPointerGetAttributes(&attr, p);
   if (err != cudaSuccess) {
@@ -32,12 +47,12 @@ int check_device_ptr(const void *p, const char *name, bool allow_null) {
   }
   if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
     return fail(STB_EDEVICE, "Check failed: %s: Expected a gpu tensor", name);
-  int dev = -1;
-  cudaGetDevice(&dev);
   if (attr.device != dev)
     return fail(STB_EDEVICE,
                 "Check failed: %s: Expected a tensor on cuda:%d, got cuda:%d", name,
                 dev, attr.device);
+  g_ptr_cache[g_ptr_next] = PtrCacheEntry{p, dev};
+  g_ptr_next = (g_ptr_next + 1) % 32;
   return STB_OK;
 }
 
