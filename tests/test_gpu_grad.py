@@ -214,3 +214,73 @@ def test_loss_is_zero_without_correspondences(cuda, batch):
     loss, gtw, gz = _run(cuda, [d, pairs[1]], poses[:2])
     assert loss[0] == 0.0 and np.all(gtw[0] == 0.0) and np.all(gz[0] == 0.0)
     assert loss[1] > 0.0
+
+
+def test_full_size_32_pairs_640x480(cuda):
+    """The loss at its full size (32 pairs of 640x480, poses after 5 Gauss-
+    Newton iterations): for every pair the twist gradient equals -2 J^T r
+    from the reference-layout partials of ICPJacobian (same correspondences,
+    1e-5 of sum 2|J||r|), the depth gradient vanishes off the
+    correspondences, and one pair's twist gradient matches FP64 central
+    differences."""
+    from slamtb_gb300 import synthetic
+    from slamtb_gb300._cslamtb import CorrespondenceMap, ICPJacobian
+    from slamtb_gb300.frame import Frame, FrameInfo, FramePointCloud, KCamera
+    from slamtb_gb300.registration import BatchRegistration, ICPOdometry, point_to_plane_loss
+    B = 32
+    src, tgt, kc = [], [], None
+    for k in range(B):
+        p = synthetic.make_pair(200 + k, width=640, height=480, device=cuda)
+        kc = KCamera(p["kcam"])
+        src.append(FramePointCloud.from_frame(Frame(FrameInfo(kc), p["source_depth"]), cuda))
+        tgt.append(FramePointCloud.from_frame(Frame(FrameInfo(kc), p["target_depth"]), cuda))
+    br = BatchRegistration([(1.0, ICPOdometry(5, geom_weight=1.0, feat_weight=0.0,
+                                              distance_threshold=DIST,
+                                              normals_angle_thresh=ANGLE))])
+    res = br.estimate_pyramids([[s] for s in src], [[t] for t in tgt])
+    poses = torch.stack([r.transform.double().float().double() for r in res]).to(cuda)
+    st = lambda f: torch.stack([f(k) for k in range(B)]).contiguous()  # noqa: E731
+    depth = st(lambda k: src[k].points[..., 2]).requires_grad_(True)
+    twist = torch.zeros(B, 6, dtype=torch.float64, device=cuda, requires_grad=True)
+    loss = point_to_plane_loss(twist, depth, st(lambda k: src[k].normals),
+                               st(lambda k: src[k].mask), st(lambda k: tgt[k].points),
+                               st(lambda k: tgt[k].normals), st(lambda k: tgt[k].mask),
+                               kc.params(), poses, DIST, ANGLE)
+    loss.sum().backward()
+    gtw = twist.grad.cpu().numpy()
+    assert torch.isfinite(loss).all() and bool((loss > 0).all())
+    h, w = 480, 640
+    for k in range(B):
+        s, t = src[k], tgt[k]
+        cmap = torch.full((h, w), io.CORRESP_EMPTY, dtype=torch.int64, device=cuda)
+        rt = poses[k].float()
+        CorrespondenceMap.compute_correspondence_map(
+            s.points.view(-1, 3), s.normals.view(-1, 3), s.mask.view(-1), rt, t.points,
+            t.normals, t.mask, torch.as_tensor(kc.matrix, device=cuda), cmap, DIST, ANGLE)
+        JtJ = torch.zeros(h * w, 6, 6, device=cuda)
+        Jr = torch.zeros(h * w, 6, device=cuda)
+        r2 = torch.zeros(h * w, device=cuda)
+        ICPJacobian.estimate_geometric(s.points.view(-1, 3), s.mask.view(-1), rt, t.points,
+                                       t.normals, torch.as_tensor(kc.matrix, device=cuda), cmap,
+                                       JtJ, Jr, r2)
+        ref = -2.0 * Jr.double().sum(0).cpu().numpy()
+        Jn = torch.linalg.norm(JtJ.double().diagonal(dim1=1, dim2=2).sqrt(), dim=1)
+        scale = float(2.0 * (Jn * r2.double().sqrt()).sum())
+        assert np.abs(gtw[k] - ref).max() <= 1e-5 * scale, k
+        matched = (cmap.cpu().numpy() >> 32).reshape(-1)
+        matched = matched[matched != (io.CORRESP_EMPTY >> 32)]
+        gz = depth.grad[k].reshape(-1).cpu().numpy()
+        off = np.ones(h * w, dtype=bool)
+        off[matched] = False
+        assert np.all(gz[off] == 0.0), k
+    # FP64 central differences of the twist gradient, pair 0
+    d0 = dict(src=dict(points=src[0].points.cpu().numpy(), normals=src[0].normals.cpu().numpy(),
+                       mask=src[0].mask.cpu().numpy()),
+              tgt=dict(points=tgt[0].points.cpu().numpy(), normals=tgt[0].normals.cpu().numpy(),
+                       mask=tgt[0].mask.cpu().numpy()),
+              kcam=kc.matrix.numpy())
+    T0 = poses[0].cpu().numpy()
+    _, m = _oracle(d0, T0)
+    fd = io.loss_twist_grad_fd(T0, np.zeros(6), d0["src"]["points"], m, h=1e-6)
+    _, sc = io.loss_twist_grad64(T0, d0["src"]["points"], m)
+    assert np.abs(gtw[0] - fd).max() <= 1e-5 * sc
