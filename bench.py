@@ -25,7 +25,9 @@ Secondary workloads (rank 0, N = 1, reported under "secondary"; skip with
       level);
   feature_1080p_16ch_bf16    16 pairs 1920x1080, 16 BF16 feature channels,
       4 levels [10, 8, 5, 3], weights geometric 10 / feature 1 (the
-      reference preset), BatchRegistration vs the plain path.
+      reference preset), BatchRegistration vs the plain path;
+  bilateral_depth_filter     the depth bilateral filter on uint16 depth,
+      640x480 and 1920x1080, widths 6 and 13.
 
 Under torchrun each rank registers its own pair (seeded by rank), no
 collective touches the data path (weak scaling); a barrier and a max over
@@ -495,6 +497,51 @@ def secondary_feature_1080p(device, seed, B=16):
                            [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, device, 5, 1, feat_bytes=32)
 
 
+def secondary_bilateral(device, seed, reps=200):
+    """The depth bilateral filter on 16-bit millimetre depth images: per
+    launch time from CUDA events over ``reps`` back-to-back launches (the
+    input stays in L2: the kernel is bound by one exponential per tap, not
+    by its 5 bytes per pixel), and the float32 oracle on one 640x480 image
+    as the CPU side."""
+    import numpy as np
+    import torch
+    from slamtb_gb300 import synthetic
+    from slamtb_gb300.processing import BilateralDepthFilter
+    out = {"workload": "bilateral depth filter, uint16 depth in mm (ElasticFusion sigmas "
+                       "29.99 / 4.5)", "cases": {}}
+    host = {}
+    for w, h in ((640, 480), (1920, 1080)):
+        z = synthetic.make_pair(seed + 3000, width=w, height=h)["source_depth"]
+        host[(w, h)] = (z * 1000).astype(np.uint16)
+        d = torch.from_numpy(host[(w, h)].astype(np.int32)).to(device).to(torch.uint16)
+        for width in (6, 13):
+            filt = BilateralDepthFilter(filter_width=width)
+            for _ in range(5):
+                filt(d)
+            st = torch.cuda.current_stream(device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(device)
+            e0.record(st)
+            for _ in range(reps):
+                filt(d)
+            e1.record(st)
+            torch.cuda.synchronize(device)
+            s = e0.elapsed_time(e1) * 1e-3 / reps
+            taps = (2 * (width // 2) + 1) ** 2
+            out["cases"][f"{w}x{h}_width{width}"] = {
+                "us_per_image": s * 1e6, "mpix_per_s": w * h / s / 1e6,
+                "gtaps_per_s": w * h * taps / s / 1e9, "taps_per_pixel": taps}
+    from oracle import frame_prep as fp
+    z = host[(640, 480)].astype(np.int32)
+    t = time.perf_counter()
+    fp.bilateral_depth_filter(z, z > 0, 6)
+    el = time.perf_counter() - t
+    out["cpu_baseline"] = {"us_per_image": el * 1e6, "mpix_per_s": 640 * 480 / el / 1e6,
+                           "cores": 1, "kind": "port",
+                           "sample": "one 640x480 image, width 6, numpy float32 oracle"}
+    return out
+
+
 def profile_case(args, device):
     """A small case of one secondary workload, --steps runs after --warmup,
     for profiler captures (prints one JSON line; not a bench result)."""
@@ -551,7 +598,8 @@ def run_secondary(device, seed):
     for name, fn in (("multiscale_hybrid_640x480", secondary_multiscale),
                      ("loss_grad_32x640x480", secondary_loss),
                      ("batch_uneven_256", secondary_batch_uneven),
-                     ("feature_1080p_16ch_bf16", secondary_feature_1080p)):
+                     ("feature_1080p_16ch_bf16", secondary_feature_1080p),
+                     ("bilateral_depth_filter", secondary_bilateral)):
         t = time.perf_counter()
         try:
             out[name] = fn(device, seed)

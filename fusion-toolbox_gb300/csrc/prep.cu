@@ -267,6 +267,79 @@ __global__ void k_interleave(const T *__restrict__ src, T *__restrict__ dst, int
   }
 }
 
+// BilateralDepthFilterKernel (src/bilateral_depth_filter.cu:15-72).  A block
+// computes a kBX x kBLR tile of outputs from a shared-memory copy of the
+// scaled depth and the mask over the tile plus the filter's halo (read once
+// from HBM, coalesced); every output then walks its (2 hw + 1)^2 taps in
+// shared memory, rows outer and columns inner as the reference, with its
+// float32 operations uncontracted.  Taps outside the image read as masked.
+constexpr int kBLR = 16;           // output rows per block (2 per thread)
+constexpr int kMaxHalfWidth = 15;  // filter_width <= 31
+constexpr int kBLW = kBX + 2 * kMaxHalfWidth, kBLH = kBLR + 2 * kMaxHalfWidth;
+
+template <typename T>
+__device__ __forceinline__ float scaled_depth(T v, float scale) {
+  return fmul((float)v, scale);
+}
+template <>
+__device__ __forceinline__ float scaled_depth<double>(double v, float scale) {
+  return __double2float_rn(__dmul_rn(v, (double)scale));
+}
+template <typename T>
+__device__ __forceinline__ T from_float(float x) {
+  return (T)x;  // integers truncate toward zero, as the reference's scalar_t(...)
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBX * kBY) k_bilateral(const T *__restrict__ depth,
+                                                         const uint8_t *__restrict__ mask,
+                                                         T *__restrict__ out, int H, int W,
+                                                         int hw, float inv_sc, float inv_ss,
+                                                         float scale, float inv_scale) {
+  __shared__ float zs[kBLH][kBLW];
+  __shared__ uint8_t ms[kBLH][kBLW];
+  const int c0 = blockIdx.x * kBX - hw, r0 = blockIdx.y * kBLR - hw;
+  const int tw = kBX + 2 * hw, th = kBLR + 2 * hw;
+  for (int k = threadIdx.y * kBX + threadIdx.x; k < tw * th; k += kBX * kBY) {
+    const int ty = k / tw, tx = k % tw;
+    const int r = r0 + ty, c = c0 + tx;
+    const bool in = r >= 0 && r < H && c >= 0 && c < W;
+    const int64_t i = in ? (int64_t)r * W + c : 0;
+    ms[ty][tx] = in && mask[i];
+    zs[ty][tx] = in ? scaled_depth(depth[i], scale) : 0.f;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int half = 0; half < kBLR / kBY; ++half) {
+    const int ly = threadIdx.y + half * kBY, lx = threadIdx.x;
+    const int row = blockIdx.y * kBLR + ly, col = blockIdx.x * kBX + lx;
+    if (row >= H || col >= W) continue;
+    const int64_t o = (int64_t)row * W + col;
+    if (!ms[ly + hw][lx + hw]) {
+      out[o] = from_float<T>(0.f);
+      continue;
+    }
+    const float z = zs[ly + hw][lx + hw];
+    float color_sum = 0.f, weight_sum = 0.f;
+    for (int y = -hw; y <= hw; ++y) {
+      for (int x = -hw; x <= hw; ++x) {
+        if (!ms[ly + hw + y][lx + hw + x]) continue;
+        const float cz = zs[ly + hw + y][lx + hw + x];
+        const float dx = (float)(-x), dy = (float)(-y);
+        const float space_sqr = fadd(fmul(dx, dx), fmul(dy, dy));
+        const float dcolor = fsub(z, cz);
+        const float color_sqr = fmul(dcolor, dcolor);
+        const float weight =
+            expf(fmul(-0.5f, fadd(fmul(space_sqr, inv_ss), fmul(color_sqr, inv_sc))));
+        color_sum = fadd(color_sum, fmul(cz, weight));
+        weight_sum = fadd(weight_sum, weight);
+      }
+    }
+    out[o] = from_float<T>(weight_sum > 0.f ? fmul(fdiv(color_sum, weight_sum), inv_scale)
+                                            : 0.f);
+  }
+}
+
 }  // namespace
 }  // namespace stb
 
@@ -412,4 +485,43 @@ extern "C" int stb_feature_interleave(const void *src, void *dst, int32_t channe
   else
     return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
   return check_launch("stb_feature_interleave");
+}
+
+extern "C" int stb_bilateral_depth_filter(const void *depth, const uint8_t *mask, void *out,
+                                          int32_t height, int32_t width, int32_t dtype,
+                                          int32_t filter_width, float sigma_color,
+                                          float sigma_space, float depth_scale, void *stream) {
+  clear_error();
+  STB_TRY(check_hw(height, width));
+  if (filter_width < 0 || filter_width / 2 > kMaxHalfWidth)
+    return fail(STB_EINVAL, "Check failed: filter_width must be in [0, %d], got %d",
+                2 * kMaxHalfWidth + 1, filter_width);
+  STB_TRY(check_device_ptr(depth, "depth"));
+  STB_TRY(check_device_ptr(mask, "mask"));
+  STB_TRY(check_device_ptr(out, "out"));
+  if (depth == out) return fail(STB_EINVAL, "Check failed: the filter cannot run in place");
+  const int hw = filter_width / 2;
+  // as the reference: 1.0 / (sigma * sigma) with the product in float and
+  // the quotient in double, both kept as float; 1.0 / depth_scale likewise
+  const float inv_sc = (float)(1.0 / (double)(sigma_color * sigma_color));
+  const float inv_ss = (float)(1.0 / (double)(sigma_space * sigma_space));
+  const float inv_scale = (float)(1.0 / (double)depth_scale);
+  const dim3 grid((width + kBX - 1) / kBX, (height + kBLR - 1) / kBLR), block(kBX, kBY);
+  const cudaStream_t st = as_stream(stream);
+#define STB_BILATERAL(T)                                                                  \
+  k_bilateral<T><<<grid, block, 0, st>>>(static_cast<const T *>(depth), mask,           \
+                                         static_cast<T *>(out), height, width, hw, inv_sc, \
+                                         inv_ss, depth_scale, inv_scale)
+  switch (dtype) {
+    case STB_F32: STB_BILATERAL(float); break;
+    case STB_F64: STB_BILATERAL(double); break;
+    case STB_U8: STB_BILATERAL(uint8_t); break;
+    case STB_I16: STB_BILATERAL(int16_t); break;
+    case STB_U16: STB_BILATERAL(uint16_t); break;
+    case STB_I32: STB_BILATERAL(int32_t); break;
+    case STB_I64: STB_BILATERAL(int64_t); break;
+    default: return fail(STB_EDTYPE, "Check failed: unsupported depth dtype %d", dtype);
+  }
+#undef STB_BILATERAL
+  return check_launch("stb_bilateral_depth_filter");
 }

@@ -16,6 +16,7 @@ STB_F32 = 0
 STB_BF16 = 1
 STB_F32_HWC = 2   # texel-major feature layout [count][channels]
 STB_BF16_HWC = 3
+STB_F64, STB_U8, STB_I16, STB_U16, STB_I32, STB_I64 = 4, 5, 6, 7, 8, 9
 
 # result block layout (doubles), see the header
 RES_TRANSFORM, RES_JTJ, RES_INFO = 0, 16, 52
@@ -53,6 +54,8 @@ _SIGNATURES = {
     "stb_icp_estimate_batch": (ctypes.c_int, [
         _vp, _i32, _i32, _vp, _i32, _i32, _i32, _vp, _i64, _vp, _sz, _vp, _vp, _i32, _vp]),
     "stb_feature_interleave": (ctypes.c_int, [_vp, _vp, _i32, _i64, _i32, _vp]),
+    "stb_bilateral_depth_filter": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _f32,
+                                                  _f32, _f32, _vp]),
     "stb_se3_exp_compose": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp]),
     "stb_se3_twist_grad": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp]),
     "stb_icp_loss_workspace_bytes": (_sz, [_i32, _i32, _i32]),

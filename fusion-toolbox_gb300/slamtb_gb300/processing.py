@@ -114,3 +114,62 @@ def interleave_features(feats):
     out = torch.empty(n, c, dtype=f.dtype, device=dev)
     _run(dev, N.lib().stb_feature_interleave, N.ptr(f), N.ptr(out), c, n, N.feat_dtype_code(f))
     return out
+
+
+_DEPTH_DTYPES = {torch.float32: N.STB_F32, torch.float64: N.STB_F64, torch.uint8: N.STB_U8,
+                 torch.int16: N.STB_I16, torch.int32: N.STB_I32, torch.int64: N.STB_I64}
+if hasattr(torch, "uint16"):
+    _DEPTH_DTYPES[torch.uint16] = N.STB_U16
+
+
+def bilateral_depth_filter(depth, mask=None, out_tensor=None, filter_width=6,
+                           sigma_color=29.9999880000072, sigma_space=4.50000000225,
+                           depth_scale=1.0):
+    """Bilateral filter of a depth image (``slamtb/processing.py:17-55``,
+    ``src/bilateral_depth_filter.cu``; defaults are ElasticFusion's).
+
+    Args:
+        depth: (H, W) depth image on a CUDA device, float32 / float64 or an
+            integer type (the result has the same dtype; integers truncate).
+        mask: (H, W) validity, default ``depth > 0``.
+        out_tensor: optional output, reused when its size matches.
+        filter_width (int): window size (at most 31).
+        sigma_color, sigma_space (float): range and spatial sigmas.
+        depth_scale (float): factor applied to the depth before filtering.
+    """
+    dev = _dev(depth)
+    d = depth.contiguous()
+    if d.dtype not in _DEPTH_DTYPES:
+        raise RuntimeError(f"Check failed: unsupported depth dtype {d.dtype}")
+    if mask is None:  # depth > 0 (unsigned 16-bit tensors compare through int16 bits)
+        m = (d.view(torch.int16) != 0) if d.dtype == getattr(torch, "uint16", None) else d > 0
+    else:
+        m = mask
+    m = m.to(device=dev, dtype=torch.bool).contiguous()
+    h, w = d.shape
+    if out_tensor is None or tuple(out_tensor.shape) != (h, w) or out_tensor.dtype != d.dtype \
+            or out_tensor.device != dev:
+        out_tensor = torch.empty(h, w, dtype=d.dtype, device=dev)
+    _run(dev, N.lib().stb_bilateral_depth_filter, N.ptr(d), N.ptr(m), N.ptr(out_tensor), h, w,
+         _DEPTH_DTYPES[d.dtype], int(filter_width), float(sigma_color), float(sigma_space),
+         float(depth_scale))
+    return out_tensor
+
+
+class BilateralDepthFilter:
+    """``slamtb/processing.py:58-76``: the filter with fixed parameters and
+    a reused output tensor."""
+
+    def __init__(self, filter_width=6, sigma_color=29.9999880000072,
+                 sigma_space=4.50000000225, depth_scale=1.0):
+        self.filter_width = filter_width
+        self.sigma_color = sigma_color
+        self.sigma_space = sigma_space
+        self.depth_scale = depth_scale
+        self._out_tensor = None
+
+    def __call__(self, depth, mask):
+        self._out_tensor = bilateral_depth_filter(
+            depth, mask, self._out_tensor, self.filter_width, self.sigma_color,
+            self.sigma_space, self.depth_scale)
+        return self._out_tensor

@@ -62,6 +62,13 @@ extern "C" {
  * reference's layout ([channels][count]) is STB_F32 / STB_BF16. */
 #define STB_F32_HWC 2
 #define STB_BF16_HWC 3
+/* Further element types of depth images (stb_bilateral_depth_filter). */
+#define STB_F64 4
+#define STB_U8 5
+#define STB_I16 6
+#define STB_U16 7
+#define STB_I32 8
+#define STB_I64 9
 
 /* ---- per-registration status bits (result block, STB_RES_STATUS) ------- */
 #define STB_ST_NOT_PD 1u     /* 6x6 J^T J was not positive definite: stopped */
@@ -305,6 +312,21 @@ STB_API int stb_icp_estimate_batch(
     int32_t channel_mode, const double *init_transforms,
     int64_t total_target_pixels, void *workspace, size_t workspace_bytes,
     double *results, double *history, int32_t tile_config, void *stream);
+
+/*
+ * Processing::BilateralDepthFilter (src/bilateral_depth_filter.cu:15-110):
+ * out[r][c] = 0 where mask[r][c] is 0, else the average of the masked
+ * neighbours' depth within filter_width / 2 pixels, weighted by
+ * exp(-0.5 (d_space^2 / sigma_space^2 + d_depth^2 / sigma_color^2)),
+ * computed in float32 on depth * depth_scale and divided back.  depth and
+ * out: [height][width] of element type dtype (STB_F32, STB_F64, STB_U8,
+ * STB_I16, STB_U16, STB_I32 or STB_I64; integers truncate), mask:
+ * uint8 [height][width].  filter_width <= 31.
+ */
+STB_API int stb_bilateral_depth_filter(const void *depth, const uint8_t *mask, void *out,
+                                       int32_t height, int32_t width, int32_t dtype,
+                                       int32_t filter_width, float sigma_color,
+                                       float sigma_space, float depth_scale, void *stream);
 
 /*
  * dst[k * channels + c] = src[c * count + k]: feature maps from the

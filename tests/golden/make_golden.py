@@ -12,6 +12,11 @@ by the reference's tests (frames 0 and 3: the synthetic pair of
 them, with their intrinsics, depth scale and ground-truth camera-to-world
 poses from ``frames.json``, as ``sample2.npz`` (depth stored as row-wise
 first differences; ``load_sample2`` undoes that).
+
+It also stores ``slamtb/_test/assets/frame_depth.png``, the depth frame of
+the reference's bilateral-filter and erosion tests
+(``slamtb/_test/test_processing.py:24-60``), as ``frame_depth.npz`` (same
+encoding; ``load_frame_depth``).
 """
 import json
 import pathlib
@@ -40,6 +45,12 @@ def load_sample2(path=HERE / "sample2.npz"):
     return out
 
 
+def load_frame_depth(path=HERE / "frame_depth.npz"):
+    """The uint16 (480, 640) depth frame of the reference's processing tests."""
+    z = np.load(path)
+    return np.cumsum(z["depth_dx"].astype(np.int32), axis=1).astype(np.uint16)
+
+
 def main(reference_root):
     root = pathlib.Path(reference_root) / "test-data" / "rgbd" / "sample2"
     meta = json.load(open(root / "frames.json"))["root"]
@@ -58,6 +69,13 @@ def main(reference_root):
         out[f"depth_bias_{i}"] = np.float32(info["depth_bias"])
     np.savez_compressed(HERE / "sample2.npz", **out)
     print("wrote", HERE / "sample2.npz")
+    depth = read_png(pathlib.Path(reference_root) / "slamtb" / "_test" / "assets" /
+                     "frame_depth.png")
+    assert depth.dtype == np.uint16
+    np.savez_compressed(HERE / "frame_depth.npz",
+                        depth_dx=np.diff(depth.astype(np.int32), axis=1,
+                                         prepend=0).astype(np.int16))
+    print("wrote", HERE / "frame_depth.npz")
 
 
 if __name__ == "__main__":

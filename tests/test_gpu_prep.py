@@ -96,3 +96,65 @@ def test_feature_pyramid(cuda, dtype):
         np.testing.assert_allclose(down, fp.downsample_features(f32, 0.5), atol=8e-3)
     pyr = P.feature_pyramid(ft, [1.0, 0.5, 0.5])
     assert [tuple(p.shape) for p in pyr] == [(3, 12, 16), (3, 24, 32), (3, 48, 64)]
+
+
+def _frame_depth():
+    import pathlib
+    import sys
+    sys.path.insert(0, str(pathlib.Path(__file__).resolve().parent / "golden"))
+    from make_golden import load_frame_depth
+    return load_frame_depth()
+
+
+def test_bilateral_reference_test_call(cuda):
+    """The reference's own bilateral test (slamtb/_test/test_processing.py:24-43):
+    its depth frame as int32, its positional arguments (filter width 13,
+    sigma_color 4.5, sigma_space 29.99), against the float32 restatement:
+    within 1 depth unit everywhere (that test's tolerance: expf may differ
+    by an ulp between implementations), equal almost everywhere."""
+    from slamtb_gb300.processing import bilateral_depth_filter
+    depth = _frame_depth().astype(np.int32)
+    mask = depth > 0
+    ref = fp.bilateral_depth_filter(depth, mask, 13, 4.50000000225, 29.9999880000072)
+    out = bilateral_depth_filter(torch.from_numpy(depth).to(cuda),
+                                 torch.from_numpy(mask).to(cuda), None, 13, 4.50000000225,
+                                 29.9999880000072).cpu().numpy()
+    assert out.dtype == np.int32
+    diff = np.abs(out.astype(np.int64) - ref)
+    assert diff.max() <= 1
+    assert (diff == 0).mean() > 0.999
+    assert np.all(out[~mask] == 0)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.int16, np.uint16, np.int64])
+def test_bilateral_dtypes_and_scale(cuda, dtype):
+    from slamtb_gb300.processing import bilateral_depth_filter
+    depth = _frame_depth()[100:260, 200:420]
+    if dtype in (np.float32, np.float64):
+        d, scale = (depth.astype(np.float64) * 0.001).astype(dtype), 1000.0
+    else:
+        d, scale = depth.astype(dtype), 0.001
+    ref = fp.bilateral_depth_filter(d, d > 0, 6, depth_scale=scale)
+    td = torch.from_numpy(d.astype(np.int32)).to(cuda).to(torch.uint16) \
+        if dtype == np.uint16 else torch.from_numpy(d).to(cuda)
+    out = bilateral_depth_filter(td, None, depth_scale=scale)
+    if dtype == np.uint16:
+        out = out.to(torch.int32)
+    out = out.cpu().numpy()
+    if np.issubdtype(dtype, np.integer):
+        assert np.abs(out.astype(np.int64) - ref.astype(np.int64)).max() <= 1
+    else:
+        np.testing.assert_allclose(out, ref, rtol=2e-6, atol=0)
+
+
+def test_bilateral_filter_class_reuses_output(cuda):
+    from slamtb_gb300.processing import BilateralDepthFilter
+    depth = torch.from_numpy(_frame_depth().astype(np.float32) * 0.001).to(cuda)
+    f = BilateralDepthFilter(filter_width=6, depth_scale=1000.0)
+    a = f(depth, depth > 0)
+    ptr = a.data_ptr()
+    b = f(depth * 1.0, depth > 0)
+    assert b.data_ptr() == ptr
+    ref = fp.bilateral_depth_filter(depth.cpu().numpy(), depth.cpu().numpy() > 0, 6,
+                                    depth_scale=1000.0)
+    np.testing.assert_allclose(b.cpu().numpy(), ref, rtol=2e-6, atol=0)

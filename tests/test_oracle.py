@@ -263,3 +263,37 @@ def test_registration_verifier_rules():
     assert not v(res(1e-3, 1e6, 0.9))     # residual above 1e-4
     assert not v(res(1e-5, 1e2, 0.9))     # covariance eigenvalue 1e-2 above 1e-4
     assert not v(res(1e-5, 1e6, 0.1))     # match ratio below 0.6
+
+
+def test_bilateral_oracle_matches_literal_loop():
+    """The vectorised restatement of BilateralDepthFilterKernel
+    (src/bilateral_depth_filter.cu:37-71) against a literal per-pixel loop
+    of the same float32 operations, on a small image with masked pixels."""
+    F = np.float32
+    rng = np.random.default_rng(0)
+    d = (rng.random((9, 11)) * 3000).astype(np.int32)
+    d[2, 3] = 0
+    d[5, :] = 0
+    m = d > 0
+    out = fp.bilateral_depth_filter(d, m, 5, 4.5, 29.99, 1.0)
+    hw = 2
+    isc = F(1.0 / float(F(F(4.5) * F(4.5))))
+    iss = F(1.0 / float(F(F(29.99) * F(29.99))))
+    ref = np.zeros_like(d)
+    for r in range(9):
+        for c in range(11):
+            if not m[r, c]:
+                continue
+            z, cs, ws = F(d[r, c]), F(0), F(0)
+            for y in range(-hw, hw + 1):
+                for x in range(-hw, hw + 1):
+                    kr, kc = r + y, c + x
+                    if not (0 <= kr < 9 and 0 <= kc < 11) or not m[kr, kc]:
+                        continue
+                    cz = F(d[kr, kc])
+                    sp = F(F(F(-x) * F(-x)) + F(F(-y) * F(-y)))
+                    dc = F(z - cz)
+                    wt = F(np.exp(F(F(-0.5) * F(F(sp * iss) + F(F(dc * dc) * isc)))))
+                    cs, ws = F(cs + F(cz * wt)), F(ws + wt)
+            ref[r, c] = int(np.trunc(F(cs / ws)))
+    np.testing.assert_array_equal(out, ref)
