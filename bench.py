@@ -514,16 +514,17 @@ def secondary_bilateral(device, seed, reps=200):
         z = synthetic.make_pair(seed + 3000, width=w, height=h)["source_depth"]
         host[(w, h)] = (z * 1000).astype(np.uint16)
         d = torch.from_numpy(host[(w, h)].astype(np.int32)).to(device).to(torch.uint16)
+        m = d.view(torch.int16) != 0
         for width in (6, 13):
             filt = BilateralDepthFilter(filter_width=width)
             for _ in range(5):
-                filt(d)
+                filt(d, m)
             st = torch.cuda.current_stream(device)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize(device)
             e0.record(st)
             for _ in range(reps):
-                filt(d)
+                filt(d, m)
             e1.record(st)
             torch.cuda.synchronize(device)
             s = e0.elapsed_time(e1) * 1e-3 / reps

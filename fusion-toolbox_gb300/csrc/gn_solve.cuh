@@ -1,6 +1,6 @@
-// FP64 Gauss-Newton step on the device: 6x6 Cholesky solve, SE(3)
-// exponential, left pose update, and the float32 pose view for the next
-// association.  Replaces the host code of the reference loop
+// Gauss-Newton step on the device: 6x6 LDL^T solve, SE(3) exponential,
+// left pose update, and the float32 pose view for the next association.
+// Replaces the host code of the reference loop
 // (slamtb/registration/icp.py:236-256: torch.cholesky + cholesky_solve on
 // the CPU, tenviz SE3.exp, transform = update @ transform).
 #pragma once
@@ -8,47 +8,6 @@
 #include "stb_common.cuh"
 
 namespace stb {
-
-// Lower Cholesky A = L L^T with LAPACK potrf's failure rule: a pivot that is
-// not > 0 (or NaN) fails.  Then solves A x = b.  Returns false on failure.
-__device__ inline bool cholesky_solve6(const double A[36], const double b[6],
-                                       double x[6]) {
-  double L[36];
-  double inv_diag[6];
-#pragma unroll
-  for (int j = 0; j < 6; ++j) {
-    double d = A[j * 6 + j];
-#pragma unroll
-    for (int k = 0; k < j; ++k) d -= L[j * 6 + k] * L[j * 6 + k];
-    if (!(d > 0.0)) return false;
-    const double ljj = sqrt(d);
-    L[j * 6 + j] = ljj;
-    inv_diag[j] = 1.0 / ljj;
-#pragma unroll
-    for (int i = j + 1; i < 6; ++i) {
-      double s = A[i * 6 + j];
-#pragma unroll
-      for (int k = 0; k < j; ++k) s -= L[i * 6 + k] * L[j * 6 + k];
-      L[i * 6 + j] = s * inv_diag[j];
-    }
-  }
-  double y[6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) {
-    double s = b[i];
-#pragma unroll
-    for (int k = 0; k < i; ++k) s -= L[i * 6 + k] * y[k];
-    y[i] = s * inv_diag[i];
-  }
-#pragma unroll
-  for (int i = 5; i >= 0; --i) {
-    double s = y[i];
-#pragma unroll
-    for (int k = i + 1; k < 6; ++k) s -= L[k * 6 + i] * x[k];
-    x[i] = s * inv_diag[i];
-  }
-  return true;
-}
 
 // Coefficients of the SE(3) exponential, A = sin t / t, B = (1 - cos t) / t^2,
 // C = (t - sin t) / t^3, of t2 = t^2.  Below t = 0.5 (every Gauss-Newton
@@ -160,37 +119,88 @@ __host__ __device__ constexpr int upper_index(int a, int b) {
 }  // namespace stb
 
 // ---------------------------------------------------------------------------
-// Warp-parallel FP64 Gauss-Newton step.  On this part every FP64 warp
-// instruction occupies the FP64 pipe of its SM sub-partition for ~64
-// cycles, however many lanes are active and whether or not it depends on
-// the previous one, so the cost of the step is its FP64 instruction count.
-// The layout therefore makes each FP64 instruction do the work of many
-// lanes: one lane per entry of the 6x6 lower triangle plus one per
-// right-hand side entry, an LDL^T factorisation (no square roots) whose
-// column step is one multiply and one FMA for all entries, pivot
-// reciprocals from the hardware approximation refined by one Newton-Raphson
-// step, the three exponential coefficients evaluated at once on three lane
-// groups (Estrin's scheme), and sign tests on the integer bits.  ~50 FP64
-// instructions per step.
+// Gauss-Newton step by one warp, in double-word arithmetic on the FP32 pipes.
+//
+// On this part every FP64 warp instruction occupies the FP64 pipe of its SM
+// sub-partition for ~64 cycles whatever its lanes or dependences, so a
+// step written in FP64 costs its FP64 instruction count (~50 of them, ~4 us
+// at the end of every iteration).  A double-word value is the unevaluated
+// sum hi + lo of two float32 with |lo| <= ulp(hi) / 2: ~48 significant bits
+// from float32 additions, multiplications and FMAs at 4 cycles each.  The
+// error-free transforms are Fast2Sum (Dekker), 2Sum (Knuth) and 2Prod by
+// FMA; the sum and the product are Algorithm 6 (AccurateDWPlusDW, relative
+// error <= 3u^2) and Algorithm 12 (DWTimesDW3, <= 4u^2) of Joldes, Muller
+// and Popescu, "Tight and rigorous error bounds for basic building blocks
+// of double-word arithmetic", ACM TOMS 44(2), 2017, u = 2^-24.
 // ---------------------------------------------------------------------------
 namespace stb {
 
-// 1/d for d > 0: rcp.approx.ftz.f64 (relative error below 2^-22) and one
-// Newton-Raphson step y <- y + y (1 - d y), which squares the error to below
-// 2^-44 (~6e-14).  A subnormal d flushes to an infinite reciprocal, which
-// turns the solution into NaN (flagged by the caller).
-__device__ __forceinline__ double rcp_fp64(double d) {
-  double y;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
-  const double e = fma(-d, y, 1.0);
-  return fma(y, e, y);
+struct dw {
+  float hi, lo;
+};
+
+// s + t = a + b exactly, for |a| >= |b| (or a == 0).
+__device__ __forceinline__ dw fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 
-// d > 0 (false for +-0, negatives and NaN; +inf passes, as the comparison
-// does) on the integer bits, off the FP64 pipe.
-__device__ __forceinline__ bool positive_bits(double d) {
-  const long long b = __double_as_longlong(d);
-  return b > 0 && b <= 0x7ff0000000000000ll;
+__device__ __forceinline__ dw two_sum_dw(float a, float b) {
+  dw r;
+  two_sum(a, b, r.hi, r.lo);
+  return r;
+}
+
+// Normalised double-word of a compensated sum (s, c).
+__device__ __forceinline__ float2 dw_of_csum(float s, float c) {
+  const dw r = two_sum_dw(s, c);
+  return make_float2(r.hi, r.lo);
+}
+
+__device__ __forceinline__ dw dw_add(dw x, dw y) {
+  const dw s = two_sum_dw(x.hi, y.hi), t = two_sum_dw(x.lo, y.lo);
+  const dw v = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
+}
+
+__device__ __forceinline__ dw dw_mul(dw x, dw y) {
+  const float ch = __fmul_rn(x.hi, y.hi);
+  const float cl1 = __fmaf_rn(x.hi, y.hi, -ch);
+  const float tl1 = __fmaf_rn(x.hi, y.lo, __fmul_rn(x.lo, y.lo));
+  const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
+  return fast_two_sum(ch, __fadd_rn(cl1, cl2));
+}
+
+// x - y z
+__device__ __forceinline__ dw dw_sub_mul(dw x, dw y, dw z) {
+  const dw p = dw_mul(y, z);
+  return dw_add(x, dw{-p.hi, -p.lo});
+}
+
+// 1 / d for d > 0: rcp.approx.ftz.f32 (relative error ~2^-23) and one
+// Newton-Raphson step y (1 + e), e = 1 - d y formed exactly enough (d.hi y
+// by 2Prod; 1 - ph is exact, ph being within a factor 2 of 1), which
+// squares the error to ~2^-46.  A subnormal d.hi flushes to an infinite
+// reciprocal, which turns the solution into NaN (flagged by the caller).
+__device__ __forceinline__ dw dw_rcp(dw d) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(d.hi));
+  const float ph = __fmul_rn(d.hi, y);
+  const float pl = __fmaf_rn(d.hi, y, -ph);
+  const float e = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, ph), pl), __fmul_rn(d.lo, y));
+  return fast_two_sum(y, __fmul_rn(y, e));
+}
+
+__device__ __forceinline__ dw shfl_dw(dw v, int src) {
+  return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// d > 0 on the integer bits (false for +-0, negatives and NaN; +inf
+// passes, as the comparison does).  For a normalised double-word the sign
+// and finiteness of hi are those of the value.
+__device__ __forceinline__ bool positive_bits(float d) {
+  const int b = __float_as_int(d);
+  return b > 0 && b <= 0x7f800000;
 }
 
 // Lane of entry (i, k), k <= i, of the 6x6 lower triangle stored column by
@@ -200,8 +210,7 @@ __host__ __device__ constexpr int tri_lane(int i, int k) { return 6 * k - k * (k
 
 // Maclaurin coefficient n (in t^2) of A = sin t / t (which = 0),
 // B = (1 - cos t) / t^2 (1) or C = (t - sin t) / t^3 (2): (-1)^n / (2n + 1 +
-// which)!, n < 8 (the series of se3_coeffs).  n is a compile-time constant,
-// which a per-lane select.
+// which)!, n < 8.  n is a compile-time constant, which a per-lane select.
 template <int n>
 __device__ __forceinline__ double se3_series_coeff(int which) {
   constexpr double f[18] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0,
@@ -213,16 +222,18 @@ __device__ __forceinline__ double se3_series_coeff(int which) {
 }
 
 // One Gauss-Newton update by one warp (all 32 lanes call it).
-//   up: the 21 packed upper-triangle entries of J^T J (shared, FP64),
-//   bv: J^T r (6), T: the current pose (16, row-major), all shared.
-// Solves J^T J x = J^T r by LDL^T with the failure rule of LAPACK potrf
-// (a pivot that is not > 0, or NaN, fails: the LDL^T pivots are the squares
-// of the Cholesky pivots), then Tn = exp(x) T.  Returns the verdict
-// (uniform); on success lanes 0..15 hold Tn's entries in tn_out (lane k ->
-// entry k), and every lane holds x in xs.
-__device__ inline bool warp_gn_update(const double *up, const double *bv, const double *T,
-                                      double *xs, double &tn_out, int lane) {
-  const unsigned full = 0xffffffffu;
+//   up: the 21 packed upper-triangle entries of J^T J and bv: J^T r (6),
+//       normalised double-words (hi, lo) in shared memory;
+//   T: the current pose (16, row-major, FP64, shared).
+// Solves J^T J x = J^T r by LDL^T with the failure rule of LAPACK potrf (a
+// pivot that is not > 0, or NaN, fails: the LDL^T pivots are the squares of
+// the Cholesky pivots), one lane per triangle entry and one per right-hand
+// side entry, so that a column step is one product and one difference for
+// all entries.  Then Tn = exp(x) T in FP64.  Returns the verdict (uniform);
+// on success lanes 0..15 hold Tn's entries in tn_out (lane k -> entry k),
+// and every lane holds x rounded to float32 in xs (for the finiteness test).
+__device__ inline bool warp_gn_update(const float2 *up, const float2 *bv, const double *T,
+                                      float *xs, double &tn_out, int lane) {
   // this lane's entry (i, k); k == 6 marks the right-hand side
   int ei = 0, ek = 0;
   if (lane < 21) {
@@ -239,24 +250,30 @@ __device__ inline bool warp_gn_update(const double *up, const double *bv, const 
   }
   const bool is_rhs = (lane >= 21 && lane < 27);
   const bool is_tri = lane < 21;
-  double v = 0.0;
-  if (is_tri) v = up[upper_index(ek, ei)];
-  if (is_rhs) v = bv[ei];
+  dw v = {0.f, 0.f};
+  if (is_tri) {
+    const float2 a = up[upper_index(ek, ei)];
+    v = {a.x, a.y};
+  }
+  if (is_rhs) {
+    const float2 b = bv[ei];
+    v = {b.x, b.y};
+  }
   bool ok = true;
   // forward: LDL^T factorisation with L z = b and y = D^-1 z fused in
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
-    const double piv = __shfl_sync(full, v, tri_lane(j, j));
-    ok = ok && positive_bits(piv);
-    const double inv = rcp_fp64(piv);
+    const dw piv = shfl_dw(v, tri_lane(j, j));
+    ok = ok && positive_bits(piv.hi);
+    const dw inv = dw_rcp(piv);
     const int src_i = (ei >= j) ? tri_lane(ei, j) : 0;
     const int src_k = is_rhs ? 21 + j : ((ek >= j && ek < 6) ? tri_lane(ek, j) : 0);
-    const double aij = __shfl_sync(full, v, src_i);
-    const double akj = __shfl_sync(full, v, src_k);
+    const dw aij = shfl_dw(v, src_i);
+    const dw akj = shfl_dw(v, src_k);
     const bool own_y = is_rhs && ei == j;
-    const double t = (own_y ? v : aij) * inv;  // L_ij, or y_j on the rhs lane j
+    const dw t = dw_mul(own_y ? v : aij, inv);  // L_ij, or y_j on the rhs lane j
     const bool upd = (is_tri && ek > j && ei >= ek) || (is_rhs && ei > j);
-    const double nv = fma(-t, akj, v);
+    const dw nv = dw_sub_mul(v, t, akj);
     if (upd) v = nv;
     if ((is_tri && ek == j && ei > j) || own_y) v = t;
   }
@@ -264,30 +281,42 @@ __device__ inline bool warp_gn_update(const double *up, const double *bv, const 
   // backward: L^T x = y; rhs lane i ends with x_i
 #pragma unroll
   for (int j = 5; j >= 0; --j) {
-    const double xj = __shfl_sync(full, v, 21 + j);
-    xs[j] = xj;
+    const dw xj = shfl_dw(v, 21 + j);
+    xs[j] = xj.hi;
     if (j > 0) {
       const int src = (is_rhs && ei < j) ? tri_lane(j, ei) : 0;
-      const double lji = __shfl_sync(full, v, src);
-      const double nv = fma(-lji, xj, v);
+      const dw lji = shfl_dw(v, src);
+      const dw nv = dw_sub_mul(v, lji, xj);
       if (is_rhs && ei < j) v = nv;
     }
   }
-  // exp(x): coefficients A (lanes 0..9), B (10..19), C (20..31) at once
-  const double wx = xs[3], wy = xs[4], wz = xs[5];
+  // x to FP64 (the rhs lane i converts x_i, then every lane gathers all six)
+  const double xd = (double)v.hi + (double)v.lo;
+  double x[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) x[k] = __shfl_sync(0xffffffffu, xd, 21 + k);
+  // exp(x) in FP64 (its rounding decides the float32 pose view of the next
+  // association, which therefore stays that of an FP64 update).  Below
+  // t = 0.5 the coefficients A = sin t / t, B = (1 - cos t) / t^2,
+  // C = (t - sin t) / t^3 are their Maclaurin series in t^2 through t^12
+  // (the first omitted term is below 0.5^14 / 15! < 5e-17), the three
+  // evaluated at once on three lane groups by Horner's rule: 6 FP64
+  // instructions; above, the closed forms.
+  const double wx = x[3], wy = x[4], wz = x[5];
   const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
   double A, B, C;
   if (t2 < 0.25) {
     const int which = lane < 10 ? 0 : (lane < 20 ? 1 : 2);
-    const double u2 = t2 * t2, u4 = u2 * u2;
-    const double a01 = fma(se3_series_coeff<1>(which), t2, se3_series_coeff<0>(which));
-    const double a23 = fma(se3_series_coeff<3>(which), t2, se3_series_coeff<2>(which));
-    const double a45 = fma(se3_series_coeff<5>(which), t2, se3_series_coeff<4>(which));
-    const double a67 = fma(se3_series_coeff<7>(which), t2, se3_series_coeff<6>(which));
-    const double coef = fma(u4, fma(u2, a67, a45), fma(u2, a23, a01));
-    A = __shfl_sync(full, coef, 0);
-    B = __shfl_sync(full, coef, 10);
-    C = __shfl_sync(full, coef, 20);
+    double coef = se3_series_coeff<6>(which);
+    coef = fma(coef, t2, se3_series_coeff<5>(which));
+    coef = fma(coef, t2, se3_series_coeff<4>(which));
+    coef = fma(coef, t2, se3_series_coeff<3>(which));
+    coef = fma(coef, t2, se3_series_coeff<2>(which));
+    coef = fma(coef, t2, se3_series_coeff<1>(which));
+    coef = fma(coef, t2, se3_series_coeff<0>(which));
+    A = __shfl_sync(0xffffffffu, coef, 0);
+    B = __shfl_sync(0xffffffffu, coef, 10);
+    C = __shfl_sync(0xffffffffu, coef, 20);
   } else {
     se3_coeffs(t2, A, B, C);
   }
@@ -304,13 +333,16 @@ __device__ inline bool warp_gn_update(const double *up, const double *bv, const 
   const bool isR = lane < 9;
   const double val = fma(isR ? A : B, Wac, fma(isR ? B : C, W2ac, diag ? 1.0 : 0.0));
   // t_a = sum_c V_ac x_c (V row a on lanes 9 + 3a ...)
-  const double v0 = __shfl_sync(full, val, 9 + 3 * ea), v1 = __shfl_sync(full, val, 10 + 3 * ea),
-               v2 = __shfl_sync(full, val, 11 + 3 * ea);
-  const double ta = fma(v0, xs[0], fma(v1, xs[1], v2 * xs[2]));
+  const double v0 = __shfl_sync(0xffffffffu, val, 9 + 3 * ea),
+               v1 = __shfl_sync(0xffffffffu, val, 10 + 3 * ea),
+               v2 = __shfl_sync(0xffffffffu, val, 11 + 3 * ea);
+  const double ta = fma(v0, x[0], fma(v1, x[1], v2 * x[2]));
   // Tn = [R t] T: lane q = 4 row + col < 12
   const int row = lane < 12 ? (lane >> 2) : 0, col = lane & 3;
-  const double r0 = __shfl_sync(full, val, 3 * row), r1 = __shfl_sync(full, val, 3 * row + 1),
-               r2 = __shfl_sync(full, val, 3 * row + 2), tr = __shfl_sync(full, ta, 3 * row);
+  const double r0 = __shfl_sync(0xffffffffu, val, 3 * row),
+               r1 = __shfl_sync(0xffffffffu, val, 3 * row + 1),
+               r2 = __shfl_sync(0xffffffffu, val, 3 * row + 2),
+               tr = __shfl_sync(0xffffffffu, ta, 3 * row);
   double tn = fma(r0, T[col], fma(r1, T[4 + col], fma(r2, T[8 + col], col == 3 ? tr : 0.0)));
   if (lane >= 12) tn = (lane == 15) ? 1.0 : 0.0;
   tn_out = tn;

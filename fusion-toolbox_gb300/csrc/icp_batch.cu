@@ -659,18 +659,19 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
 }
 
 // ---------------------------------------------------------------------------
-// per-pair FP64 step by warp 0 (totals in smem)
+// per-pair Gauss-Newton step by warp 0 (totals in smem)
 // ---------------------------------------------------------------------------
 __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const double *tot,
-                          const double *T) {
+                          const float2 *totw, const double *T) {
   const int lane = threadIdx.x & 31;
   PairState *ps = a.ps + p;
   const LevelP &q = a.lp[level];
   const double cg = tot[kCountGeomB], cf = tot[kCountFeatB];
   const double count = q.use_geom ? fmax(cg, cf) : cf;
   double *H = a.history ? a.history + ((size_t)p * a.total_iters + s) * STB_HIST_SIZE : nullptr;
-  double xs[6], tn;
-  const bool ok = warp_gn_update(tot, tot + kJrB, T, xs, tn, lane);
+  float xs[6];
+  double tn;
+  const bool ok = warp_gn_update(totw, totw + kJrB, T, xs, tn, lane);
   double *R = a.results + (size_t)p * STB_RES_SIZE;
   for (int k = lane; k < 36; k += 32) {
     const int r = k / 6, c = k % 6;
@@ -740,6 +741,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   __shared__ int s_last;
   __shared__ float bs[32], bc[32];
   __shared__ double tot[32];
+  __shared__ float2 totw[32];
   const int p = cache_pair(a, off, level, t, !kInfo, tc);
   if (tc.skip) return;
   const Pose32 &P = tc.P;
@@ -879,7 +881,10 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
     fold_slots<kN>(a.grp_part + (size_t)(g0 + c0) * kSlotFloats, cnt, bs, bc);
     if (threadIdx.x < kN) csum_merge(run[0], bs[threadIdx.x], bc[threadIdx.x]);
   }
-  if (threadIdx.x < kN) tot[threadIdx.x] = (double)run[0].s + (double)run[0].c;
+  if (threadIdx.x < kN) {
+    tot[threadIdx.x] = (double)run[0].s + (double)run[0].c;
+    totw[threadIdx.x] = dw_of_csum(run[0].s, run[0].c);
+  }
   __syncthreads();
   if (kInfo) {
     double *R = a.results + (size_t)p * STB_RES_SIZE;
@@ -893,7 +898,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
       R[STB_RES_RESIDUAL] = n > 0.0 ? __ldcg(&a.ps[p].last_r2) / n : INFINITY;
     }
   } else if (threadIdx.x < 32) {
-    pair_step(a, p, level, s, tot, tc.T);
+    pair_step(a, p, level, s, tot, totw, tc.T);
   }
   __syncthreads();
 }

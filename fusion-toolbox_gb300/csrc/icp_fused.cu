@@ -277,13 +277,15 @@ __device__ __forceinline__ bool publish_slot(const float2 *bsum, float2 *part, u
   return true;
 }
 
-// Last block: FP64 totals of kN accumulators from all block slots.  Warp w
+// Last block: totals of kN accumulators from all block slots, in FP64 and
+// (when totw is given) as double-words for the step.  Warp w
 // folds slots w, w + 8, ... with lane = accumulator; every load of a round
 // (kFoldLoads slots) is issued before its additions, so 300 slots cost two
 // L2 round trips.  The eight warp results are merged through shared memory.
 constexpr int kFoldLoads = 24;
 template <int kN, int kT>
-__device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, double *tot) {
+__device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, double *tot,
+                                            float2 *totw = nullptr) {
   __shared__ float2 wsum[kT / 32][32];
   constexpr int kW = kT / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -306,6 +308,7 @@ __device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, dou
 #pragma unroll
     for (int w = 0; w < kW; ++w) csum_merge(u, wsum[w][threadIdx.x].x, wsum[w][threadIdx.x].y);
     tot[threadIdx.x] = (double)u.s + (double)u.c;
+    if (totw) totw[threadIdx.x] = dw_of_csum(u.s, u.c);
   }
   __syncthreads();
 }
@@ -325,18 +328,21 @@ __device__ __forceinline__ void load_state_view(StateView &V, const State *S) {
   if (threadIdx.x == 17) V.iters_done = S->iters_done;
 }
 
-// One Gauss-Newton step from the FP64 totals in shared memory, by one warp
-// (warp_gn_update of gn_solve.cuh).  The residual r2 / count is stored for
-// the information pass to divide.
-__device__ void gn_step_warp(const Job *J, const StateView &V, const double *tot, int iter) {
+// One Gauss-Newton step from the totals in shared memory, by one warp
+// (warp_gn_update of gn_solve.cuh, on their double-words; the FP64 copies go
+// to the result and the history).  The residual r2 / count is stored for the
+// information pass to divide.
+__device__ void gn_step_warp(const Job *J, const StateView &V, const double *tot,
+                             const float2 *totw, int iter) {
   __shared__ float rt32[12];
   const int lane = threadIdx.x & 31;
   State *S = J->state;
   const double cg = tot[kCountGeom], cf = tot[kCountFeat];
   const double count = J->use_geom ? fmax(cg, cf) : cf;
   double *H = J->history ? J->history + (size_t)iter * STB_HIST_SIZE : nullptr;
-  double xs[6], tn;
-  const bool ok = warp_gn_update(tot, tot + kJr, V.T, xs, tn, lane);
+  float xs[6];
+  double tn;
+  const bool ok = warp_gn_update(totw, totw + kJr, V.T, xs, tn, lane);
   double *R = J->result;
   for (int k = lane; k < 36; k += 32) {
     const int r = k / 6, c = k % 6;
@@ -413,6 +419,7 @@ __global__ void __launch_bounds__(kT) k_reduce(const Job *__restrict__ J, int ep
   __shared__ float2 bsum[kAccs];
   __shared__ int is_last;
   __shared__ double tot[kAccs];
+  __shared__ float2 totw[kAccs];
   State *S = J->state;
   grid_dependency_wait();  // the association has written the key map
   grid_launch_dependents();
@@ -494,10 +501,10 @@ __global__ void __launch_bounds__(kT) k_reduce(const Job *__restrict__ J, int ep
 
   block_reduce<kAccs, kT>(acc, red, bsum);
   if (!publish_slot<kAccs>(bsum, J->part, &S->ticket, &is_last)) return;
-  grid_totals<kAccs, kT>(J->part, gridDim.x, tot);
+  grid_totals<kAccs, kT>(J->part, gridDim.x, tot, totw);
   if (threadIdx.x < 32) {
     if (threadIdx.x == 0) S->ticket = 0;
-    gn_step_warp(J, V, tot, epoch);
+    gn_step_warp(J, V, tot, totw, epoch);
   }
 }
 

@@ -168,7 +168,7 @@ class BilateralDepthFilter:
         self.depth_scale = depth_scale
         self._out_tensor = None
 
-    def __call__(self, depth, mask):
+    def __call__(self, depth, mask=None):
         self._out_tensor = bilateral_depth_filter(
             depth, mask, self._out_tensor, self.filter_width, self.sigma_color,
             self.sigma_space, self.depth_scale)
