@@ -44,8 +44,9 @@ constexpr int kSlotFloats = 64;       // (s[32], c[32]) per partial slot
 constexpr int kMinTile = kThreads * 2;
 constexpr unsigned kSpinLimit = 1u << 26;  // x >= 32 ns sleeps: a few seconds
 constexpr int kJrB = 21, kR2B = 27, kCountGeomB = 28, kCountFeatB = 29;
-// barrier words: [0] root arrivals, [1] generation, [2] error, [8 + g] the
-// arrivals of group g (room for 4088 groups of 8 blocks)
+// barrier words: [0] root arrivals, [1] generation, [2] error, [4] and [5]
+// the tile counters of alternating phases, [8 + g] the arrivals of group g
+// (room for 4088 groups of 8 blocks)
 constexpr size_t kSyncBytes = 16384;
 
 struct LevelP {
@@ -171,6 +172,32 @@ __device__ bool grid_sync(unsigned *sync) {
   }
   __syncthreads();
   return s_ok;
+}
+
+// Dynamic tile scheduling.  A block's first tile of a phase is its block
+// index; later ones are handed out by an atomic counter (sync[4 + (phase &
+// 1)], offset by the grid size) rather than by a fixed stride, so a block
+// whose tiles finish early takes more.  With the fixed stride, blocks spent
+// about a seventh of the 256-pair run waiting at the phases' grid barriers
+// for the slowest block.  Thread 0 fetches the next index while the block
+// works on the current tile, so a phase with at most one tile per block (a
+// single pair) pays no fetch latency.  Block 0 zeroes the other counter at
+// the start of a phase: its last user ended at the previous grid barrier,
+// and its next user starts after the next one.  The fetched index alternates
+// between two shared words: a word is rewritten two tiles later, after a
+// barrier that every thread passes only once it has read it.
+template <typename F>
+__device__ __forceinline__ void for_each_tile(unsigned *sync, int phase, long long ntiles, F f) {
+  __shared__ unsigned s_next[2];
+  unsigned *ctr = sync + 4 + (phase & 1);
+  if (blockIdx.x == 0 && threadIdx.x == 0) sync[4 + ((phase + 1) & 1)] = 0u;
+  long long t = blockIdx.x;
+  for (int i = 0; t < ntiles; i ^= 1) {
+    if (threadIdx.x == 0) s_next[i] = gridDim.x + atomicAdd(ctr, 1u);
+    f(t);
+    __syncthreads();
+    t = s_next[i];
+  }
 }
 
 constexpr int kStageOff = 1025;  // offsets staged in shared memory up to 1024 pairs
@@ -941,6 +968,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
   if (!grid_sync(a.sync)) return;
 
   int s = 0;
+  int phase = 0;  // tile phases so far (selects the tile counter)
   for (int level = 0; level < a.L; ++level) {
     // level start: the reference's next estimator gets the previous result's
     // transform, None (identity) when that level's first iteration failed
@@ -974,13 +1002,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
     for (int it = 0; it < a.lp[level].iters; ++it, ++s) {
       const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
       reset_cache(tc);
-      for (long long t = blockIdx.x; t < src_tiles; t += gridDim.x)
+      for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
         assoc_tile(a, off, level, t, s, false, tc, ctl, ph);
+      });
       if (!grid_sync(a.sync)) return;
       off = stage_offsets(a.tgt_off + row, a.B, s_off);
       reset_cache(tc);
-      for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
+      for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
         reduce_tile<FT, kFeat, false, kHWC>(a, off, level, t, s, tc, ctl, ph);
+      });
       if (!grid_sync(a.sync)) return;
     }
   }
@@ -991,13 +1021,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
   const long long tgt_tiles = __ldcg(a.tgt_off + row + a.B);
   const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
   reset_cache(tc);
-  for (long long t = blockIdx.x; t < src_tiles; t += gridDim.x)
+  for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
     assoc_tile(a, off, level, t, s, true, tc, ctl, ph);
+  });
   if (!grid_sync(a.sync)) return;
   off = stage_offsets(a.tgt_off + row, a.B, s_off);
   reset_cache(tc);
-  for (long long t = blockIdx.x; t < tgt_tiles; t += gridDim.x)
+  for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
     reduce_tile<FT, false, true, false>(a, off, level, t, s, tc, ctl, ph);
+  });
 }
 
 // Flags every pair's status when the persistent kernel stopped early:

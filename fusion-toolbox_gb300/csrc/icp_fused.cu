@@ -83,7 +83,29 @@ struct Job {
   float2 *part;  // per block: kSlotAccs (sum, compensation) pairs
   int nblocks;
   State *state;
+  // intrinsics (fx, cx, fy, cy) and initial pose given as host values
+  // (kcam / init null): carried in the launch parameters, no copy
+  float kcam_v[4];
+  double init_v[16];
+  int has_init_v;
 };
+static_assert(sizeof(Job) <= 1024, "the workspace's Job slot is 1024 bytes");
+
+// Host-side: intrinsics and initial pose into the Job, by pointer (device
+// memory) or by value (host memory, read here).
+inline void set_small_inputs(Job &job, const float *kcam, bool kcam_host, const double *init,
+                             bool init_host) {
+  job.kcam = kcam_host ? nullptr : kcam;
+  if (kcam_host) {
+    job.kcam_v[0] = kcam[0];
+    job.kcam_v[1] = kcam[2];
+    job.kcam_v[2] = kcam[4];
+    job.kcam_v[3] = kcam[5];
+  }
+  job.init = init_host ? nullptr : init;
+  job.has_init_v = init != nullptr && init_host;
+  for (int k = 0; k < 16; ++k) job.init_v[k] = job.has_init_v ? init[k] : 0.0;
+}
 
 constexpr size_t kSlot = 1024;
 
@@ -124,11 +146,12 @@ __global__ void k_begin(Job job, Job *dst) {
   *dst = job;
   State *S = job.state;
   for (int k = 0; k < 16; ++k)
-    S->T[k] = job.init ? job.init[k] : ((k % 5) == 0 ? 1.0 : 0.0);
-  S->pose.fx = job.kcam[0];
-  S->pose.cx = job.kcam[2];
-  S->pose.fy = job.kcam[4];
-  S->pose.cy = job.kcam[5];
+    S->T[k] = job.init ? job.init[k]
+                       : (job.has_init_v ? job.init_v[k] : ((k % 5) == 0 ? 1.0 : 0.0));
+  S->pose.fx = job.kcam ? job.kcam[0] : job.kcam_v[0];
+  S->pose.cx = job.kcam ? job.kcam[2] : job.kcam_v[1];
+  S->pose.fy = job.kcam ? job.kcam[4] : job.kcam_v[2];
+  S->pose.cy = job.kcam ? job.kcam[5] : job.kcam_v[3];
   refresh_pose32(S->pose, S->T);
   S->ticket = 0;
   S->stopped = 0;
@@ -841,7 +864,8 @@ extern "C" int stb_icp_estimate(
     if (channel_mode != 0 && channel_mode != 1)
       return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
   }
-  STB_TRY(check_device_ptr(kcam, "kcam"));
+  bool kcam_host, init_host;
+  STB_TRY(check_small_input(kcam, "kcam", false, &kcam_host));
   STB_TRY(check_device_ptr(src_points, "src_points"));
   STB_TRY(check_device_ptr(src_normals, "src_normals"));
   STB_TRY(check_device_ptr(src_mask, "src_mask"));
@@ -852,7 +876,7 @@ extern "C" int stb_icp_estimate(
     STB_TRY(check_device_ptr(src_feats, "src_feats"));
     STB_TRY(check_device_ptr(tgt_feats, "tgt_feats"));
   }
-  STB_TRY(check_device_ptr(init_transform, "transform", true));
+  STB_TRY(check_small_input(init_transform, "transform", true, &init_host));
   STB_TRY(check_device_ptr(workspace, "workspace"));
   STB_TRY(check_device_ptr(result, "result"));
   STB_TRY(check_device_ptr(history, "history", true));
@@ -873,7 +897,6 @@ extern "C" int stb_icp_estimate(
   p.job_dev = reinterpret_cast<Job *>(ws);
 
   Job job;
-  job.kcam = kcam;
   job.sp = src_points;
   job.sn = src_normals;
   job.sm = src_mask;
@@ -887,7 +910,7 @@ extern "C" int stb_icp_estimate(
   job.tf = tgt_feats;
   job.C = p.C;
   job.dtype = p.dtype;
-  job.init = init_transform;
+  set_small_inputs(job, kcam, kcam_host, init_transform, init_host);
   job.iters = num_iters;
   job.channel_mode = p.channel_mode;
   job.use_geom = use_geom;
@@ -1048,7 +1071,8 @@ extern "C" int stb_icp_estimate_static(
     if (channel_mode != 0 && channel_mode != 1)
       return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
   }
-  STB_TRY(check_device_ptr(kcam, "kcam"));
+  bool kcam_host, init_host;
+  STB_TRY(check_small_input(kcam, "kcam", false, &kcam_host));
   STB_TRY(check_device_ptr(src_points, "src_points"));
   STB_TRY(check_device_ptr(src_normals, "src_normals"));
   STB_TRY(check_device_ptr(src_mask, "src_mask"));
@@ -1059,7 +1083,7 @@ extern "C" int stb_icp_estimate_static(
     STB_TRY(check_device_ptr(src_feats, "src_feats"));
     STB_TRY(check_device_ptr(tgt_feats, "tgt_feats"));
   }
-  STB_TRY(check_device_ptr(init_transform, "transform", true));
+  STB_TRY(check_small_input(init_transform, "transform", true, &init_host));
   STB_TRY(check_device_ptr(result, "result"));
   STB_TRY(check_device_ptr(history, "history", true));
   STB_TRY(prepare_reduce_kernels());
@@ -1081,7 +1105,6 @@ extern "C" int stb_icp_estimate_static(
   p.job_dev = reinterpret_cast<Job *>(ws);
 
   Job job;
-  job.kcam = kcam;
   job.sp = src_points;
   job.sn = src_normals;
   job.sm = src_mask;
@@ -1095,7 +1118,7 @@ extern "C" int stb_icp_estimate_static(
   job.tf = tgt_feats;
   job.C = p.C;
   job.dtype = p.dtype;
-  job.init = init_transform;
+  set_small_inputs(job, kcam, kcam_host, init_transform, init_host);
   job.iters = num_iters;
   job.channel_mode = p.channel_mode;
   job.use_geom = use_geom;

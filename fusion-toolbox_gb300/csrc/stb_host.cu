@@ -56,6 +56,25 @@ int check_device_ptr(const void *p, const char *name, bool allow_null) {
   return STB_OK;
 }
 
+int check_small_input(const void *p, const char *name, bool allow_null, bool *on_host) {
+  *on_host = false;
+  if (p == nullptr) return allow_null ? STB_OK : fail(STB_EINVAL, "Check failed: %s: null pointer", name);
+  int dev = -1;
+  cudaGetDevice(&dev);
+  for (const PtrCacheEntry &e : g_ptr_cache)
+    if (e.p == p && e.dev == dev) return STB_OK;
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(STB_EDEVICE, "Check failed: %s: not a host or device address", name);
+  }
+  if (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeUnregistered) {
+    *on_host = true;
+    return STB_OK;
+  }
+  return check_device_ptr(p, name, false);
+}
+
 int check_launch(const char *what) {
   const cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess)

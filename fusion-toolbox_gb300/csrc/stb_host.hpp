@@ -20,6 +20,11 @@ void clear_error();
 // gpu tensor" (include/slamtb/error.hpp:12-37).
 int check_device_ptr(const void *p, const char *name, bool allow_null = false);
 
+// For small inputs whose values a call reads on the host (intrinsics, an
+// initial pose): device memory of the current device (*on_host = false), or
+// host memory, pinned or pageable (*on_host = true).
+int check_small_input(const void *p, const char *name, bool allow_null, bool *on_host);
+
 // STB_ECUDA with the CUDA error string if the last launch failed.
 int check_launch(const char *what);
 

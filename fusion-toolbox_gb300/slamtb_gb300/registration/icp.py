@@ -6,8 +6,10 @@ the Gauss-Newton loop runs on the device as one call into
 the result at the end instead of the reference's ~8 synchronisations per
 iteration.
 """
+import ctypes
 import math
 
+import numpy as np
 import torch
 
 from .. import _native as N
@@ -15,10 +17,21 @@ from .. import processing
 from .result import RegistrationResult
 
 
-def _kcam_matrix(kcam, device):
-    m = kcam.matrix if hasattr(kcam, "matrix") else kcam
-    m = torch.as_tensor(m)
-    return m.to(device=device, dtype=torch.float32).contiguous()
+def _small_input(x, device, tdtype, ndtype, numel, name):
+    """(keep-alive, pointer) of the intrinsics or the initial pose: a tensor
+    on the device as it is, anything else as a host array that the library
+    reads during the call (into the launch parameters: no copy, no wait)."""
+    if isinstance(x, torch.Tensor) and x.device == device:
+        a = x.to(dtype=tdtype).contiguous()
+        ptr = N.ptr(a)
+    else:
+        if isinstance(x, torch.Tensor):
+            x = x.detach().cpu().numpy()
+        a = np.ascontiguousarray(x, dtype=ndtype)
+        ptr = ctypes.c_void_p(a.ctypes.data)
+    if (a.numel() if isinstance(a, torch.Tensor) else a.size) != numel:
+        raise RuntimeError(f"Check failed: {name} must have {numel} entries")
+    return a, ptr
 
 
 class _Workspace:
@@ -30,6 +43,14 @@ class _Workspace:
         self.buf = None
         self.result = None
         self.history = None
+        self.result_host = None
+
+    def host_result(self):
+        """Pinned host copy of the result block (reused; the returned
+        RegistrationResult never aliases it)."""
+        if self.result_host is None:
+            self.result_host = torch.empty(N.RES_SIZE, dtype=torch.float64, pin_memory=True)
+        return self.result_host
 
     def get(self, device, num_source, height, width, num_iters, history):
         need = int(N.lib().stb_icp_workspace_bytes(num_source, height, width))
@@ -127,9 +148,11 @@ class ICPOdometry:
         res, hist, n, dtype = self.launch(
             kcam, source_points, source_normals, source_mask, source_feats, target_points,
             target_mask, target_normals, target_feats, transform)
-        out = res.cpu()
+        out = self._ws.host_result()
+        out.copy_(res, non_blocking=True)
         if hist is not None:
             self.last_history = hist[:self.num_iters].cpu()
+        torch.cuda.current_stream(res.device).synchronize()
         return self._result(out, n, dtype)
 
     def launch(self, kcam, source_points, source_normals, source_mask, source_feats=None,
@@ -145,7 +168,6 @@ class ICPOdometry:
         if device.type != "cuda":
             raise RuntimeError("Check failed: target_points: Expected a gpu tensor "
                                "(slamtb_gb300 runs on CUDA devices only)")
-        k = _kcam_matrix(kcam, device)
         sp = source_points.reshape(-1, 3)
         sn = source_normals.reshape(-1, 3)
         sm = source_mask.reshape(-1)
@@ -185,15 +207,17 @@ class ICPOdometry:
                 tf = processing.interleave_features(tf)
                 sf = processing.interleave_features(sf)
                 code += N.STB_F32_HWC
-        init = None
+        m = kcam.matrix if hasattr(kcam, "matrix") else kcam
+        k, kptr = _small_input(m, device, torch.float32, np.float32, 9, "kcam")
+        init = iptr = None
         if transform is not None:
-            init = torch.as_tensor(transform).to(device=device, dtype=torch.float64).contiguous()
-
+            init, iptr = _small_input(transform, device, torch.float64, np.float64, 16,
+                                      "transform")
         ws, res, hist = self._ws.get(device, n, h, w, self.num_iters, self.record_history)
         with torch.cuda.device(device):
             N.check(N.lib().stb_icp_estimate(
-                N.ptr(k), N.ptr(sp), N.ptr(sn), N.ptr(sm), n, N.ptr(sf), N.ptr(tp),
-                N.ptr(tn), N.ptr(tm), h, w, N.ptr(tf), channels, code, N.ptr(init),
+                kptr, N.ptr(sp), N.ptr(sn), N.ptr(sm), n, N.ptr(sf), N.ptr(tp),
+                N.ptr(tn), N.ptr(tm), h, w, N.ptr(tf), channels, code, iptr,
                 self.num_iters, float(self.geom_weight),
                 float(self.feat_weight if has_features else 0.0),
                 float(self.distance_threshold), float(self.normals_angle_thresh),
@@ -201,16 +225,21 @@ class ICPOdometry:
                 0 if self.feat_channel_mode == "last" else 1,
                 N.ptr(ws), ws.numel(), N.ptr(res), N.ptr(hist), int(self.use_graph),
                 N.stream_of(device)))
+        del k, init  # kept alive through the call
         return res, hist, n, sp.dtype
 
     @staticmethod
     def _result(out, n, dtype):
-        info = out[N.RES_INFO:N.RES_INFO + 36].view(6, 6).to(dtype)
-        if int(out[N.RES_ITERS]) == 0:
+        """RegistrationResult of one float64 result block (a CPU tensor);
+        the returned tensors are copies."""
+        o = out.numpy()
+        info = torch.from_numpy(o[N.RES_INFO:N.RES_INFO + 36].reshape(6, 6).astype(
+            np.float32 if dtype == torch.float32 else np.float64))
+        if int(o[N.RES_ITERS]) == 0:
             return RegistrationResult(information=info)
         return RegistrationResult(
-            out[N.RES_TRANSFORM:N.RES_TRANSFORM + 16].view(4, 4).clone(), info,
-            float(out[N.RES_RESIDUAL]), float(out[N.RES_MATCHES]) / n)
+            torch.from_numpy(o[N.RES_TRANSFORM:N.RES_TRANSFORM + 16].reshape(4, 4).copy()),
+            info, float(o[N.RES_RESIDUAL]), float(o[N.RES_MATCHES]) / n)
 
     def estimate_frame(self, source_frame, target_frame, source_feats=None,
                        target_feats=None, transform=None, device=None):

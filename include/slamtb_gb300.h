@@ -222,7 +222,10 @@ STB_API size_t stb_icp_workspace_bytes(int64_t num_source, int32_t height,
  * kcam: float32 3x3.  src_*: as stb_correspondence_map (source_mask must
  * have num_source entries).  src_feats / tgt_feats: NULL for geometric-only
  * or [channels, num_source] / [channels, height, width] of feat_dtype.
- * init_transform: float64 4x4 device pointer or NULL (identity).
+ * init_transform: float64 4x4 or NULL (identity).  kcam and init_transform
+ * may be device or host pointers: host values are read during the call and
+ * carried in the launch parameters (no copy, no synchronisation), so the
+ * host buffers can be reused as soon as the call returns.
  * channel_mode: 0 = reference behaviour (last channel's J), 1 = sum over
  * channels.  result: float64 [STB_RES_SIZE] device block.  history: NULL or
  * float64 [num_iters, STB_HIST_SIZE] per-iteration records.

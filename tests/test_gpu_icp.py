@@ -205,3 +205,38 @@ def test_interleave_features_is_a_transpose(cuda, dtype):
         out = interleave_features(f)
         assert out.shape == (h * w, c)
         assert torch.equal(out, f.reshape(c, -1).t().contiguous())
+
+
+def test_host_intrinsics_and_pose(cuda, pair0):
+    """Intrinsics as a host KCamera and initial poses as host tensors are
+    read during the call into the launch parameters: the results equal those
+    of device inputs, also with launches queued back to back, each with its
+    own pose (a later call's parameters never reach an earlier launch)."""
+    from slamtb_gb300.frame import KCamera
+    from slamtb_gb300.registration.icp import ICPOdometry
+    x = _dev(pair0, cuda)
+    x.pop("sf"), x.pop("tf")
+    icp = ICPOdometry(**GEOM)
+    kc = KCamera(pair0["kcam"])
+    rng = np.random.default_rng(3)
+    poses = []
+    for _ in range(7):
+        T = np.eye(4)
+        T[:3, 3] = rng.uniform(-0.01, 0.01, 3)
+        poses.append(torch.from_numpy(T))
+    ref = [_run_gpu(x, icp, transform=T.to(cuda)).transform.numpy().copy() for T in poses]
+    host = [icp.estimate(kc, x["sp"], x["sn"], x["sm"], target_points=x["tp"],
+                         target_mask=x["tm"], target_normals=x["tn"],
+                         transform=T).transform.numpy().copy() for T in poses]
+    for a, b in zip(ref, host):
+        np.testing.assert_array_equal(a, b)
+    # queued: every launch before any result is read (the result block is
+    # reused, so each is cloned on the stream right after its launch)
+    outs = [icp.launch(kc, x["sp"], x["sn"], x["sm"], target_points=x["tp"],
+                       target_mask=x["tm"], target_normals=x["tn"], transform=T)[0].clone()
+            for T in poses]
+    torch.cuda.synchronize(cuda)
+    from slamtb_gb300 import _native as N
+    for a, o in zip(ref, outs):
+        np.testing.assert_array_equal(a, o.cpu().numpy()[N.RES_TRANSFORM:N.RES_TRANSFORM + 16]
+                                      .reshape(4, 4))
