@@ -56,6 +56,13 @@ _SIGNATURES = {
     "stb_feature_interleave": (ctypes.c_int, [_vp, _vp, _i32, _i64, _i32, _vp]),
     "stb_bilateral_depth_filter": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _f32,
                                                   _f32, _f32, _vp]),
+    "stb_exp_rt_to_matrix": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp]),
+    "stb_exp_rt_to_matrix_backward": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "stb_matrix_to_exp_rt": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp]),
+    "stb_fpcl_match_forward": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _i64, _vp,
+                                              _vp, _vp, _vp, _vp, _vp, _i32, _vp]),
+    "stb_fpcl_match_backward": (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _i64, _vp, _vp, _vp,
+                                               _f64, _vp, _i32, _vp]),
     "stb_se3_exp_compose": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp]),
     "stb_se3_twist_grad": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp]),
     "stb_icp_loss_workspace_bytes": (_sz, [_i32, _i32, _i32]),

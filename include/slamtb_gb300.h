@@ -512,6 +512,65 @@ STB_API int stb_gaussian_blur3(const void *feats, int32_t channels,
                                int32_t feat_dtype, double sigma, void *dst,
                                void *stream);
 
+/* ---- differentiable registration layer (AutogradICP) ------------------ */
+
+/*
+ * ExpRtToMatrixOp::Forward (src/exp_rt_to_matrix.cu:41-53): count twists
+ * exp_rt [count][6] = [t; w] (t the translation, w the rotation axis times
+ * its angle) to matrix [count][3][4] = [R(w) | t], R by Rodrigues' formula.
+ * dtype: STB_F32 or STB_F64 (both arrays).
+ */
+STB_API int stb_exp_rt_to_matrix(const void *exp_rt, void *matrix, int64_t count,
+                                 int32_t dtype, void *stream);
+
+/*
+ * ExpRtToMatrixOp::Backward (src/exp_rt_to_matrix.cu:101-121): d_exp_rt
+ * [count][6] from d_matrix [count][3][4], the forward's exp_rt and matrix,
+ * with the rotation derivative of Gallego and Yezzi (src/exp_rt.hpp:90-138).
+ */
+STB_API int stb_exp_rt_to_matrix_backward(const void *d_matrix, const void *exp_rt,
+                                          const void *matrix, void *d_exp_rt, int64_t count,
+                                          int32_t dtype, void *stream);
+
+/*
+ * MatrixToExpRtOp::Forward (src/matrix_to_exp_rt.cu:35-48): matrix
+ * [count][3][4] to exp_rt [count][6] (translation, axis x angle of R).
+ */
+STB_API int stb_matrix_to_exp_rt(const void *matrix, void *exp_rt, int64_t count,
+                                 int32_t dtype, void *stream);
+
+/*
+ * FPCLMatcherOp::Forward (src/fpcl_matcher.cu:85-123).  src_points
+ * [num_source][3] (already in the target camera frame) are projected with
+ * kcam [3][3]; point i matches when its rounded projection lies in the
+ * height x width image and the high 32 bits of merge_map [height][width]
+ * (a stb_correspondence_map result) there equal i.  A match writes the
+ * target point and normal at that pixel to out_points / out_normals
+ * [num_source][3] and the bilinear sample of tgt_feats [channels][height]
+ * [width] at the unrounded projection to out_feats [channels][num_source];
+ * match_mask [num_source] gets 1.  Points that do not match get 0 and zero
+ * outputs.  dtype: STB_F32 or STB_F64 (every float array and kcam).
+ */
+STB_API int stb_fpcl_match_forward(const void *tgt_points, const void *tgt_normals,
+                                   const void *tgt_feats, int32_t channels, int32_t height,
+                                   int32_t width, const void *src_points, int64_t num_source,
+                                   const void *kcam, const int64_t *merge_map, void *out_points,
+                                   void *out_normals, void *out_feats, uint8_t *match_mask,
+                                   int32_t dtype, void *stream);
+
+/*
+ * FPCLMatcherOp::Backward (src/fpcl_matcher.cu:193-226): dx_points
+ * [num_source][3] = d loss / d source point from dl_feats [channels]
+ * [num_source] = d loss / d out_feats, by central differences of the
+ * bilinear sample with step grad_precision (0 < grad_precision < 0.5)
+ * through the projection's Jacobian; 0 where match_mask is 0.
+ */
+STB_API int stb_fpcl_match_backward(const void *tgt_feats, int32_t channels, int32_t height,
+                                    int32_t width, const void *src_points, int64_t num_source,
+                                    const uint8_t *match_mask, const void *dl_feats,
+                                    const void *kcam, double grad_precision, void *dx_points,
+                                    int32_t dtype, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

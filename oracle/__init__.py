@@ -14,6 +14,9 @@ Contents
 ``frame_prep``   numpy restatement of the frame preparation that feeds the
                  path (mask erosion, back-projection, central-difference
                  normals, XYZ / mask / feature pyramids).
+``autograd_oracle``  restatement of the differentiable registration layer
+                 (twist <-> matrix maps and their backward in FP64; the
+                 frame point-cloud matcher, FP32 op by op).
 ``png16``        a small PNG reader for the reference's 16-bit depth test
                  frames (the image has neither cv2 nor PIL).
 ``icp_port.c``   C/OpenMP restatement of the reference's CPU ICP path,

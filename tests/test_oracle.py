@@ -297,3 +297,102 @@ def test_bilateral_oracle_matches_literal_loop():
                     cs, ws = F(cs + F(cz * wt)), F(ws + wt)
             ref[r, c] = int(np.trunc(F(cs / ws)))
     np.testing.assert_array_equal(out, ref)
+
+
+def test_exp_rt_oracle_is_a_rotation_with_the_twist_axis():
+    from oracle import autograd_oracle as ao
+    rng = np.random.default_rng(5)
+    for w in [np.zeros(3), np.array([1e-9, 0, 0]), rng.normal(size=3) * 0.1,
+              rng.normal(size=3) * 1.2]:
+        R = ao.rotation64(w)
+        np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-14)
+        assert abs(np.linalg.det(R) - 1.0) < 1e-13
+        np.testing.assert_allclose(R @ w, w, atol=1e-14)
+        np.testing.assert_allclose(np.trace(R), 1 + 2 * np.cos(np.linalg.norm(w)), atol=1e-13)
+
+
+def test_exp_rt_backward_oracle_matches_finite_differences():
+    """The Gallego-Yezzi restatement against central differences of the
+    forward, including angles near the 1e-12 switch."""
+    from oracle import autograd_oracle as ao
+    rng = np.random.default_rng(6)
+    x = np.concatenate([rng.normal(size=(6, 3)), rng.normal(size=(6, 3))], axis=1)
+    x[1, 3:] *= 1e-3
+    x[2, 3:] *= 2.5 / np.linalg.norm(x[2, 3:])
+    x[3, 3:] = 0.0
+    g = rng.normal(size=(6, 3, 4))
+    an = ao.exp_rt_to_matrix_backward64(g, x)
+    fd = ao.exp_rt_to_matrix_fd64(g, x)
+    np.testing.assert_allclose(an, fd, rtol=1e-7, atol=1e-8)
+
+
+def test_matrix_to_exp_rt_oracle_round_trip():
+    from oracle import autograd_oracle as ao
+    rng = np.random.default_rng(7)
+    x = rng.normal(size=(8, 6))
+    x[:, 3:] *= (rng.uniform(0.01, 3.0, size=8) / np.linalg.norm(x[:, 3:], axis=1))[:, None]
+    np.testing.assert_allclose(ao.matrix_to_exp_rt64(ao.exp_rt_to_matrix64(x)), x, atol=1e-10)
+
+
+def test_fpcl_matcher_oracle_matches_literal_loops():
+    """The vectorised matcher restatement against per-point loops of the
+    same float32 operations (fpcl_matcher.cu:46-80 and :150-189)."""
+    from oracle import autograd_oracle as ao
+    F = np.float32
+    rng = np.random.default_rng(8)
+    h, w, c = 6, 7, 2
+    kcam = np.array([[5.0, 0, 3.1], [0, 5.0, 2.6], [0, 0, 1]], F)
+    tp = rng.normal(size=(h, w, 3)).astype(F)
+    tn = rng.normal(size=(h, w, 3)).astype(F)
+    tf = rng.normal(size=(c, h, w)).astype(F)
+    sp = np.stack([rng.uniform(-0.8, 0.8, 12), rng.uniform(-0.6, 0.6, 12),
+                   rng.uniform(1.0, 2.0, 12)], 1).astype(F)
+    ref = np.full((h, w), 0x0FFFFFFF7F800000, np.int64)
+    for i, p in enumerate(sp):      # every point wins its own pixel when free
+        uu = (kcam[0, 0] * p[0]) / p[2] + kcam[0, 2]
+        vv = (kcam[1, 1] * p[1]) / p[2] + kcam[1, 2]
+        r, q = int(np.floor(vv + 0.5)), int(np.floor(uu + 0.5))
+        if 0 <= r < h and 0 <= q < w and (ref[r, q] >> 32) == 0x0FFFFFFF:
+            ref[r, q] = np.int64(i) << 32
+    pts, nrm, fts, mask = ao.fpcl_forward32(tp, tn, tf, sp, kcam, ref)
+    dl = rng.normal(size=(c, 12)).astype(F)
+    dx = ao.fpcl_backward32(tf, sp, mask, dl, kcam, 0.005)
+
+    def bil(ch, u, v):
+        ui, vi = int(np.trunc(u)), int(np.trunc(v))
+        ur, vr = F(u - F(ui)), F(v - F(vi))
+        f = tf[ch]
+        v00 = f[vi, ui]
+        v10 = f[vi, ui + 1] if ui + 1 < w else F(0)
+        v01 = f[vi + 1, ui] if vi + 1 < h else F(0)
+        v11 = f[vi + 1, ui + 1] if (ui + 1 < w and vi + 1 < h) else F(0)
+        a0 = F(F(v00 * F(F(1) - ur)) + F(v10 * ur))
+        a1 = F(F(v01 * F(F(1) - ur)) + F(v11 * ur))
+        return F(F(a0 * F(F(1) - vr)) + F(a1 * vr))
+
+    for i, p in enumerate(sp):
+        u = F(F(F(kcam[0, 0] * p[0]) / p[2]) + kcam[0, 2])
+        v = F(F(F(kcam[1, 1] * p[1]) / p[2]) + kcam[1, 2])
+        q, r = int(np.floor(float(u) + 0.5)), int(np.floor(float(v) + 0.5))
+        ok = 0 <= q < w and 0 <= r < h and (ref[r, q] >> 32) == i
+        assert mask[i] == ok
+        if not ok:
+            assert not pts[i].any() and not dx[i].any()
+            continue
+        np.testing.assert_array_equal(pts[i], tp[r, q])
+        for ch in range(c):
+            assert fts[ch, i] == bil(ch, u, v)
+        hh = F(0.005)
+        dv = F(F(1) / F(F(2) * hh))
+        gu = gv = F(0)
+        for ch in range(c):
+            du = F(F(bil(ch, F(u + hh), v) - bil(ch, max(F(u - hh), F(0)), v)) * dv)
+            dvv = F(F(bil(ch, u, F(v + hh)) - bil(ch, u, max(F(v - hh), F(0)))) * dv)
+            gu = F(gu + F(du * dl[ch, i]))
+            gv = F(gv + F(dvv * dl[ch, i]))
+        z2 = F(p[2] * p[2])
+        j00, j02 = F(kcam[0, 0] / p[2]), F(F(-p[0] * kcam[0, 0]) / z2)
+        j11, j12 = F(kcam[1, 1] / p[2]), F(F(-p[1] * kcam[1, 1]) / z2)
+        np.testing.assert_array_equal(dx[i], [F(j00 * gu), F(j11 * gv),
+                                              F(F(j02 * gu) + F(j12 * gv))])
+    assert mask.sum() >= 4
