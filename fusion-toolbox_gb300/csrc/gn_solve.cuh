@@ -221,19 +221,42 @@ __device__ __forceinline__ double se3_series_coeff(int which) {
   return which == 0 ? ca : (which == 1 ? cb : cc);
 }
 
+// The same coefficient as a double-word constant (hi = the float32
+// rounding, lo = the float32 rounding of the remainder).
+template <int n>
+__device__ __forceinline__ dw se3_series_coeff_dw(int which) {
+  constexpr double f[18] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0,
+                            3628800.0, 39916800.0, 479001600.0, 6227020800.0, 87178291200.0,
+                            1307674368000.0, 20922789888000.0, 355687428096000.0};
+  constexpr double s = (n & 1) ? -1.0 : 1.0;
+  constexpr double c[3] = {s / f[2 * n + 1], s / f[2 * n + 2], s / f[2 * n + 3]};
+  constexpr float h0 = (float)c[0], h1 = (float)c[1], h2 = (float)c[2];
+  constexpr float l0 = (float)(c[0] - (double)h0), l1 = (float)(c[1] - (double)h1),
+                  l2 = (float)(c[2] - (double)h2);
+  return which == 0 ? dw{h0, l0} : (which == 1 ? dw{h1, l1} : dw{h2, l2});
+}
+
+// FP64 value -> normalised double-word.
+__device__ __forceinline__ float2 dw_of_double(double x) {
+  const float h = __double2float_rn(x);
+  return make_float2(h, __double2float_rn(x - (double)h));
+}
+
 // One Gauss-Newton update by one warp (all 32 lanes call it).
 //   up: the 21 packed upper-triangle entries of J^T J and bv: J^T r (6),
 //       normalised double-words (hi, lo) in shared memory;
-//   T: the current pose (16, row-major, FP64, shared).
+//   T: the current pose as double-words (16, row-major, shared).
 // Solves J^T J x = J^T r by LDL^T with the failure rule of LAPACK potrf (a
 // pivot that is not > 0, or NaN, fails: the LDL^T pivots are the squares of
 // the Cholesky pivots), one lane per triangle entry and one per right-hand
 // side entry, so that a column step is one product and one difference for
-// all entries.  Then Tn = exp(x) T in FP64.  Returns the verdict (uniform);
-// on success lanes 0..15 hold Tn's entries in tn_out (lane k -> entry k),
-// and every lane holds x rounded to float32 in xs (for the finiteness test).
-__device__ inline bool warp_gn_update(const float2 *up, const float2 *bv, const double *T,
-                                      float *xs, double &tn_out, int lane) {
+// all entries.  Then Tn = exp(x) T, also in double-words: within ~1e-14 of
+// the FP64 update, so the float32 view of the pose (its high words) is
+// that of the FP64 pose.  Returns the verdict (uniform); on success lanes
+// 0..15 hold Tn's entries in tn_out (lane k -> entry k), and every lane
+// holds x rounded to float32 in xs (for the finiteness test).
+__device__ inline bool warp_gn_update(const float2 *up, const float2 *bv, const float2 *T,
+                                      float *xs, float2 &tn_out, int lane) {
   // this lane's entry (i, k); k == 6 marks the right-hand side
   int ei = 0, ek = 0;
   if (lane < 21) {
@@ -290,62 +313,70 @@ __device__ inline bool warp_gn_update(const float2 *up, const float2 *bv, const 
       if (is_rhs && ei < j) v = nv;
     }
   }
-  // x to FP64 (the rhs lane i converts x_i, then every lane gathers all six)
-  const double xd = (double)v.hi + (double)v.lo;
-  double x[6];
+  dw x[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) x[k] = __shfl_sync(0xffffffffu, xd, 21 + k);
-  // exp(x) in FP64 (its rounding decides the float32 pose view of the next
-  // association, which therefore stays that of an FP64 update).  Below
-  // t = 0.5 the coefficients A = sin t / t, B = (1 - cos t) / t^2,
-  // C = (t - sin t) / t^3 are their Maclaurin series in t^2 through t^12
-  // (the first omitted term is below 0.5^14 / 15! < 5e-17), the three
-  // evaluated at once on three lane groups by Horner's rule: 6 FP64
-  // instructions; above, the closed forms.
-  const double wx = x[3], wy = x[4], wz = x[5];
-  const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
-  double A, B, C;
-  if (t2 < 0.25) {
+  for (int k = 0; k < 6; ++k) x[k] = shfl_dw(v, 21 + k);
+  // exp(x).  Below t = 0.5 the coefficients A = sin t / t, B = (1 - cos t) /
+  // t^2, C = (t - sin t) / t^3 are their Maclaurin series in t^2 through
+  // t^12 (the first omitted term is below 0.5^14 / 15! < 5e-17), the three
+  // at once on three lane groups by Horner's rule: the terms from t^8 on in
+  // float32 (each below 6e-16 of its rounding), the rest in double-words.
+  // Above, the FP64 closed forms.
+  const dw wx = x[3], wy = x[4], wz = x[5];
+  const dw t2 = dw_add(dw_add(dw_mul(wx, wx), dw_mul(wy, wy)), dw_mul(wz, wz));
+  dw A, B, C;
+  if (t2.hi < 0.25f) {
     const int which = lane < 10 ? 0 : (lane < 20 ? 1 : 2);
-    double coef = se3_series_coeff<6>(which);
-    coef = fma(coef, t2, se3_series_coeff<5>(which));
-    coef = fma(coef, t2, se3_series_coeff<4>(which));
-    coef = fma(coef, t2, se3_series_coeff<3>(which));
-    coef = fma(coef, t2, se3_series_coeff<2>(which));
-    coef = fma(coef, t2, se3_series_coeff<1>(which));
-    coef = fma(coef, t2, se3_series_coeff<0>(which));
-    A = __shfl_sync(0xffffffffu, coef, 0);
-    B = __shfl_sync(0xffffffffu, coef, 10);
-    C = __shfl_sync(0xffffffffu, coef, 20);
+    const float th = t2.hi;
+    const float tail = __fmaf_rn(__fmaf_rn(se3_series_coeff_dw<6>(which).hi, th,
+                                           se3_series_coeff_dw<5>(which).hi),
+                                 th, se3_series_coeff_dw<4>(which).hi);
+    dw coef = {tail, 0.f};
+    coef = dw_add(dw_mul(coef, t2), se3_series_coeff_dw<3>(which));
+    coef = dw_add(dw_mul(coef, t2), se3_series_coeff_dw<2>(which));
+    coef = dw_add(dw_mul(coef, t2), se3_series_coeff_dw<1>(which));
+    coef = dw_add(dw_mul(coef, t2), se3_series_coeff_dw<0>(which));
+    A = shfl_dw(coef, 0);
+    B = shfl_dw(coef, 10);
+    C = shfl_dw(coef, 20);
   } else {
-    se3_coeffs(t2, A, B, C);
+    double Ad, Bd, Cd;
+    se3_coeffs((double)t2.hi + (double)t2.lo, Ad, Bd, Cd);
+    const float2 a2 = dw_of_double(Ad), b2 = dw_of_double(Bd), c2 = dw_of_double(Cd);
+    A = {a2.x, a2.y};
+    B = {b2.x, b2.y};
+    C = {c2.x, c2.y};
   }
   // lanes 0..8 hold R_ac = I + A W + B W^2, lanes 9..17 V_ac = I + B W + C W^2
   const int e = lane < 9 ? lane : (lane < 18 ? lane - 9 : 0);
   const int ea = e / 3, ec = e % 3;
-  const double wa = ea == 0 ? wx : (ea == 1 ? wy : wz);
-  const double wc = ec == 0 ? wx : (ec == 1 ? wy : wz);
+  const dw wa = ea == 0 ? wx : (ea == 1 ? wy : wz);
+  const dw wc = ec == 0 ? wx : (ec == 1 ? wy : wz);
   // W = hat(w): W_01 = -wz, W_02 = wy, W_10 = wz, W_12 = -wx, W_20 = -wy, W_21 = wx
-  const double Wac = e == 1 ? -wz : e == 2 ? wy : e == 3 ? wz : e == 5 ? -wx : e == 6 ? -wy
-                   : e == 7 ? wx : 0.0;
+  const dw nwx = {-wx.hi, -wx.lo}, nwy = {-wy.hi, -wy.lo}, nwz = {-wz.hi, -wz.lo};
+  const dw zero = {0.f, 0.f};
+  const dw Wac = e == 1 ? nwz : e == 2 ? wy : e == 3 ? wz : e == 5 ? nwx : e == 6 ? nwy
+               : e == 7 ? wx : zero;
   const bool diag = (ea == ec);
-  const double W2ac = fma(wa, wc, diag ? -t2 : 0.0);  // W^2 = w w^T - |w|^2 I
+  const dw ww = dw_mul(wa, wc);
+  const dw W2ac = diag ? dw_add(ww, dw{-t2.hi, -t2.lo}) : ww;  // W^2 = w w^T - |w|^2 I
   const bool isR = lane < 9;
-  const double val = fma(isR ? A : B, Wac, fma(isR ? B : C, W2ac, diag ? 1.0 : 0.0));
+  dw val = dw_add(dw_mul(isR ? A : B, Wac), dw_mul(isR ? B : C, W2ac));
+  if (diag) val = dw_add(val, dw{1.f, 0.f});
   // t_a = sum_c V_ac x_c (V row a on lanes 9 + 3a ...)
-  const double v0 = __shfl_sync(0xffffffffu, val, 9 + 3 * ea),
-               v1 = __shfl_sync(0xffffffffu, val, 10 + 3 * ea),
-               v2 = __shfl_sync(0xffffffffu, val, 11 + 3 * ea);
-  const double ta = fma(v0, x[0], fma(v1, x[1], v2 * x[2]));
+  const dw v0 = shfl_dw(val, 9 + 3 * ea), v1 = shfl_dw(val, 10 + 3 * ea),
+           v2 = shfl_dw(val, 11 + 3 * ea);
+  const dw ta = dw_add(dw_add(dw_mul(v0, x[0]), dw_mul(v1, x[1])), dw_mul(v2, x[2]));
   // Tn = [R t] T: lane q = 4 row + col < 12
   const int row = lane < 12 ? (lane >> 2) : 0, col = lane & 3;
-  const double r0 = __shfl_sync(0xffffffffu, val, 3 * row),
-               r1 = __shfl_sync(0xffffffffu, val, 3 * row + 1),
-               r2 = __shfl_sync(0xffffffffu, val, 3 * row + 2),
-               tr = __shfl_sync(0xffffffffu, ta, 3 * row);
-  double tn = fma(r0, T[col], fma(r1, T[4 + col], fma(r2, T[8 + col], col == 3 ? tr : 0.0)));
-  if (lane >= 12) tn = (lane == 15) ? 1.0 : 0.0;
-  tn_out = tn;
+  const dw r0 = shfl_dw(val, 3 * row), r1 = shfl_dw(val, 3 * row + 1),
+           r2 = shfl_dw(val, 3 * row + 2), tr = shfl_dw(ta, 3 * row);
+  const float2 T0 = T[col], T1 = T[4 + col], T2 = T[8 + col];
+  dw tn = dw_add(dw_add(dw_mul(r0, dw{T0.x, T0.y}), dw_mul(r1, dw{T1.x, T1.y})),
+                 dw_mul(r2, dw{T2.x, T2.y}));
+  if (col == 3) tn = dw_add(tn, tr);
+  if (lane >= 12) tn = {(lane == 15) ? 1.f : 0.f, 0.f};
+  tn_out = make_float2(tn.hi, tn.lo);
   return true;
 }
 

@@ -697,8 +697,12 @@ __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const dou
   const double count = q.use_geom ? fmax(cg, cf) : cf;
   double *H = a.history ? a.history + ((size_t)p * a.total_iters + s) * STB_HIST_SIZE : nullptr;
   float xs[6];
-  double tn;
-  const bool ok = warp_gn_update(totw, totw + kJrB, T, xs, tn, lane);
+  __shared__ float2 s_tw[16];
+  if (lane < 16) s_tw[lane] = dw_of_double(T[lane]);
+  __syncwarp();
+  float2 tnw;
+  const bool ok = warp_gn_update(totw, totw + kJrB, s_tw, xs, tnw, lane);
+  const double tn = (double)tnw.x + (double)tnw.y;
   double *R = a.results + (size_t)p * STB_RES_SIZE;
   for (int k = lane; k < 36; k += 32) {
     const int r = k / 6, c = k % 6;

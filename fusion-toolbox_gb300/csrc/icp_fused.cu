@@ -53,9 +53,9 @@ constexpr unsigned long long kMaxSources = 1ull << 24;
 constexpr int kJr = 21, kR2 = 27, kCountGeom = 28, kCountFeat = 29;
 
 struct State {
-  double T[16];  // current pose, FP64
-  Pose32 pose;   // its float32 view + intrinsics
-  double last_r2, last_count;  // of the last successful step (residual = r2 / count)
+  float2 Tw[16];  // current pose as double-words (within ~1e-14 of FP64)
+  Pose32 pose;    // its float32 view (the high words) + intrinsics
+  float2 last_tot[32];  // totals (double-words) of the last successful step
   unsigned ticket;
   unsigned stopped;
   unsigned status;
@@ -145,20 +145,20 @@ __global__ void k_begin(Job job, Job *dst) {
   if (threadIdx.x != 0) return;
   *dst = job;
   State *S = job.state;
+  double T[16];
   for (int k = 0; k < 16; ++k)
-    S->T[k] = job.init ? job.init[k]
-                       : (job.has_init_v ? job.init_v[k] : ((k % 5) == 0 ? 1.0 : 0.0));
+    T[k] = job.init ? job.init[k]
+                    : (job.has_init_v ? job.init_v[k] : ((k % 5) == 0 ? 1.0 : 0.0));
   S->pose.fx = job.kcam ? job.kcam[0] : job.kcam_v[0];
   S->pose.cx = job.kcam ? job.kcam[2] : job.kcam_v[1];
   S->pose.fy = job.kcam ? job.kcam[4] : job.kcam_v[2];
   S->pose.cy = job.kcam ? job.kcam[5] : job.kcam_v[3];
-  refresh_pose32(S->pose, S->T);
+  refresh_pose32(S->pose, T);
+  for (int k = 0; k < 16; ++k) S->Tw[k] = dw_of_double(T[k]);
   S->ticket = 0;
   S->stopped = 0;
   S->status = 0;
   S->iters_done = 0;
-  S->last_r2 = 0.0;
-  S->last_count = 0.0;
   for (int k = 0; k < STB_RES_SIZE; ++k) job.result[k] = 0.0;
   job.result[STB_RES_RESIDUAL] = INFINITY;
 }
@@ -300,8 +300,8 @@ __device__ __forceinline__ bool publish_slot(const float2 *bsum, float2 *part, u
   return true;
 }
 
-// Last block: totals of kN accumulators from all block slots, in FP64 and
-// (when totw is given) as double-words for the step.  Warp w
+// Last block: totals of kN accumulators from all block slots, in FP64 (when
+// tot is given) and as double-words (when totw is given).  Warp w
 // folds slots w, w + 8, ... with lane = accumulator; every load of a round
 // (kFoldLoads slots) is issued before its additions, so 300 slots cost two
 // L2 round trips.  The eight warp results are merged through shared memory.
@@ -330,7 +330,7 @@ __device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, dou
     CSum u = {0.f, 0.f};
 #pragma unroll
     for (int w = 0; w < kW; ++w) csum_merge(u, wsum[w][threadIdx.x].x, wsum[w][threadIdx.x].y);
-    tot[threadIdx.x] = (double)u.s + (double)u.c;
+    if (tot) tot[threadIdx.x] = (double)u.s + (double)u.c;
     if (totw) totw[threadIdx.x] = dw_of_csum(u.s, u.c);
   }
   __syncthreads();
@@ -340,89 +340,93 @@ __device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, dou
 // then finds it in shared memory instead of paying an L2 round trip in the
 // serial tail).
 struct StateView {
-  double T[16];
+  float2 Tw[16];
   unsigned status;
   int iters_done;
 };
 
 __device__ __forceinline__ void load_state_view(StateView &V, const State *S) {
-  if (threadIdx.x < 16) V.T[threadIdx.x] = S->T[threadIdx.x];
+  if (threadIdx.x < 16) V.Tw[threadIdx.x] = S->Tw[threadIdx.x];
   if (threadIdx.x == 16) V.status = S->status;
   if (threadIdx.x == 17) V.iters_done = S->iters_done;
 }
 
-// One Gauss-Newton step from the totals in shared memory, by one warp
-// (warp_gn_update of gn_solve.cuh, on their double-words; the FP64 copies go
-// to the result and the history).  The residual r2 / count is stored for the
-// information pass to divide.
-__device__ void gn_step_warp(const Job *J, const StateView &V, const double *tot,
-                             const float2 *totw, int iter) {
+// One Gauss-Newton step from the totals in shared memory, by warp 0 of the
+// last block: the solve on the double-words (warp_gn_update of
+// gn_solve.cuh), then what the next kernel reads (the pose as double-words
+// and as a float32 view with its normal matrix, the status, the stop flag,
+// the iteration count) and the totals of a successful step for the result.
+// No FP64 instruction is on this path: the FP64 result block is written
+// once per registration by the information pass.  When a history is
+// recorded, warp 1 writes this iteration's FP64 record meanwhile and, after
+// the verdict (named barrier 1), its pose.
+__device__ void gn_step(const Job *J, const StateView &V, const float2 *totw, int iter) {
   __shared__ float rt32[12];
+  __shared__ float2 s_tn[16];
+  __shared__ int s_ok;
+  __shared__ double s_tot[kAccs];
   const int lane = threadIdx.x & 31;
   State *S = J->state;
-  const double cg = tot[kCountGeom], cf = tot[kCountFeat];
-  const double count = J->use_geom ? fmax(cg, cf) : cf;
   double *H = J->history ? J->history + (size_t)iter * STB_HIST_SIZE : nullptr;
-  float xs[6];
-  double tn;
-  const bool ok = warp_gn_update(totw, totw + kJr, V.T, xs, tn, lane);
-  double *R = J->result;
-  for (int k = lane; k < 36; k += 32) {
-    const int r = k / 6, c = k % 6;
-    const double a = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
-    if (H) H[STB_HIST_JTJ + k] = a;
-    if (ok) R[STB_RES_JTJ + k] = a;
-  }
-  if (H && lane < 6) H[STB_HIST_JR + lane] = tot[kJr + lane];
-  if (!ok) {
-    if (lane == 0) {
-      unsigned st = V.status | STB_ST_NOT_PD;
-      if (count == 0.0) st |= STB_ST_NO_MATCHES;
-      S->status = st;
-      S->stopped = 1;
-      R[STB_RES_STATUS] = (double)st;
-      if (H) {
-        H[STB_HIST_R2] = tot[kR2];
-        H[STB_HIST_GEOM_COUNT] = cg;
-        H[STB_HIST_FEAT_COUNT] = cf;
-        H[STB_HIST_OK] = 0.0;
+  if (threadIdx.x < 32) {
+    float xs[6];
+    float2 tn;
+    const bool ok = warp_gn_update(totw, totw + kJr, V.Tw, xs, tn, lane);
+    // count == 0 on the high words (counts are non-negative)
+    const float cg = totw[kCountGeom].x, cf = totw[kCountFeat].x;
+    const bool no_match = (J->use_geom ? fmaxf(cg, cf) : cf) == 0.f;
+    if (ok) {
+      if (lane < 16) {
+        s_tn[lane] = tn;
+        S->Tw[lane] = tn;
       }
+      if (lane < 12) {
+        rt32[lane] = tn.x;  // the float32 rounding of the pose entry
+        S->pose.rt[lane] = tn.x;
+      }
+      if (lane < kAccs) S->last_tot[lane] = totw[lane];
+      __syncwarp();
     }
+    if (lane == 0) {
+      unsigned st = V.status;
+      if (!ok) {
+        st |= STB_ST_NOT_PD;
+        S->stopped = 1;
+      } else {
+        bool finite = true;
+        for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
+        if (!finite) st |= STB_ST_NAN;
+        float nm[9];
+        inverse_transpose(rt32, nm);
+        for (int k = 0; k < 9; ++k) S->pose.nm[k] = nm[k];
+        S->iters_done = V.iters_done + 1;
+      }
+      if (no_match) st |= STB_ST_NO_MATCHES;
+      S->status = st;
+      s_ok = ok;
+    }
+    if (H) asm volatile("bar.sync 1, 64;" ::: "memory");
     return;
   }
-  if (lane < 12) {
-    rt32[lane] = __double2float_rn(tn);
-    S->pose.rt[lane] = rt32[lane];
-  }
-  if (lane < 16) {
-    S->T[lane] = tn;
-    R[STB_RES_TRANSFORM + lane] = tn;
-    if (H) H[STB_HIST_TRANSFORM + lane] = tn;
-  }
+  if (!H) return;
+  // warp 1: the FP64 history record (exact conversions: a normalised
+  // double-word has at most 49 significant bits)
+  if (lane < kAccs) s_tot[lane] = (double)totw[lane].x + (double)totw[lane].y;
   __syncwarp();
-  if (lane == 0) {
-    unsigned st = V.status;
-    bool finite = true;
-    for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
-    if (!finite) st |= STB_ST_NAN;
-    if (count == 0.0) st |= STB_ST_NO_MATCHES;
-    S->status = st;
-    float nm[9];
-    inverse_transpose(rt32, nm);
-    for (int k = 0; k < 9; ++k) S->pose.nm[k] = nm[k];
-    S->iters_done = V.iters_done + 1;
-    S->last_r2 = tot[kR2];
-    S->last_count = count;
-    R[STB_RES_MATCHES] = count;
-    R[STB_RES_ITERS] = (double)(V.iters_done + 1);
-    R[STB_RES_STATUS] = (double)st;
-    if (H) {
-      H[STB_HIST_R2] = tot[kR2];
-      H[STB_HIST_GEOM_COUNT] = cg;
-      H[STB_HIST_FEAT_COUNT] = cf;
-      H[STB_HIST_OK] = 1.0;
-    }
+  for (int k = lane; k < 36; k += 32) {
+    const int r = k / 6, c = k % 6;
+    H[STB_HIST_JTJ + k] = s_tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
   }
+  if (lane < 6) H[STB_HIST_JR + lane] = s_tot[kJr + lane];
+  if (lane == 0) {
+    H[STB_HIST_R2] = s_tot[kR2];
+    H[STB_HIST_GEOM_COUNT] = s_tot[kCountGeom];
+    H[STB_HIST_FEAT_COUNT] = s_tot[kCountFeat];
+  }
+  asm volatile("bar.sync 1, 64;" ::: "memory");
+  const bool ok = s_ok;
+  if (lane == 0) H[STB_HIST_OK] = ok ? 1.0 : 0.0;
+  if (ok && lane < 16) H[STB_HIST_TRANSFORM + lane] = (double)s_tn[lane].x + (double)s_tn[lane].y;
 }
 
 // Pixels of one thread per round of the reduction loop; all their loads
@@ -441,7 +445,6 @@ __global__ void __launch_bounds__(kT) k_reduce(const Job *__restrict__ J, int ep
   float(*red)[kT] = reinterpret_cast<float(*)[kT]>(s_red);
   __shared__ float2 bsum[kAccs];
   __shared__ int is_last;
-  __shared__ double tot[kAccs];
   __shared__ float2 totw[kAccs];
   State *S = J->state;
   grid_dependency_wait();  // the association has written the key map
@@ -524,10 +527,10 @@ __global__ void __launch_bounds__(kT) k_reduce(const Job *__restrict__ J, int ep
 
   block_reduce<kAccs, kT>(acc, red, bsum);
   if (!publish_slot<kAccs>(bsum, J->part, &S->ticket, &is_last)) return;
-  grid_totals<kAccs, kT>(J->part, gridDim.x, tot, totw);
-  if (threadIdx.x < 32) {
+  grid_totals<kAccs, kT>(J->part, gridDim.x, nullptr, totw);
+  if (threadIdx.x < 64) {
     if (threadIdx.x == 0) S->ticket = 0;
-    gn_step_warp(J, V, tot, totw, epoch);
+    gn_step(J, V, totw, epoch);
   }
 }
 
@@ -570,10 +573,30 @@ __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__
     const int r = k / 6, c = k % 6;
     R[STB_RES_INFO + k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
   }
+  // the result of the last successful step (its pose, J^T J, match count,
+  // residual r2 / count, icp.py:249-253), once per registration
+  const int done = S->iters_done;
+  if (done > 0) {
+    for (int k = threadIdx.x; k < 36; k += blockDim.x) {
+      const int r = k / 6, c = k % 6;
+      const float2 a = S->last_tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
+      R[STB_RES_JTJ + k] = (double)a.x + (double)a.y;
+    }
+    if (threadIdx.x < 16)
+      R[STB_RES_TRANSFORM + threadIdx.x] =
+          (double)S->Tw[threadIdx.x].x + (double)S->Tw[threadIdx.x].y;
+  }
   if (threadIdx.x == 0) {
     S->ticket = 0;
-    // the residual of the last successful step, r2 / count (icp.py:251)
-    if (S->iters_done > 0) R[STB_RES_RESIDUAL] = S->last_r2 / S->last_count;
+    if (done > 0) {
+      const float2 g = S->last_tot[kCountGeom], f = S->last_tot[kCountFeat],
+                   r2 = S->last_tot[kR2];
+      const double cg = (double)g.x + (double)g.y, cf = (double)f.x + (double)f.y;
+      const double count = J->use_geom ? fmax(cg, cf) : cf;
+      R[STB_RES_MATCHES] = count;
+      R[STB_RES_ITERS] = (double)done;
+      R[STB_RES_RESIDUAL] = ((double)r2.x + (double)r2.y) / count;
+    }
     R[STB_RES_STATUS] = (double)S->status;
   }
 }
