@@ -27,7 +27,10 @@ Secondary workloads (rank 0, N = 1, reported under "secondary"; skip with
       4 levels [10, 8, 5, 3], weights geometric 10 / feature 1 (the
       reference preset), BatchRegistration vs the plain path;
   bilateral_depth_filter     the depth bilateral filter on uint16 depth,
-      640x480 and 1920x1080, widths 6 and 13.
+      640x480 and 1920x1080, widths 6 and 13;
+  autograd_layer             ExpRtToMatrix forward + backward (1 M twists),
+      the frame point-cloud matcher forward + backward (640x480, 3
+      channels), one AutogradICP registration (320x240).
 
 Under torchrun each rank registers its own pair (seeded by rank), no
 collective touches the data path (weak scaling); a barrier and a max over
@@ -543,6 +546,84 @@ def secondary_bilateral(device, seed, reps=200):
     return out
 
 
+def secondary_autograd(device, seed, reps=50):
+    """The differentiable registration layer: ExpRtToMatrix forward +
+    backward on 1 M twists, the frame point-cloud matcher forward + backward
+    on a 640x480 pair (3 feature channels; the forward includes its
+    correspondence map), and one AutogradICP registration (depth only, 20
+    BFGS iterations and 100 SGD steps, 320x240).  CUDA events for the
+    kernels, wall clock for the optimiser (host-driven, as the
+    reference's)."""
+    import numpy as np
+    import torch
+    from slamtb_gb300 import synthetic
+    from slamtb_gb300.frame import Frame, FrameInfo, FramePointCloud, KCamera
+    from slamtb_gb300.registration import AutogradICP, ExpRtToMatrix
+    from slamtb_gb300.spatial import FPCLMatcherOp
+    st = torch.cuda.current_stream(device)
+
+    def ev_time(fn, n):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        e0.record(st)
+        for _ in range(n):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize(device)
+        return e0.elapsed_time(e1) * 1e-3 / n
+
+    rng = np.random.default_rng(seed)
+    x = torch.from_numpy(rng.normal(size=(1 << 20, 6)).astype(np.float32) * 0.3).to(device)
+    x.requires_grad_(True)
+    g = torch.randn(1 << 20, 3, 4, device=device)
+
+    def exp_fb():
+        ExpRtToMatrix.apply(x).backward(g)
+    t_exp = ev_time(exp_fb, reps)
+    p = synthetic.make_pair(seed + 5000, width=W, height=H, feature_channels=3)
+    k = KCamera(p["kcam"])
+    src = FramePointCloud.from_frame(Frame(FrameInfo(k), p["source_depth"]), device)
+    tgt = FramePointCloud.from_frame(Frame(FrameInfo(k), p["target_depth"]), device)
+    gt = torch.from_numpy(p["gt"]).float().to(device)
+    m = src.mask.reshape(-1)
+    sp = (src.points.reshape(-1, 3)[m] @ gt[:3, :3].T + gt[:3, 3]).contiguous()
+    sn = (src.normals.reshape(-1, 3)[m] @ gt[:3, :3].T).contiguous()
+    target = FPCLMatcherOp.Target(tgt.points, tgt.normals, tgt.mask,
+                                  torch.from_numpy(p["target_feats"]).to(device), k, DIST,
+                                  math.radians(30))
+    spg = sp.clone().requires_grad_(True)
+    dl = torch.randn(3, sp.size(0), device=device)
+
+    def match_fb():
+        FPCLMatcherOp.apply(spg, sn, target, FPCLMatcherOp.Match()).backward(dl)
+    t_match = ev_time(match_fb, reps)
+    p2 = synthetic.make_pair(seed + 5001, width=320, height=240, max_rot_deg=2.0,
+                             max_trans=0.02)
+    k2 = KCamera(p2["kcam"])
+    s2 = FramePointCloud.from_frame(Frame(FrameInfo(k2), p2["source_depth"]), device)
+    t2 = FramePointCloud.from_frame(Frame(FrameInfo(k2), p2["target_depth"]), device)
+    icp = AutogradICP(20, geom_weight=1.0, feat_weight=0.0, distance_threshold=DIST,
+                      normals_angle_thresh=math.radians(30))
+    args2 = (k2, s2.points.reshape(-1, 3), s2.normals.reshape(-1, 3), s2.mask.reshape(-1))
+    kw2 = dict(target_points=t2.points, target_mask=t2.mask, target_normals=t2.normals)
+    icp.estimate(*args2, **kw2)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    res = icp.estimate(*args2, **kw2)
+    t_agicp = time.perf_counter() - t0
+    return {"workload": "differentiable registration layer (AutogradICP)",
+            "exp_rt_to_matrix_fwd_bwd": {"twists": 1 << 20, "us": t_exp * 1e6,
+                                         "mtwists_per_s": (1 << 20) / t_exp / 1e6},
+            "fpcl_matcher_fwd_bwd_640x480": {"points": int(sp.size(0)), "channels": 3,
+                                            "us": t_match * 1e6,
+                                            "mpoints_per_s": sp.size(0) / t_match / 1e6},
+            "autograd_icp_320x240": {"seconds": t_agicp, "bfgs_iters": 20, "sgd_steps": 100,
+                                     "rel_pose_err_vs_ground_truth": _rel_pose(
+                                         res.transform.numpy(), p2["gt"])}}
+
+
 def profile_case(args, device):
     """A small case of one secondary workload, --steps runs after --warmup,
     for profiler captures (prints one JSON line; not a bench result)."""
@@ -600,7 +681,8 @@ def run_secondary(device, seed):
                      ("loss_grad_32x640x480", secondary_loss),
                      ("batch_uneven_256", secondary_batch_uneven),
                      ("feature_1080p_16ch_bf16", secondary_feature_1080p),
-                     ("bilateral_depth_filter", secondary_bilateral)):
+                     ("bilateral_depth_filter", secondary_bilateral),
+                     ("autograd_layer", secondary_autograd)):
         t = time.perf_counter()
         try:
             out[name] = fn(device, seed)
