@@ -456,24 +456,35 @@ __device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *o
 // ---------------------------------------------------------------------------
 // phase A: association of one source tile
 // ---------------------------------------------------------------------------
-constexpr int kChunk = 4;   // pixels per thread per pipelined reduction chunk
-constexpr int kChunkA = 4;  // points per thread per pipelined association chunk
+// Pixels per thread of a staged sub-chunk (kCh, a template parameter of
+// the tile functions) and blocks per SM of the kernel.  The geometric-only
+// kernel runs 3 blocks of 256 threads per SM (80 registers, 3-pixel
+// sub-chunks whose two 24 KB stages fit three blocks' shared memory): 24
+// warps instead of 16 hide more of the gathers' latency, and the 256-pair
+// run took 29.5 ms instead of 32.6.  With a feature term the spills at 80
+// registers would cost more than the warps gain, so those kernels keep 2
+// blocks of 128 registers and 4-pixel sub-chunks.
+template <bool kFeat>
+struct BatchShape {
+  static constexpr int kCh = kFeat ? 4 : 3;
+  static constexpr int kBlocksPerSM = kFeat ? 2 : 3;
+};
 
 // ---------------------------------------------------------------------------
 // Bulk-copy staging of a tile's contiguous streams.  A tile is walked in
-// sub-chunks of kSub pixels; each sub-chunk's streams (reduction: keys,
+// sub-chunks of kThreads * kCh pixels; each sub-chunk's streams (reduction: keys,
 // target points, target normals; association: source points, normals,
 // mask) are copied into one of two shared-memory stages by cp.async.bulk
 // (issued by thread 0, completion counted on the stage's mbarrier) while the
-// block computes on the other stage.  This keeps ~32 KB per block in flight
+// block computes on the other stage.  This keeps a stage per block in flight
 // independently of occupancy; only the true gathers (winners' source points,
 // projected target pixels, feature taps) remain per-thread loads.
 // A stream whose base is not 16-byte aligned, and the bytes of a stream past
 // its last 16-byte multiple, are copied by the threads with plain loads.
 // ---------------------------------------------------------------------------
-constexpr int kSub = kThreads * kChunk;  // pixels per staged sub-chunk (1024)
-constexpr int kStageBytes = kSub * 32;   // keys 8 + xyz 12 + normal 12 per pixel
-constexpr int kStageSmem = 2 * kStageBytes;
+// a stage holds one sub-chunk of kThreads * kCh pixels at 32 bytes per pixel
+// (keys 8 + xyz 12 + normal 12)
+__host__ __device__ constexpr int stage_bytes(int kCh) { return kThreads * kCh * 32; }
 
 struct StageCtl {
   unsigned long long bar[2];  // mbarriers of the two stages
@@ -489,7 +500,10 @@ struct StageStream {
 
 extern __shared__ __align__(128) unsigned char s_stage[];
 
-__device__ __forceinline__ unsigned char *stage_buf(int st) { return s_stage + st * kStageBytes; }
+template <int kCh>
+__device__ __forceinline__ unsigned char *stage_buf(int st) {
+  return s_stage + st * stage_bytes(kCh);
+}
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -607,9 +621,11 @@ __device__ __forceinline__ void stage_pipeline(int nsub, StageCtl &ctl, unsigned
   }
 }
 
+template <int kCh>
 __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *off, int level,
                                            long long t, int s, bool force, TileCache &tc,
                                            StageCtl &ctl, unsigned &ph) {
+  constexpr int kSub = kThreads * kCh;  // pixels of a staged sub-chunk
   const int p = cache_pair(a, off, level, t, !force, tc);
   if (tc.skip) return;
   const Pose32 &P = tc.P;
@@ -627,7 +643,7 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
   auto issue = [&](int c) {
     const long long b0 = start + (long long)c * kSub;
     const unsigned n = (unsigned)min((long long)kSub, end - b0);
-    unsigned char *buf = stage_buf(c & 1);
+    unsigned char *buf = stage_buf<kCh>(c & 1);
     const StageStream ss[3] = {{buf, lv.src_points + 3 * b0, 12u * n, 4},
                                {buf + kSub * 12, lv.src_normals + 3 * b0, 12u * n, 4},
                                {buf + kSub * 24, lv.src_mask + b0, n, 1}};
@@ -636,16 +652,16 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
   auto compute = [&](int c, int st) {
     const long long b0 = start + (long long)c * kSub;
     const int n = (int)min((long long)kSub, end - b0);
-    const float *sp = reinterpret_cast<const float *>(stage_buf(st));
+    const float *sp = reinterpret_cast<const float *>(stage_buf<kCh>(st));
     const float *sn = sp + kSub * 3;
-    const unsigned char *sm = stage_buf(st) + kSub * 24;
+    const unsigned char *sm = stage_buf<kCh>(st) + kSub * 24;
     // round 1: projection and target gathers
-    float3 Tp[kChunkA];
-    long long pix[kChunkA];
-    bool ok[kChunkA];
-    float qx[kChunkA], qy[kChunkA], qz[kChunkA], mx[kChunkA], my[kChunkA], mz[kChunkA];
+    float3 Tp[kCh];
+    long long pix[kCh];
+    bool ok[kCh];
+    float qx[kCh], qy[kCh], qz[kCh], mx[kCh], my[kCh], mz[kCh];
 #pragma unroll
-    for (int k = 0; k < kChunkA; ++k) {
+    for (int k = 0; k < kCh; ++k) {
       const int j = k * kThreads + threadIdx.x;
       ok[k] = j < n && sm[j < n ? j : 0];
       const int jj = ok[k] ? j : 0;
@@ -665,7 +681,7 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
     }
     // round 2: gates and the z-buffer
 #pragma unroll
-    for (int k = 0; k < kChunkA; ++k) {
+    for (int k = 0; k < kCh; ++k) {
       if (!ok[k]) continue;
       const int j = k * kThreads + threadIdx.x;
       const float dx = fsub(qx[k], Tp[k].x), dy = fsub(qy[k], Tp[k].y),
@@ -764,11 +780,12 @@ __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const dou
 // ---------------------------------------------------------------------------
 // phase B: reduction of one target tile (+ group / pair folds and the step)
 // ---------------------------------------------------------------------------
-template <typename FT, bool kFeat, bool kInfo, bool kHWC>
+template <typename FT, bool kFeat, bool kInfo, bool kHWC, int kCh>
 __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long *off, int level,
                                             long long t, int s, TileCache &tc, StageCtl &ctl,
                                             unsigned &ph) {
   constexpr int kN = kInfo ? 21 : kAccsB;
+  constexpr int kSub = kThreads * kCh;  // pixels of a staged sub-chunk
   __shared__ int s_last;
   __shared__ float bs[32], bc[32];
   __shared__ double tot[32];
@@ -800,7 +817,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   auto issue = [&](int c) {
     const long long b0 = start + (long long)c * kSub;
     const unsigned n = (unsigned)min((long long)kSub, end - b0);
-    unsigned char *buf = stage_buf(c & 1);
+    unsigned char *buf = stage_buf<kCh>(c & 1);
     const StageStream ss[3] = {{buf, keys + b0, 8u * n, 8},
                                {buf + kSub * 8, lv.tgt_points + 3 * b0, 12u * n, 4},
                                {buf + kSub * 20, lv.tgt_normals + 3 * b0, need_n ? 12u * n : 0u, 4}};
@@ -809,14 +826,14 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   auto compute = [&](int c, int st) {
     const long long b0 = start + (long long)c * kSub;
     const int nn = (int)min((long long)kSub, end - b0);
-    const unsigned long long *skeys = reinterpret_cast<const unsigned long long *>(stage_buf(st));
-    const float *stq = reinterpret_cast<const float *>(stage_buf(st) + kSub * 8);
-    const float *stn = reinterpret_cast<const float *>(stage_buf(st) + kSub * 20);
+    const unsigned long long *skeys = reinterpret_cast<const unsigned long long *>(stage_buf<kCh>(st));
+    const float *stq = reinterpret_cast<const float *>(stage_buf<kCh>(st) + kSub * 8);
+    const float *stn = reinterpret_cast<const float *>(stage_buf<kCh>(st) + kSub * 20);
     // round 1: the winners' source points (the gathers that remain)
-    unsigned long long key[kChunk];
-    float spt[kChunk][3];
+    unsigned long long key[kCh];
+    float spt[kCh][3];
 #pragma unroll
-    for (int k = 0; k < kChunk; ++k) {
+    for (int k = 0; k < kCh; ++k) {
       const int j = k * kThreads + threadIdx.x;
       key[k] = j < nn ? skeys[j] : 0ull;
       const bool m = (unsigned)(key[k] >> 56) == tag;
@@ -826,7 +843,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
     }
     // round 2: residuals, Jacobians and the per-thread sums
 #pragma unroll
-    for (int k = 0; k < kChunk; ++k) {
+    for (int k = 0; k < kCh; ++k) {
       if ((unsigned)(key[k] >> 56) != tag) continue;
       const int j = k * kThreads + threadIdx.x;
       const float qx = stq[3 * j], qy = stq[3 * j + 1], qz = stq[3 * j + 2];
@@ -935,7 +952,9 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
 }
 
 template <typename FT, bool kFeat, bool kHWC>
-__global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
+__global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
+    k_batch(const BatchArgs args) {
+  constexpr int kCh = BatchShape<kFeat>::kCh;
   // the argument block is staged in shared memory so that device functions
   // can take it by reference without a per-thread local copy
   __shared__ BatchArgs a;
@@ -1007,13 +1026,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
       const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
       reset_cache(tc);
       for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
-        assoc_tile(a, off, level, t, s, false, tc, ctl, ph);
+        assoc_tile<kCh>(a, off, level, t, s, false, tc, ctl, ph);
       });
       if (!grid_sync(a.sync)) return;
       off = stage_offsets(a.tgt_off + row, a.B, s_off);
       reset_cache(tc);
       for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
-        reduce_tile<FT, kFeat, false, kHWC>(a, off, level, t, s, tc, ctl, ph);
+        reduce_tile<FT, kFeat, false, kHWC, kCh>(a, off, level, t, s, tc, ctl, ph);
       });
       if (!grid_sync(a.sync)) return;
     }
@@ -1026,13 +1045,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_batch(const BatchArgs args) {
   const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
   reset_cache(tc);
   for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
-    assoc_tile(a, off, level, t, s, true, tc, ctl, ph);
+    assoc_tile<kCh>(a, off, level, t, s, true, tc, ctl, ph);
   });
   if (!grid_sync(a.sync)) return;
   off = stage_offsets(a.tgt_off + row, a.B, s_off);
   reset_cache(tc);
   for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
-    reduce_tile<FT, false, true, false>(a, off, level, t, s, tc, ctl, ph);
+    reduce_tile<FT, false, true, false, kCh>(a, off, level, t, s, tc, ctl, ph);
   });
 }
 
@@ -1054,6 +1073,7 @@ int launch_batch(const BatchArgs &args, cudaStream_t st) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  constexpr int kStageSmem = 2 * stage_bytes(BatchShape<kFeat>::kCh);
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageSmem) !=
       cudaSuccess)
     return check_launch("cudaFuncSetAttribute");
