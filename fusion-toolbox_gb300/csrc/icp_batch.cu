@@ -457,16 +457,18 @@ __device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *o
 // phase A: association of one source tile
 // ---------------------------------------------------------------------------
 // Pixels per thread of a staged sub-chunk (kCh, a template parameter of
-// the tile functions) and blocks per SM of the kernel.  The geometric-only
-// kernel runs 3 blocks of 256 threads per SM (80 registers, 3-pixel
-// sub-chunks whose two 24 KB stages fit three blocks' shared memory): 24
-// warps instead of 16 hide more of the gathers' latency, and the 256-pair
-// run took 29.5 ms instead of 32.6.  With a feature term the spills at 80
-// registers would cost more than the warps gain, so those kernels keep 2
-// blocks of 128 registers and 4-pixel sub-chunks.
+// the tile functions) and blocks per SM of the kernel, measured on GB300:
+//   * geometric only: 3 blocks of 256 threads per SM (80 registers, 3-pixel
+//     sub-chunks whose two 24 KB stages fit three blocks' shared memory).
+//     24 warps instead of 16 hide more of the gathers' latency: the
+//     256-pair run took 29.5 ms instead of 32.6 (2 blocks, 4 pixels).
+//   * with a feature term: 2 blocks of 128 registers and 2-pixel sub-chunks.
+//     Three blocks at 80 registers spill enough to lose (16 x 1080p: 264
+//     pairs/s against 382); 2-pixel sub-chunks spill less than 4-pixel ones
+//     (16 x 1080p: 409 pairs/s against 382).
 template <bool kFeat>
 struct BatchShape {
-  static constexpr int kCh = kFeat ? 4 : 3;
+  static constexpr int kCh = kFeat ? 2 : 3;
   static constexpr int kBlocksPerSM = kFeat ? 2 : 3;
 };
 
