@@ -58,6 +58,8 @@ ITERS = 10
 DIST = 0.1
 ANGLE = math.radians(20.0)
 W, H = 640, 480
+WORKLOAD = ("plain geometric point-to-plane ICP, 1 frame pair 640x480 per rank, "
+            "10 GN iterations, d=0.1 m, 20 deg")
 # Algorithmic bytes per pixel of the level per launch (packed element sizes):
 # association = source xyz + normal + mask (25) + gathered target xyz +
 # normal + mask (25) + correspondence-map init and update (16);
@@ -216,7 +218,7 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "plain geometric ICP, 1 pair 640x480, 10 GN iterations",
+        "config": {"workload": WORKLOAD,
                    "iters_per_step": iters},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
@@ -877,8 +879,7 @@ def main():
             "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "plain geometric point-to-plane ICP, 1 frame pair "
-                                   "640x480 per rank, 10 GN iterations, d=0.1 m, 20 deg",
+            "config": {"workload": WORKLOAD,
                        "l2": "flushed (512 MB write) before every step; the pair "
                              "(~18 MB) stays L2-resident across its 10 iterations",
                        "graph": "CUDA graph per registration"},
