@@ -80,6 +80,7 @@ struct BatchArgs {
   float *tile_part, *grp_part;
   unsigned long long *keys;
   long long keys_cap, tiles_cap, groups_cap;
+  int off_cap;  // offset-row entries staged in shared memory (0: read from L2)
 };
 
 __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -200,20 +201,23 @@ __device__ __forceinline__ void for_each_tile(unsigned *sync, int phase, long lo
   }
 }
 
-constexpr int kStageOff = 1025;  // offsets staged in shared memory up to 1024 pairs
+// An offset row (B + 1 entries) is staged in the dynamic shared memory after
+// the two stages when the launch has room for it without losing a block per
+// SM (a.off_cap >= B + 1, decided on the host); otherwise it is read from L2.
 
-// Entry k of an offset row: a plain (shared-memory) load when the row was
-// staged, an L2 load (coherent with other blocks' writes) when it was not.
-__device__ __forceinline__ long long off_at(const long long *off, int B, long long k) {
-  return (B + 1 <= kStageOff) ? off[k] : __ldcg(off + k);
+// Entry k of an offset row: a shared-memory load when the row was staged,
+// an L2 load (coherent with other blocks' writes) when it was not.
+__device__ __forceinline__ long long off_at(const long long *off, const BatchArgs &a,
+                                            long long k) {
+  return (a.B + 1 <= a.off_cap) ? off[k] : __ldcg(off + k);
 }
 
 // Pair owning work item t: off[lo] <= t < off[lo + 1].
-__device__ __forceinline__ int find_pair(const long long *off, int B, long long t) {
-  int lo = 0, hi = B;
+__device__ __forceinline__ int find_pair(const long long *off, const BatchArgs &a, long long t) {
+  int lo = 0, hi = a.B;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
-    if (off_at(off, B, mid) <= t)
+    if (off_at(off, a, mid) <= t)
       lo = mid;
     else
       hi = mid;
@@ -223,11 +227,11 @@ __device__ __forceinline__ int find_pair(const long long *off, int B, long long 
 
 // Copies one level's offset row to shared memory (when it fits) and returns
 // the array the phase should search.
-__device__ __forceinline__ const long long *stage_offsets(const long long *row, int B,
-                                                          long long *smem) {
+__device__ __forceinline__ const long long *stage_offsets(const long long *row,
+                                                          const BatchArgs &a, long long *smem) {
   __syncthreads();
-  if (B + 1 > kStageOff) return row;
-  for (int k = threadIdx.x; k <= B; k += blockDim.x) smem[k] = __ldcg(row + k);
+  if (a.B + 1 > a.off_cap) return row;
+  for (int k = threadIdx.x; k <= a.B; k += blockDim.x) smem[k] = __ldcg(row + k);
   __syncthreads();
   return smem;
 }
@@ -345,10 +349,16 @@ __device__ __forceinline__ void acc_se3(float *acc, const float *Jv, float r, fl
   for (int a = 0; a < 6; ++a) acc[kJrB + a] += w1 * (Jv[a] * r);
 }
 
+// Dynamic shared memory of the kernel: two staging buffers, then the staged
+// offset row.  Between a tile's pipeline and the next tile's first copy the
+// staging buffers are idle: the block sum and the slot folds of the tile's
+// epilogue use their first bytes as scratch.
+extern __shared__ __align__(128) unsigned char s_stage[];
+
 // block reduction of kN accumulators into smem out_s/out_c (threads < kN)
 template <int kN>
 __device__ __forceinline__ void block_sum(const float *acc_in, float *out_s, float *out_c) {
-  __shared__ float ws[kThreads / 32][kN][2];
+  float(*ws)[kN][2] = reinterpret_cast<float(*)[kN][2]>(s_stage);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int a = 0; a < kN; ++a) {
@@ -376,7 +386,7 @@ __device__ __forceinline__ void block_sum(const float *acc_in, float *out_s, flo
 template <int kN>
 __device__ __forceinline__ void fold_slots(const float *slots, int count, float *out_s,
                                            float *out_c) {
-  __shared__ float fs[kThreads / 32][32][2];
+  float(*fs)[32][2] = reinterpret_cast<float(*)[32][2]>(s_stage + 2048);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // thread (warp w, lane a) sums slots w, w + 8, ... for accumulator a
   CSum t = {0.f, 0.f};
@@ -436,7 +446,7 @@ __device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *o
   // the shared flags are rewritten
   __syncthreads();
   if (threadIdx.x == 0) {
-    const int p = find_pair(off, a.B, t);
+    const int p = find_pair(off, a, t);
     s_new = (p != tc.p);
     if (s_new) {
       tc.p = p;
@@ -458,17 +468,19 @@ __device__ __forceinline__ int cache_pair(const BatchArgs &a, const long long *o
 // ---------------------------------------------------------------------------
 // Pixels per thread of a staged sub-chunk (kCh, a template parameter of
 // the tile functions) and blocks per SM of the kernel, measured on GB300:
-//   * geometric only: 3 blocks of 256 threads per SM (80 registers, 3-pixel
-//     sub-chunks whose two 24 KB stages fit three blocks' shared memory).
-//     24 warps instead of 16 hide more of the gathers' latency: the
-//     256-pair run took 29.5 ms instead of 32.6 (2 blocks, 4 pixels).
+//   * geometric only: 3 blocks of 256 threads per SM (80 registers, 4-pixel
+//     sub-chunks; two 32 KB stages per block fit three blocks' shared memory
+//     because the epilogue scratch lives in the idle stages).  24 warps
+//     instead of 16 hide more of the gathers' latency: the 256-pair run
+//     took 27.9 ms, against 32.6 with 2 blocks and 29.5 with 3-pixel
+//     sub-chunks (the run tracks the pixels in flight per SM).
 //   * with a feature term: 2 blocks of 128 registers and 2-pixel sub-chunks.
 //     Three blocks at 80 registers spill enough to lose (16 x 1080p: 264
 //     pairs/s against 382); 2-pixel sub-chunks spill less than 4-pixel ones
 //     (16 x 1080p: 409 pairs/s against 382).
 template <bool kFeat>
 struct BatchShape {
-  static constexpr int kCh = kFeat ? 2 : 3;
+  static constexpr int kCh = kFeat ? 2 : 4;
   static constexpr int kBlocksPerSM = kFeat ? 2 : 3;
 };
 
@@ -500,7 +512,6 @@ struct StageStream {
   unsigned elem;  // element size of the plain copy (1, 4 or 8)
 };
 
-extern __shared__ __align__(128) unsigned char s_stage[];
 
 template <int kCh>
 __device__ __forceinline__ unsigned char *stage_buf(int st) {
@@ -632,7 +643,7 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
   if (tc.skip) return;
   const Pose32 &P = tc.P;
   const stb_level &lv = tc.lv;
-  const long long lt = t - off_at(off, a.B, p);
+  const long long lt = t - off_at(off, a, p);
   const LevelP &q = a.lp[level];
   const int H = lv.height, W = lv.width;
   unsigned long long *keys = a.keys + __ldcg(a.key_off + p);
@@ -797,8 +808,8 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   const Pose32 &P = tc.P;
   const stb_level &lv = tc.lv;
   const size_t row = (size_t)level * (a.B + 1);
-  const long long t0 = off_at(off, a.B, p);
-  const long long ntiles = off_at(off, a.B, p + 1) - t0;
+  const long long t0 = off_at(off, a, p);
+  const long long ntiles = off_at(off, a, p + 1) - t0;
   const long long lt = t - t0;
   const LevelP &q = a.lp[level];
   const int H = lv.height, W = lv.width;
@@ -957,10 +968,10 @@ template <typename FT, bool kFeat, bool kHWC>
 __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
     k_batch(const BatchArgs args) {
   constexpr int kCh = BatchShape<kFeat>::kCh;
+  long long *s_off = reinterpret_cast<long long *>(s_stage + 2 * stage_bytes(kCh));
   // the argument block is staged in shared memory so that device functions
   // can take it by reference without a per-thread local copy
   __shared__ BatchArgs a;
-  __shared__ long long s_off[kStageOff];
   __shared__ TileCache tc;
   __shared__ StageCtl ctl;
   unsigned ph = 0;  // expected parities of the two staging barriers
@@ -1025,13 +1036,13 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
     const long long src_tiles = __ldcg(a.src_off + row + a.B);
     const long long tgt_tiles = __ldcg(a.tgt_off + row + a.B);
     for (int it = 0; it < a.lp[level].iters; ++it, ++s) {
-      const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
+      const long long *off = stage_offsets(a.src_off + row, a, s_off);
       reset_cache(tc);
       for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
         assoc_tile<kCh>(a, off, level, t, s, false, tc, ctl, ph);
       });
       if (!grid_sync(a.sync)) return;
-      off = stage_offsets(a.tgt_off + row, a.B, s_off);
+      off = stage_offsets(a.tgt_off + row, a, s_off);
       reset_cache(tc);
       for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
         reduce_tile<FT, kFeat, false, kHWC, kCh>(a, off, level, t, s, tc, ctl, ph);
@@ -1044,13 +1055,13 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
   const size_t row = (size_t)level * (a.B + 1);
   const long long src_tiles = __ldcg(a.src_off + row + a.B);
   const long long tgt_tiles = __ldcg(a.tgt_off + row + a.B);
-  const long long *off = stage_offsets(a.src_off + row, a.B, s_off);
+  const long long *off = stage_offsets(a.src_off + row, a, s_off);
   reset_cache(tc);
   for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
     assoc_tile<kCh>(a, off, level, t, s, true, tc, ctl, ph);
   });
   if (!grid_sync(a.sync)) return;
-  off = stage_offsets(a.tgt_off + row, a.B, s_off);
+  off = stage_offsets(a.tgt_off + row, a, s_off);
   reset_cache(tc);
   for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
     reduce_tile<FT, false, true, false, kCh>(a, off, level, t, s, tc, ctl, ph);
@@ -1076,15 +1087,22 @@ int launch_batch(const BatchArgs &args, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   constexpr int kStageSmem = 2 * stage_bytes(BatchShape<kFeat>::kCh);
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageSmem) !=
-      cudaSuccess)
+  // the offset rows go after the stages when that keeps the blocks per SM
+  const int off_bytes = 8 * (args.B + 1);
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kStageSmem + off_bytes) != cudaSuccess)
     return check_launch("cudaFuncSetAttribute");
+  int with_off = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, kStageSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&with_off, kern, kThreads,
+                                                kStageSmem + off_bytes);
+  const bool stage_off = with_off >= per_sm;
+  const int smem = kStageSmem + (stage_off ? off_bytes : 0);
   if (per_sm < 1) return fail(STB_ECUDA, "Cuda call error stb_icp_estimate_batch: kernel does not fit an SM");
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(sms * per_sm);
   cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = kStageSmem;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
@@ -1092,6 +1110,7 @@ int launch_batch(const BatchArgs &args, cudaStream_t st) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   BatchArgs a = args;
+  a.off_cap = stage_off ? args.B + 1 : 0;
   const cudaError_t err = cudaLaunchKernelEx(&cfg, kern, a);
   if (err != cudaSuccess)
     return fail(STB_ECUDA, "Cuda call error stb_icp_estimate_batch: %s", cudaGetErrorString(err));
