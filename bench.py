@@ -28,6 +28,8 @@ Secondary workloads (rank 0, N = 1, reported under "secondary"; skip with
       reference preset), BatchRegistration vs the plain path;
   bilateral_depth_filter     the depth bilateral filter on uint16 depth,
       640x480 and 1920x1080, widths 6 and 13;
+  plain_kernels_larger_images  the plain path's association and reduction
+      kernels at 1920x1080 and 3840x2160 (fraction of measured HBM);
   autograd_layer             ExpRtToMatrix forward + backward (1 M twists),
       the frame point-cloud matcher forward + backward (640x480, 3
       channels), one AutogradICP registration (320x240).
@@ -548,6 +550,56 @@ def secondary_bilateral(device, seed, reps=200):
     return out
 
 
+def secondary_plain_sizes(device, seed, reps=20):
+    """The plain path's kernels at larger images (one pair, 10 iterations,
+    geometric): per-launch CUDA-event times of the association and of the
+    reduction with its step (the profiled graph replay), and the fraction
+    of the measured HBM bandwidth their algorithmic bytes reach.  At
+    640x480 an iteration is a latency chain; these show how the same
+    kernels do when there are bytes enough to stream."""
+    import torch
+    from slamtb_gb300 import _native as N
+    from slamtb_gb300 import synthetic
+    from slamtb_gb300.frame import Frame, FrameInfo, FramePointCloud, KCamera
+    from slamtb_gb300.registration.icp import ICPOdometry
+    peak, kind = measured_peak()
+    out = {"peak_gbs": peak, "peak_source": kind}
+    for w, h in ((1920, 1080), (3840, 2160)):
+        p = synthetic.make_pair(seed + 6000, width=w, height=h)
+        k = KCamera(p["kcam"])
+        src = FramePointCloud.from_frame(Frame(FrameInfo(k), p["source_depth"]), device)
+        tgt = FramePointCloud.from_frame(Frame(FrameInfo(k), p["target_depth"]), device)
+        icp = ICPOdometry(ITERS, geom_weight=1.0, feat_weight=0.0, distance_threshold=DIST,
+                          normals_angle_thresh=ANGLE)
+        kc = torch.from_numpy(p["kcam"]).to(device)
+        args_ = (kc, src.points.reshape(-1, 3), src.normals.reshape(-1, 3), src.mask.reshape(-1))
+        kw = dict(target_points=tgt.points, target_mask=tgt.mask, target_normals=tgt.normals)
+        for _ in range(3):
+            icp.launch(*args_, **kw)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            icp.launch(*args_, **kw)
+        torch.cuda.synchronize(device)
+        reg_ms = (time.perf_counter() - t0) * 1e3 / reps
+        N.profile_enable(True)
+        prof = {kk: [0.0, 0] for kk in N.PROFILE_KINDS}
+        for _ in range(reps):
+            icp.launch(*args_, **kw)
+            torch.cuda.synchronize(device)
+            for kk, (ms, cnt) in N.profile_read().items():
+                prof[kk][0] += ms
+                prof[kk][1] += cnt
+        N.profile_enable(False)
+        case = {"registration_ms": reg_ms, "gn_iters_per_s": ITERS / (reg_ms * 1e-3)}
+        for kk in ("association", "reduction+solve"):
+            us = prof[kk][0] / max(prof[kk][1], 1) * 1e3
+            gbs = ALG_BYTES[kk] * w * h / (us * 1e-6) / 1e9
+            case[kk] = {"us_per_launch": us, "achieved_gbs": gbs, "frac": gbs / peak}
+        out[f"{w}x{h}"] = case
+    return out
+
+
 def secondary_autograd(device, seed, reps=50):
     """The differentiable registration layer: ExpRtToMatrix forward +
     backward on 1 M twists, the frame point-cloud matcher forward + backward
@@ -684,7 +736,8 @@ def run_secondary(device, seed):
                      ("batch_uneven_256", secondary_batch_uneven),
                      ("feature_1080p_16ch_bf16", secondary_feature_1080p),
                      ("bilateral_depth_filter", secondary_bilateral),
-                     ("autograd_layer", secondary_autograd)):
+                     ("autograd_layer", secondary_autograd),
+                     ("plain_kernels_larger_images", secondary_plain_sizes)):
         t = time.perf_counter()
         try:
             out[name] = fn(device, seed)
