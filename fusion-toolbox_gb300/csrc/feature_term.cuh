@@ -16,8 +16,10 @@
 namespace stb {
 
 // J^T J (upper triangle, 21 slots, by w2) and J^T r (6 slots from 21, by
-// w1) of one Jacobian row, into per-thread float32 partials.
-__device__ __forceinline__ void acc_se3_terms(float *acc, const float *Jv, float r, float w1,
+// w1) of one Jacobian row, into per-thread float32 partials (a register
+// array, or StridedAcc accumulators in shared memory).
+template <typename Acc>
+__device__ __forceinline__ void acc_se3_terms(Acc acc, const float *Jv, float r, float w1,
                                               float w2) {
 #pragma unroll
   for (int a = 0; a < 6; ++a)
@@ -40,12 +42,12 @@ __device__ __forceinline__ void feature_jacobian(const float3 &Tp, float du, flo
 
 // Returns true when the pixel passes the gate (its J terms are then in
 // acc, J^T r with -wf1 as icp.py:222); sq receives sum_c r_c^2.
-template <typename FT, bool kHWC>
+template <typename FT, bool kHWC, typename Acc>
 __device__ __forceinline__ bool feature_term(const FeatView<FT, kHWC> &tf,
                                              const FeatView<FT, kHWC> &sf, long long i,
                                              const Pose32 &P, const float3 &Tp, int H, int W,
                                              float feat_thr2, int mode, float wf1, float wf2,
-                                             float *acc, float &sq) {
+                                             Acc acc, float &sq) {
   const int C = tf.C;
   float u, v;
   project(P, Tp, u, v);

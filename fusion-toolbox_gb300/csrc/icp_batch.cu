@@ -339,7 +339,8 @@ __device__ void build_offsets(const BatchArgs &a) {
 // Per-thread partial sums are plain float32: a thread adds at most
 // tile / 256 <= 16 pixels, so its rounding error stays below ~1e-6 of the
 // sum of magnitudes; compensation (TwoSum) starts at the warp level.
-__device__ __forceinline__ void acc_se3(float *acc, const float *Jv, float r, float w1,
+template <typename Acc>
+__device__ __forceinline__ void acc_se3(Acc acc, const float *Jv, float r, float w1,
                                         float w2) {
 #pragma unroll
   for (int a = 0; a < 6; ++a)
@@ -350,14 +351,15 @@ __device__ __forceinline__ void acc_se3(float *acc, const float *Jv, float r, fl
 }
 
 // Dynamic shared memory of the kernel: two staging buffers, then the staged
-// offset row.  Between a tile's pipeline and the next tile's first copy the
+// offset row, then (kernels with a feature term) the per-thread
+// accumulators of the reduction.  Between a tile's pipeline and the next tile's first copy the
 // staging buffers are idle: the block sum and the slot folds of the tile's
 // epilogue use their first bytes as scratch.
 extern __shared__ __align__(128) unsigned char s_stage[];
 
 // block reduction of kN accumulators into smem out_s/out_c (threads < kN)
-template <int kN>
-__device__ __forceinline__ void block_sum(const float *acc_in, float *out_s, float *out_c) {
+template <int kN, typename Acc>
+__device__ __forceinline__ void block_sum(Acc acc_in, float *out_s, float *out_c) {
   float(*ws)[kN][2] = reinterpret_cast<float(*)[kN][2]>(s_stage);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -512,6 +514,28 @@ struct StageStream {
   unsigned elem;  // element size of the plain copy (1, 4 or 8)
 };
 
+
+// offset row bytes after the stages (B + 1 entries when staged), 16-aligned
+__host__ __device__ inline int off_row_bytes(int off_cap) { return (8 * off_cap + 15) & ~15; }
+constexpr int kAccSmemBytes = kAccsB * kThreads * 4;  // feature kernels' accumulators
+
+template <int kCh>
+__device__ __forceinline__ float *smem_acc(const BatchArgs &a) {
+  return reinterpret_cast<float *>(s_stage + 2 * stage_bytes(kCh) + off_row_bytes(a.off_cap));
+}
+
+template <bool kSmem>
+struct AccPick;
+template <>
+struct AccPick<false> {
+  static __device__ __forceinline__ float *get(float *regs, float *) { return regs; }
+};
+template <>
+struct AccPick<true> {
+  static __device__ __forceinline__ StridedAcc<kThreads> get(float *, float *smem) {
+    return {smem};
+  }
+};
 
 template <int kCh>
 __device__ __forceinline__ unsigned char *stage_buf(int st) {
@@ -817,7 +841,11 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   const unsigned long long *keys = a.keys + __ldcg(a.key_off + p);
   const unsigned tag = btag(s);
 
-  float acc[kN];
+  // With a feature term the 30 accumulators live in shared memory (their
+  // registers would spill at this kernel's 128); otherwise in registers.
+  constexpr bool kSmemAcc = kFeat && !kInfo;
+  float acc_r[kSmemAcc ? 1 : kN];
+  const auto acc = AccPick<kSmemAcc>::get(acc_r, smem_acc<kCh>(a) + threadIdx.x);
 #pragma unroll
   for (int k = 0; k < kN; ++k) acc[k] = 0.f;
 
@@ -1086,9 +1114,10 @@ int launch_batch(const BatchArgs &args, cudaStream_t st) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  constexpr int kStageSmem = 2 * stage_bytes(BatchShape<kFeat>::kCh);
+  constexpr int kStageSmem = 2 * stage_bytes(BatchShape<kFeat>::kCh) +
+                             (kFeat ? kAccSmemBytes : 0);
   // the offset rows go after the stages when that keeps the blocks per SM
-  const int off_bytes = 8 * (args.B + 1);
+  const int off_bytes = off_row_bytes(args.B + 1);
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            kStageSmem + off_bytes) != cudaSuccess)
     return check_launch("cudaFuncSetAttribute");

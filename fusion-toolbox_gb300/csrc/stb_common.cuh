@@ -152,6 +152,14 @@ __device__ __forceinline__ float bilin_c(const FeatView<T, kHWC> &f, int c, int 
 // Compensated float32 sums: a value is carried as (s, c) with the exact sum
 // s + c; TwoSum (Knuth) keeps the rounding error of every addition.
 // ---------------------------------------------------------------------------
+// Per-thread accumulators in shared memory, transposed ([slot][thread]):
+// the lanes of a warp touching one slot fall in distinct banks.
+template <int kStride>
+struct StridedAcc {
+  float *p;
+  __device__ __forceinline__ float &operator[](int k) const { return p[k * kStride]; }
+};
+
 struct CSum {
   float s, c;
 };
