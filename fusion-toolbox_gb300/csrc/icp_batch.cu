@@ -692,7 +692,7 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
     const float *sp = reinterpret_cast<const float *>(stage_buf<kCh>(st));
     const float *sn = sp + kSub * 3;
     const unsigned char *sm = stage_buf<kCh>(st) + kSub * 24;
-    // round 1: projection and target gathers
+    // pass 1: projection and target gathers
     float3 Tp[kCh];
     long long pix[kCh];
     bool ok[kCh];
@@ -716,7 +716,7 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
       my[k] = __ldg(lv.tgt_normals + 3 * pix[k] + 1);
       mz[k] = __ldg(lv.tgt_normals + 3 * pix[k] + 2);
     }
-    // round 2: gates and the z-buffer
+    // pass 2: gates and the z-buffer
 #pragma unroll
     for (int k = 0; k < kCh; ++k) {
       if (!ok[k]) continue;
@@ -870,7 +870,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
     const unsigned long long *skeys = reinterpret_cast<const unsigned long long *>(stage_buf<kCh>(st));
     const float *stq = reinterpret_cast<const float *>(stage_buf<kCh>(st) + kSub * 8);
     const float *stn = reinterpret_cast<const float *>(stage_buf<kCh>(st) + kSub * 20);
-    // round 1: the winners' source points (the gathers that remain)
+    // pass 1: the winners' source points (the gathers that remain)
     unsigned long long key[kCh];
     float spt[kCh][3];
 #pragma unroll
@@ -882,7 +882,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
 #pragma unroll
       for (int d = 0; d < 3; ++d) spt[k][d] = kInfo ? 0.f : __ldg(lv.src_points + 3 * i + d);
     }
-    // round 2: residuals, Jacobians and the per-thread sums
+    // pass 2: residuals, Jacobians and the per-thread sums
 #pragma unroll
     for (int k = 0; k < kCh; ++k) {
       if ((unsigned)(key[k] >> 56) != tag) continue;

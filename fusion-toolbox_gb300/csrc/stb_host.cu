@@ -19,7 +19,7 @@ int fail(int code, const char *fmt, ...) {
 void clear_error() { g_message[0] = '\0'; }
 
 // Recently validated device pointers of this thread (a tracker passes the
-// same buffers every frame): a hit skips the driver query.  Only pointers
+// same buffers every frame): a hit skips cudaPointerGetAttributes.  Only pointers
 // that passed as device memory of the current device are remembered, so a
 // host pointer is always queried and refused.
 struct PtrCacheEntry {

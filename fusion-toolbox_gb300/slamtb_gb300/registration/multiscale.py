@@ -57,5 +57,5 @@ class MultiscaleRegistration:
         return curr_result
 
 
-# The name spec callers use for the multiscale ICP wrapper.
+# The other name of the multiscale ICP wrapper (MultiscaleICPOdometry).
 MultiscaleICPOdometry = MultiscaleRegistration
