@@ -1,0 +1,82 @@
+"""Host-side logic of the package that needs no GPU: the rigid transform and
+Huber loss of AutogradICP's closure, the small host inputs handed to the C
+entry by value, and the unpacking of the FP64 result block."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+
+def test_rigid_transform_points_and_normals():
+    """camera.py:310-408: R p + t for points, (R^-1)^T n for normals."""
+    from slamtb_gb300.camera import RigidTransform
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=3)
+    a *= 0.7 / np.linalg.norm(a)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    R = np.eye(3) + np.sin(0.7) / 0.7 * K + (1 - np.cos(0.7)) / 0.49 * K @ K
+    T = np.eye(4)
+    T[:3, :3] = R * 1.5  # a non-rigid scale shows the inverse transpose at work
+    T[:3, 3] = [0.1, -0.2, 0.3]
+    p = rng.normal(size=(7, 3))
+    n = rng.normal(size=(7, 3))
+    rt = RigidTransform(torch.from_numpy(T))
+    np.testing.assert_allclose((rt @ torch.from_numpy(p)).numpy(), p @ T[:3, :3].T + T[:3, 3],
+                               atol=1e-12)
+    np.testing.assert_allclose(rt.transform_normals(torch.from_numpy(n)).numpy(),
+                               n @ np.linalg.inv(T[:3, :3]), atol=1e-12)
+
+
+def test_huber_loss_matches_the_reference_formula():
+    """autogradicp.py:60-90: mean of the residuals below alpha plus the mean
+    of alpha |r| - alpha over the rest (either part may be empty)."""
+    from slamtb_gb300.registration.autogradicp import _HuberLoss
+    h = _HuberLoss(2.0)
+    r = torch.tensor([0.5, 1.0, 3.0, 5.0])
+    assert float(h(r)) == pytest.approx(0.75 + ((2 * 3 - 2) + (2 * 5 - 2)) / 2)
+    assert float(h(torch.tensor([0.1, 0.3]))) == pytest.approx(0.2)
+    assert h(torch.tensor([])) == 0
+
+
+def test_small_host_inputs_are_passed_by_value():
+    """Intrinsics and initial poses held on the host reach the C entry as
+    contiguous float32 / float64 arrays of the right size."""
+    from slamtb_gb300.registration.icp import _small_input
+    k = torch.tensor([[500.0, 0, 320], [0, 510, 240], [0, 0, 1]], dtype=torch.float64)
+    arr, ptr = _small_input(k, torch.device("cuda", 0), torch.float32, np.float32, 9, "kcam")
+    assert arr.dtype == np.float32 and arr.flags["C_CONTIGUOUS"] and ptr.value == arr.ctypes.data
+    np.testing.assert_array_equal(arr.reshape(3, 3), k.numpy().astype(np.float32))
+    T = np.eye(4)[:, ::-1]  # a non-contiguous view
+    arr, _ = _small_input(T, torch.device("cuda", 0), torch.float64, np.float64, 16, "transform")
+    assert arr.flags["C_CONTIGUOUS"]
+    np.testing.assert_array_equal(arr, T)
+    with pytest.raises(RuntimeError, match="16 entries"):
+        _small_input(np.eye(3), torch.device("cuda", 0), torch.float64, np.float64, 16,
+                     "transform")
+
+
+def test_result_block_unpacking():
+    """The FP64 result block (STB_RES_* layout) -> RegistrationResult, as
+    icp.py:249-262: the transform and information as tensors that do not
+    alias the (reused) block, the residual, and matches over source points;
+    an empty result (information only) when no iteration succeeded."""
+    from slamtb_gb300 import _native as N
+    from slamtb_gb300.registration.icp import ICPOdometry
+    out = torch.zeros(N.RES_SIZE, dtype=torch.float64)
+    T = torch.arange(16, dtype=torch.float64)
+    out[N.RES_TRANSFORM:N.RES_TRANSFORM + 16] = T
+    out[N.RES_INFO:N.RES_INFO + 36] = torch.arange(36, dtype=torch.float64) * 0.5
+    out[N.RES_RESIDUAL] = 0.25
+    out[N.RES_MATCHES] = 300.0
+    out[N.RES_ITERS] = 10.0
+    res = ICPOdometry._result(out, 1200, torch.float32)
+    np.testing.assert_array_equal(res.transform.numpy(), T.view(4, 4).numpy())
+    assert res.information.dtype == torch.float32 and res.information.shape == (6, 6)
+    assert res.residual == 0.25 and res.match_ratio == 0.25
+    out[N.RES_TRANSFORM] = 99.0
+    assert res.transform[0, 0] == 0.0  # a copy
+    out[N.RES_ITERS] = 0.0
+    empty = ICPOdometry._result(out, 1200, torch.float32)
+    assert empty.transform is None and empty.information is not None
+    assert math.isinf(empty.residual)
