@@ -88,45 +88,87 @@ __device__ __forceinline__ void pair_pose(const LossArgs &a, Pose32 &P) {
 }
 
 // Source point i of a pair from its depth (stb_depth_to_points' arithmetic).
-__device__ __forceinline__ float3 source_point(const LossArgs &a, float z, int64_t i) {
+__device__ __forceinline__ float3 source_point(const LossArgs &a, float z, int i) {
   const float u = (float)(i % a.W), v = (float)(i / a.W);
   return make_float3(fdiv(fmul(fsub(u, a.cx), z), a.fx), fdiv(fmul(fsub(v, a.cy), z), a.fy), z);
 }
+
+// Pixels per thread per round of the loss kernels: every load of a round
+// is issued before the first dependent use, so a thread waits for one
+// gather round trip per round instead of one per pixel.  The pixels of a
+// thread keep the grid-stride order, so sums are the same bits.  Two
+// pixels keep 4-5 blocks of 256 resident per SM (the register caps of the
+// launch bounds: k_g_assoc 64 without one, k_g_adjoint 64, k_g_loss 48);
+// four pixels need about 115 registers and halve the occupancy, which
+// costs more than the extra loads in flight win.
+constexpr int kP = 2;
 
 __global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long long *keys_all,
                                                 float thr2, float cos_max) {
   __shared__ Pose32 P;
   pair_pose(a, P);
   const int H = a.H, W = a.W;
-  const int64_t npix = (int64_t)H * W;
+  const int npix = H * W;  // < 2^24, checked on the host
   const size_t po = (size_t)blockIdx.y * npix;
   unsigned long long *keys = keys_all + po;
   const float *tp = a.tp + 3 * po, *tn = a.tn + 3 * po, *sn = a.sn + 3 * po;
   const uint8_t *tm = a.tm + po;
-  for (int64_t i = blockIdx.x * (int64_t)kT + threadIdx.x; i < npix;
-       i += (int64_t)gridDim.x * kT) {
-    if (!a.sm[po + i]) continue;
-    const float3 s = source_point(a, a.depth[po + i], i);
-    const float3 Tp = transform_point(P.rt, s.x, s.y, s.z);
-    float u, v;
-    project(P, Tp, u, v);
-    int ui, vi;
-    if (!round_in(u, W, ui) || !round_in(v, H, vi)) continue;
-    const int64_t pix = (int64_t)vi * W + ui;
-    if (!tm[pix]) continue;
-    const float dx = fsub(tp[3 * pix], Tp.x), dy = fsub(tp[3 * pix + 1], Tp.y),
-                dz = fsub(tp[3 * pix + 2], Tp.z);
-    const float sq = dot3(dx, dy, dz, dx, dy, dz);
-    if (sq > thr2) continue;
-    const float3 Tn = transform_normal(P.nm, sn[3 * i], sn[3 * i + 1], sn[3 * i + 2]);
-    const float nx = tn[3 * pix], ny = tn[3 * pix + 1], nz = tn[3 * pix + 2];
-    const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, nx, ny, nz),
-                         fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
-                              __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz))));
-    if (c >= -1.0f && c <= cos_max) continue;
-    atomicMin(keys + pix, ((unsigned long long)kTag << 56) |
-                              ((unsigned long long)__float_as_uint(__fsqrt_rn(sq)) << 24) |
-                              (unsigned long long)i);
+  const int stride = gridDim.x * kT;
+  for (int i0 = blockIdx.x * kT + threadIdx.x; i0 < npix; i0 += stride * kP) {
+    // pass 1: the source pixels (coalesced), their projections, and the
+    // gathers of the projected target pixels
+    bool ok[kP];
+    int pix[kP];
+    float3 Tp[kP];
+    float z[kP];
+#pragma unroll
+    for (int k = 0; k < kP; ++k) {
+      const int i = i0 + k * stride;
+      const int ic = i < npix ? i : 0;
+      ok[k] = i < npix && a.sm[po + ic];
+      z[k] = a.depth[po + ic];
+    }
+#pragma unroll
+    for (int k = 0; k < kP; ++k) {
+      const int i = i0 + k * stride;
+      const float3 s = source_point(a, z[k], i < npix ? i : 0);
+      Tp[k] = transform_point(P.rt, s.x, s.y, s.z);
+      float u, v;
+      project(P, Tp[k], u, v);
+      int ui = 0, vi = 0;
+      ok[k] = ok[k] && round_in(u, W, ui) && round_in(v, H, vi);
+      pix[k] = ok[k] ? vi * W + ui : 0;
+    }
+    float q[kP][3], m[kP][3];
+    bool tv[kP];
+#pragma unroll
+    for (int k = 0; k < kP; ++k) {
+      tv[k] = tm[pix[k]];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        q[k][d] = tp[3 * pix[k] + d];
+        m[k][d] = tn[3 * pix[k] + d];
+      }
+    }
+    // pass 2: the gates and the z-buffer
+#pragma unroll
+    for (int k = 0; k < kP; ++k) {
+      if (!ok[k] || !tv[k]) continue;
+      const int i = i0 + k * stride;
+      const float dx = fsub(q[k][0], Tp[k].x), dy = fsub(q[k][1], Tp[k].y),
+                  dz = fsub(q[k][2], Tp[k].z);
+      const float sq = dot3(dx, dy, dz, dx, dy, dz);
+      if (sq > thr2) continue;
+      const float3 Tn = transform_normal(P.nm, sn[3 * i], sn[3 * i + 1], sn[3 * i + 2]);
+      const float nx = m[k][0], ny = m[k][1], nz = m[k][2];
+      const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, nx, ny, nz),
+                           fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
+                                __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz))));
+      if (c >= -1.0f && c <= cos_max) continue;
+      atomicMin(keys + pix[k], ((unsigned long long)kTag << 56) |
+                                   ((unsigned long long)__float_as_uint(__fsqrt_rn(sq)) << 24) |
+                                   (unsigned long long)i);
+    }
   }
 }
 
@@ -174,39 +216,75 @@ __device__ bool pair_fold(CSum *acc, float *part_all, unsigned *tickets, double 
   return true;
 }
 
-// Residual at target pixel pix of the pair (offset po) and its
-// correspondence i; returns r and the transformed source point and normal.
-__device__ __forceinline__ float residual(const LossArgs &a, const Pose32 &P, size_t po,
-                                          int64_t pix, int64_t i, float3 &Tp, float3 &n) {
-  const float3 s = source_point(a, a.depth[po + i], i);
-  Tp = transform_point(P.rt, s.x, s.y, s.z);
-  const float *tp = a.tp + 3 * (po + pix), *tn = a.tn + 3 * (po + pix);
-  n = make_float3(tn[0], tn[1], tn[2]);
-  return dot3(fsub(tp[0], Tp.x), fsub(tp[1], Tp.y), fsub(tp[2], Tp.z), n.x, n.y, n.z);
+// The inputs of a round's residuals: keys, then (matched pixels) the
+// winners' depths (the gather) and the target points and normals.
+struct Round {
+  bool m[kP];
+  int i[kP];
+  float z[kP], q[kP][3], n[kP][3];
+};
+
+__device__ __forceinline__ void load_round(const LossArgs &a, size_t po, int npix,
+                                           const unsigned long long *keys, int p0, int stride,
+                                           Round &R) {
+  unsigned long long key[kP];
+#pragma unroll
+  for (int k = 0; k < kP; ++k) {
+    const int pix = p0 + k * stride;
+    key[k] = pix < npix ? __ldcg(keys + pix) : 0ull;
+  }
+#pragma unroll
+  for (int k = 0; k < kP; ++k) {
+    const int pix = p0 + k * stride;
+    R.m[k] = (unsigned)(key[k] >> 56) == kTag;
+    R.i[k] = R.m[k] ? (int)(key[k] & 0xffffffull) : 0;
+    const int pc = R.m[k] ? pix : 0;
+    R.z[k] = a.depth[po + R.i[k]];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      R.q[k][d] = a.tp[3 * (po + pc) + d];
+      R.n[k][d] = a.tn[3 * (po + pc) + d];
+    }
+  }
 }
 
-__global__ void __launch_bounds__(kT) k_g_loss(const LossArgs a,
+// r = (q - Tp) . n of pixel k of a round (the value residual() computes).
+__device__ __forceinline__ float round_residual(const LossArgs &a, const Pose32 &P,
+                                                const Round &R, int k, float3 &Tp,
+                                                float3 &n) {
+  const float3 s = source_point(a, R.z[k], R.i[k]);
+  Tp = transform_point(P.rt, s.x, s.y, s.z);
+  n = make_float3(R.n[k][0], R.n[k][1], R.n[k][2]);
+  return dot3(fsub(R.q[k][0], Tp.x), fsub(R.q[k][1], Tp.y), fsub(R.q[k][2], Tp.z), n.x, n.y,
+              n.z);
+}
+
+__global__ void __launch_bounds__(kT, 5) k_g_loss(const LossArgs a,
                                                const unsigned long long *keys_all, float *part,
                                                unsigned *tickets, double *loss) {
   __shared__ Pose32 P;
   __shared__ double tot[8];
   pair_pose(a, P);
-  const int64_t npix = (int64_t)a.H * a.W;
+  const int npix = a.H * a.W;
   const size_t po = (size_t)blockIdx.y * npix;
   const unsigned long long *keys = keys_all + po;
+  const int stride = gridDim.x * kT;
   CSum acc[1] = {{0.f, 0.f}};
-  for (int64_t pix = blockIdx.x * (int64_t)kT + threadIdx.x; pix < npix;
-       pix += (int64_t)gridDim.x * kT) {
-    const unsigned long long key = __ldcg(keys + pix);
-    if ((unsigned)(key >> 56) != kTag) continue;
-    float3 Tp, n;
-    const float r = residual(a, P, po, pix, (int64_t)(key & 0xffffffull), Tp, n);
-    csum_add(acc[0], r * r);
+  for (int p0 = blockIdx.x * kT + threadIdx.x; p0 < npix; p0 += stride * kP) {
+    Round R;
+    load_round(a, po, npix, keys, p0, stride, R);
+#pragma unroll
+    for (int k = 0; k < kP; ++k) {
+      if (!R.m[k]) continue;
+      float3 Tp, n;
+      const float r = round_residual(a, P, R, k, Tp, n);
+      csum_add(acc[0], r * r);
+    }
   }
   if (pair_fold<1>(acc, part, tickets, tot) && threadIdx.x == 0) loss[blockIdx.y] = tot[0];
 }
 
-__global__ void __launch_bounds__(kT) k_g_adjoint(const LossArgs a,
+__global__ void __launch_bounds__(kT, 4) k_g_adjoint(const LossArgs a,
                                                   const unsigned long long *keys_all,
                                                   const double *grad_loss, float *part,
                                                   unsigned *tickets, double *grad_tangent,
@@ -214,34 +292,38 @@ __global__ void __launch_bounds__(kT) k_g_adjoint(const LossArgs a,
   __shared__ Pose32 P;
   __shared__ double tot[8];
   pair_pose(a, P);
-  const int64_t npix = (int64_t)a.H * a.W;
+  const int npix = a.H * a.W;
   const size_t po = (size_t)blockIdx.y * npix;
   const unsigned long long *keys = keys_all + po;
   const float g = (float)grad_loss[blockIdx.y];
   float *gz = grad_depth ? grad_depth + po : nullptr;
+  const int stride = gridDim.x * kT;
   CSum acc[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) acc[k] = {0.f, 0.f};
-  for (int64_t pix = blockIdx.x * (int64_t)kT + threadIdx.x; pix < npix;
-       pix += (int64_t)gridDim.x * kT) {
-    const unsigned long long key = __ldcg(keys + pix);
-    if ((unsigned)(key >> 56) != kTag) continue;
-    const int64_t i = (int64_t)(key & 0xffffffull);
-    float3 Tp, n;
-    const float r = residual(a, P, po, pix, i, Tp, n);
-    const float Jv[6] = {n.x, n.y, n.z, Tp.y * n.z - Tp.z * n.y, Tp.z * n.x - Tp.x * n.z,
-                         Tp.x * n.y - Tp.y * n.x};
-    const float s = -2.f * g * r;
+  for (int p0 = blockIdx.x * kT + threadIdx.x; p0 < npix; p0 += stride * kP) {
+    Round R;
+    load_round(a, po, npix, keys, p0, stride, R);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) csum_add(acc[k], s * Jv[k]);
-    if (gz) {
-      // R^T n, with R the float32 rotation of the pose
-      const float *R = P.rt;
-      const float rn0 = R[0] * n.x + R[4] * n.y + R[8] * n.z;
-      const float rn1 = R[1] * n.x + R[5] * n.y + R[9] * n.z;
-      const float rn2 = R[2] * n.x + R[6] * n.y + R[10] * n.z;
-      const float d0 = ((float)(i % a.W) - P.cx) / P.fx, d1 = ((float)(i / a.W) - P.cy) / P.fy;
-      gz[i] = s * (rn0 * d0 + rn1 * d1 + rn2);
+    for (int k = 0; k < kP; ++k) {
+      if (!R.m[k]) continue;
+      const int i = R.i[k];
+      float3 Tp, n;
+      const float r = round_residual(a, P, R, k, Tp, n);
+      const float Jv[6] = {n.x, n.y, n.z, Tp.y * n.z - Tp.z * n.y, Tp.z * n.x - Tp.x * n.z,
+                           Tp.x * n.y - Tp.y * n.x};
+      const float s = -2.f * g * r;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) csum_add(acc[c], s * Jv[c]);
+      if (gz) {
+        // R^T n, with R the float32 rotation of the pose
+        const float *Rt = P.rt;
+        const float rn0 = Rt[0] * n.x + Rt[4] * n.y + Rt[8] * n.z;
+        const float rn1 = Rt[1] * n.x + Rt[5] * n.y + Rt[9] * n.z;
+        const float rn2 = Rt[2] * n.x + Rt[6] * n.y + Rt[10] * n.z;
+        const float d0 = ((float)(i % a.W) - P.cx) / P.fx, d1 = ((float)(i / a.W) - P.cy) / P.fy;
+        gz[i] = s * (rn0 * d0 + rn1 * d1 + rn2);
+      }
     }
   }
   if (pair_fold<6>(acc, part, tickets, tot) && grad_tangent && threadIdx.x < 6)
