@@ -73,16 +73,26 @@ inline GradLayout grad_layout(int B, int64_t px) {
   return g;
 }
 
-// float32 pose of pair blockIdx.y, into shared memory.
-__device__ __forceinline__ void pair_pose(const LossArgs &a, Pose32 &P) {
-  if (threadIdx.x == 0) {
-    double T[16];
-    for (int k = 0; k < 16; ++k) T[k] = a.poses[blockIdx.y * 16 + k];
-    P.fx = a.fx;
-    P.fy = a.fy;
-    P.cx = a.cx;
-    P.cy = a.cy;
-    refresh_pose32(P, T);
+// float32 pose of pair blockIdx.y, into shared memory (refresh_pose32's
+// values), in two halves so that a kernel can issue its first pixel loads
+// in between: pose_load starts lanes 0..11 loading one FP64 entry each;
+// pose_finish converts them, forms the normal matrix on thread 0 and ends
+// with the block barrier.
+__device__ __forceinline__ double pose_load(const LossArgs &a) {
+  return threadIdx.x < 12 ? a.poses[blockIdx.y * 16 + threadIdx.x] : 0.0;
+}
+
+__device__ __forceinline__ void pose_finish(const LossArgs &a, Pose32 &P, double t) {
+  if (threadIdx.x < 32) {
+    if (threadIdx.x < 12) P.rt[threadIdx.x] = __double2float_rn(t);
+    __syncwarp();
+    if (threadIdx.x == 0) {
+      P.fx = a.fx;
+      P.fy = a.fy;
+      P.cx = a.cx;
+      P.cy = a.cy;
+      inverse_transpose(P.rt, P.nm);
+    }
   }
   __syncthreads();
 }
@@ -103,10 +113,28 @@ __device__ __forceinline__ float3 source_point(const LossArgs &a, float z, int i
 // costs more than the extra loads in flight win.
 constexpr int kP = 2;
 
+// The source half of a round of k_g_assoc (pose-independent): mask and
+// depth of pixels i0 + k * stride.
+struct SourceRound {
+  bool ok[kP];
+  float z[kP];
+};
+
+__device__ __forceinline__ void load_sources(const LossArgs &a, size_t po, int npix, int i0,
+                                             int stride, SourceRound &S) {
+#pragma unroll
+  for (int k = 0; k < kP; ++k) {
+    const int i = i0 + k * stride;
+    const int ic = i < npix ? i : 0;
+    S.ok[k] = i < npix && a.sm[po + ic];
+    S.z[k] = a.depth[po + ic];
+  }
+}
+
 __global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long long *keys_all,
                                                 float thr2, float cos_max) {
   __shared__ Pose32 P;
-  pair_pose(a, P);
+  const double pose_entry = pose_load(a);
   const int H = a.H, W = a.W;
   const int npix = H * W;  // < 2^24, checked on the host
   const size_t po = (size_t)blockIdx.y * npix;
@@ -114,29 +142,25 @@ __global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long 
   const float *tp = a.tp + 3 * po, *tn = a.tn + 3 * po, *sn = a.sn + 3 * po;
   const uint8_t *tm = a.tm + po;
   const int stride = gridDim.x * kT;
-  for (int i0 = blockIdx.x * kT + threadIdx.x; i0 < npix; i0 += stride * kP) {
-    // pass 1: the source pixels (coalesced), their projections, and the
-    // gathers of the projected target pixels
+  int i0 = blockIdx.x * kT + threadIdx.x;
+  SourceRound S;
+  load_sources(a, po, npix, i0, stride, S);  // in flight across the barrier
+  pose_finish(a, P, pose_entry);
+  while (true) {
+    // the projections of the source pixels, and the gathers of the
+    // projected target pixels
     bool ok[kP];
     int pix[kP];
     float3 Tp[kP];
-    float z[kP];
 #pragma unroll
     for (int k = 0; k < kP; ++k) {
       const int i = i0 + k * stride;
-      const int ic = i < npix ? i : 0;
-      ok[k] = i < npix && a.sm[po + ic];
-      z[k] = a.depth[po + ic];
-    }
-#pragma unroll
-    for (int k = 0; k < kP; ++k) {
-      const int i = i0 + k * stride;
-      const float3 s = source_point(a, z[k], i < npix ? i : 0);
+      const float3 s = source_point(a, S.z[k], i < npix ? i : 0);
       Tp[k] = transform_point(P.rt, s.x, s.y, s.z);
       float u, v;
       project(P, Tp[k], u, v);
       int ui = 0, vi = 0;
-      ok[k] = ok[k] && round_in(u, W, ui) && round_in(v, H, vi);
+      ok[k] = S.ok[k] && round_in(u, W, ui) && round_in(v, H, vi);
       pix[k] = ok[k] ? vi * W + ui : 0;
     }
     float q[kP][3], m[kP][3];
@@ -150,7 +174,7 @@ __global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long 
         m[k][d] = tn[3 * pix[k] + d];
       }
     }
-    // pass 2: the gates and the z-buffer
+    // the gates and the z-buffer
 #pragma unroll
     for (int k = 0; k < kP; ++k) {
       if (!ok[k] || !tv[k]) continue;
@@ -169,6 +193,9 @@ __global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long 
                                    ((unsigned long long)__float_as_uint(__fsqrt_rn(sq)) << 24) |
                                    (unsigned long long)i);
     }
+    i0 += stride * kP;
+    if (i0 >= npix) break;
+    load_sources(a, po, npix, i0, stride, S);
   }
 }
 
@@ -264,15 +291,17 @@ __global__ void __launch_bounds__(kT, 5) k_g_loss(const LossArgs a,
                                                unsigned *tickets, double *loss) {
   __shared__ Pose32 P;
   __shared__ double tot[8];
-  pair_pose(a, P);
+  const double pose_entry = pose_load(a);
   const int npix = a.H * a.W;
   const size_t po = (size_t)blockIdx.y * npix;
   const unsigned long long *keys = keys_all + po;
   const int stride = gridDim.x * kT;
   CSum acc[1] = {{0.f, 0.f}};
-  for (int p0 = blockIdx.x * kT + threadIdx.x; p0 < npix; p0 += stride * kP) {
-    Round R;
-    load_round(a, po, npix, keys, p0, stride, R);
+  int p0 = blockIdx.x * kT + threadIdx.x;
+  Round R;
+  load_round(a, po, npix, keys, p0, stride, R);  // in flight across the barrier
+  pose_finish(a, P, pose_entry);
+  while (true) {
 #pragma unroll
     for (int k = 0; k < kP; ++k) {
       if (!R.m[k]) continue;
@@ -280,6 +309,9 @@ __global__ void __launch_bounds__(kT, 5) k_g_loss(const LossArgs a,
       const float r = round_residual(a, P, R, k, Tp, n);
       csum_add(acc[0], r * r);
     }
+    p0 += stride * kP;
+    if (p0 >= npix) break;
+    load_round(a, po, npix, keys, p0, stride, R);
   }
   if (pair_fold<1>(acc, part, tickets, tot) && threadIdx.x == 0) loss[blockIdx.y] = tot[0];
 }
@@ -291,7 +323,7 @@ __global__ void __launch_bounds__(kT, 4) k_g_adjoint(const LossArgs a,
                                                   float *grad_depth) {
   __shared__ Pose32 P;
   __shared__ double tot[8];
-  pair_pose(a, P);
+  const double pose_entry = pose_load(a);
   const int npix = a.H * a.W;
   const size_t po = (size_t)blockIdx.y * npix;
   const unsigned long long *keys = keys_all + po;
@@ -301,9 +333,11 @@ __global__ void __launch_bounds__(kT, 4) k_g_adjoint(const LossArgs a,
   CSum acc[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) acc[k] = {0.f, 0.f};
-  for (int p0 = blockIdx.x * kT + threadIdx.x; p0 < npix; p0 += stride * kP) {
-    Round R;
-    load_round(a, po, npix, keys, p0, stride, R);
+  int p0 = blockIdx.x * kT + threadIdx.x;
+  Round R;
+  load_round(a, po, npix, keys, p0, stride, R);  // in flight across the barrier
+  pose_finish(a, P, pose_entry);
+  while (true) {
 #pragma unroll
     for (int k = 0; k < kP; ++k) {
       if (!R.m[k]) continue;
@@ -325,6 +359,9 @@ __global__ void __launch_bounds__(kT, 4) k_g_adjoint(const LossArgs a,
         gz[i] = s * (rn0 * d0 + rn1 * d1 + rn2);
       }
     }
+    p0 += stride * kP;
+    if (p0 >= npix) break;
+    load_round(a, po, npix, keys, p0, stride, R);
   }
   if (pair_fold<6>(acc, part, tickets, tot) && grad_tangent && threadIdx.x < 6)
     grad_tangent[blockIdx.y * 6 + threadIdx.x] = tot[threadIdx.x];
