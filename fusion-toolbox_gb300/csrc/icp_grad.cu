@@ -384,47 +384,84 @@ __global__ void k_se3_exp_compose(const double *twist, const double *base, doubl
 // ad(xi) = [[phi^, rho^], [0, phi^]] (Barfoot, State Estimation for
 // Robotics, sec. 7.1.5), in FP64 until the term falls below 1e-20 of the
 // sum (at most 96 terms).
-__global__ void k_se3_twist_grad(const double *twist, const double *g_in, double *g_out, int B) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= B) return;
-  double ad[36] = {0};
+//
+// Every term ad^n / (n + 1)! has the form [[A, B], [0, A]] (3x3 blocks), so
+// one warp per pair carries its 18 distinct entries, one per lane (lanes
+// 0..8 A row-major, 9..17 B), through the recurrence
+// A' = A phi^ / (n + 1), B' = (A rho^ + B phi^) / (n + 1), the terms in
+// shared memory.  A thread per pair would issue all 36 entries' FP64
+// products and divisions one after the other.
+constexpr int kTwistWarps = 4;  // pairs per block
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Column j of the hat matrix of (x, y, z): [[0, -z, y], [z, 0, -x], [-y, x, 0]].
+__device__ __forceinline__ void hat_column(double x, double y, double z, int j, double c[3]) {
+  c[0] = j == 0 ? 0.0 : (j == 1 ? -z : y);
+  c[1] = j == 0 ? z : (j == 1 ? 0.0 : -x);
+  c[2] = j == 0 ? -y : (j == 1 ? x : 0.0);
+}
+
+__global__ void __launch_bounds__(32 * kTwistWarps)
+    k_se3_twist_grad(const double *twist, const double *g_in, double *g_out, int B) {
+  __shared__ double s_term[kTwistWarps][18], s_sum[kTwistWarps][18];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int p = blockIdx.x * kTwistWarps + w;
+  if (p >= B) return;  // the whole warp
   const double r0 = twist[p * 6], r1 = twist[p * 6 + 1], r2 = twist[p * 6 + 2];
   const double w0 = twist[p * 6 + 3], w1 = twist[p * 6 + 4], w2 = twist[p * 6 + 5];
-  auto put_hat = [&](int r, int c, double x, double y, double z) {
-    ad[(r + 0) * 6 + c + 1] = -z;
-    ad[(r + 0) * 6 + c + 2] = y;
-    ad[(r + 1) * 6 + c + 0] = z;
-    ad[(r + 1) * 6 + c + 2] = -x;
-    ad[(r + 2) * 6 + c + 0] = -y;
-    ad[(r + 2) * 6 + c + 1] = x;
-  };
-  put_hat(0, 0, w0, w1, w2);
-  put_hat(0, 3, r0, r1, r2);
-  put_hat(3, 3, w0, w1, w2);
-  double S[36], term[36], next[36];
-  for (int k = 0; k < 36; ++k) S[k] = term[k] = (k % 7 == 0) ? 1.0 : 0.0;
+  const bool mine = lane < 18, in_a = lane < 9;
+  const int e = in_a ? lane : (mine ? lane - 9 : 0);
+  const int i = e / 3, j = e % 3;
+  double wc[3], rc[3];
+  hat_column(w0, w1, w2, j, wc);
+  hat_column(r0, r1, r2, j, rc);
+  // the n = 0 term and the sum: the identity
+  double sum = (lane == 0 || lane == 4 || lane == 8) ? 1.0 : 0.0;
+  if (mine) s_term[w][lane] = sum;
+  __syncwarp();
   for (int n = 1; n <= 96; ++n) {
-    double tmax = 0.0, smax = 0.0;
-    for (int i = 0; i < 6; ++i)
-      for (int j = 0; j < 6; ++j) {
-        double a = 0.0;
-        for (int k = 0; k < 6; ++k) a += term[i * 6 + k] * ad[k * 6 + j];
-        next[i * 6 + j] = a / (double)(n + 1);
+    double a = 0.0;
+    if (mine) {
+      const double *A = s_term[w], *Bm = s_term[w] + 9;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) a += A[i * 3 + k] * (in_a ? wc[k] : rc[k]);
+      if (!in_a) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a += Bm[i * 3 + k] * wc[k];
       }
-    for (int k = 0; k < 36; ++k) {
-      term[k] = next[k];
-      S[k] += term[k];
-      tmax = fmax(tmax, fabs(term[k]));
-      smax = fmax(smax, fabs(S[k]));
     }
+    const double next = a / (double)(n + 1);
+    __syncwarp();
+    double tabs = 0.0, sabs = 0.0;
+    if (mine) {
+      s_term[w][lane] = next;
+      sum += next;
+      tabs = fabs(next);
+      sabs = fabs(sum);
+    }
+    __syncwarp();
+    const double tmax = warp_max(tabs), smax = warp_max(sabs);
     if (tmax <= 1e-20 * smax) break;
   }
-  double g[6];
-  for (int k = 0; k < 6; ++k) g[k] = g_in[p * 6 + k];
-  for (int j = 0; j < 6; ++j) {
-    double a = 0.0;
-    for (int i = 0; i < 6; ++i) a += S[i * 6 + j] * g[i];
-    g_out[p * 6 + j] = a;
+  if (mine) s_sum[w][lane] = sum;
+  __syncwarp();
+  if (lane < 6) {
+    // column `lane` of J_l = [[SA, SB], [0, SA]] against g
+    const double *SA = s_sum[w], *SB = s_sum[w] + 9;
+    const int c = lane;
+    double acc = 0.0;
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+      const double s = r < 3 ? (c < 3 ? SA[r * 3 + c] : SB[r * 3 + c - 3])
+                             : (c < 3 ? 0.0 : SA[(r - 3) * 3 + c - 3]);
+      acc += s * g_in[p * 6 + r];
+    }
+    g_out[p * 6 + c] = acc;
   }
 }
 
@@ -496,8 +533,8 @@ extern "C" int stb_se3_twist_grad(const double *twist, const double *grad_tangen
   STB_TRY(check_device_ptr(twist, "twist"));
   STB_TRY(check_device_ptr(grad_tangent, "grad_tangent"));
   STB_TRY(check_device_ptr(grad_twist, "grad_twist"));
-  k_se3_twist_grad<<<(num_pairs + 63) / 64, 64, 0, as_stream(stream)>>>(twist, grad_tangent,
-                                                                      grad_twist, num_pairs);
+  k_se3_twist_grad<<<(num_pairs + kTwistWarps - 1) / kTwistWarps, 32 * kTwistWarps, 0,
+                     as_stream(stream)>>>(twist, grad_tangent, grad_twist, num_pairs);
   return check_launch("stb_se3_twist_grad");
 }
 
