@@ -252,7 +252,7 @@ __device__ __forceinline__ float2 dw_of_double(double x) {
 // side entry, so that a column step is one product and one difference for
 // all entries.  Then Tn = exp(x) T, also in double-words: within ~1e-14 of
 // the FP64 update, so the float32 view of the pose (its high words) is
-// that of the FP64 pose.  Returns the verdict (uniform); on success lanes
+// that of the FP64 pose.  Returns the solve status (warp-uniform); on success lanes
 // 0..15 hold Tn's entries in tn_out (lane k -> entry k), and every lane
 // holds x rounded to float32 in xs (for the finiteness test).
 __device__ inline bool warp_gn_update(const float2 *up, const float2 *bv, const float2 *T,

@@ -359,7 +359,7 @@ __device__ __forceinline__ void load_state_view(StateView &V, const State *S) {
 // No FP64 instruction is on this path: the FP64 result block is written
 // once per registration by the information pass.  When a history is
 // recorded, warp 1 writes this iteration's FP64 record meanwhile and, after
-// the verdict (named barrier 1), its pose.
+// the solve status is known (named barrier 1), its pose.
 __device__ void gn_step(const Job *J, const StateView &V, const float2 *totw, int iter) {
   __shared__ float rt32[12];
   __shared__ float2 s_tn[16];

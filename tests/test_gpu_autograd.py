@@ -3,7 +3,7 @@ ExpRtToMatrix / MatrixToExpRt (twist <-> [R | t]) against the FP64
 oracle and autograd's gradcheck, the frame point-cloud matcher's forward
 and backward bit for bit against the float32 restatement (on a
 correspondence map that is itself checked bit for bit), and the
-AutogradICP driver on a synthetic pair."""
+AutogradICP optimisation loop on a synthetic pair."""
 import math
 
 import numpy as np
