@@ -12,6 +12,7 @@ import torch
 from . import _build
 
 STB_OK = 0
+STB_EINVAL, STB_EDEVICE, STB_EDTYPE, STB_ECUDA, STB_ETIMEOUT = 1, 2, 3, 4, 5
 STB_F32 = 0
 STB_BF16 = 1
 STB_F32_HWC = 2   # texel-major feature layout [count][channels]

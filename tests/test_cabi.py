@@ -1,6 +1,9 @@
 """The C-ABI library builds, loads, and exports every function the public
 header declares (no GPU needed: only host-side entry points are called)."""
+import ctypes
 import pathlib
+
+import pytest
 
 from slamtb_gb300 import _build, _native
 
@@ -25,3 +28,56 @@ def test_host_only_entry_points():
     big = lib.stb_icp_workspace_bytes(640 * 480, 480, 640)
     assert 0 < small < big
     assert big >= 8 * 640 * 480
+
+
+# Entry points whose arguments are all checked on the host before any device
+# work: every one of them turns null pointers and empty or invalid sizes into
+# a status code and a "Check failed:" message (the reference's error prefix,
+# error.hpp) without touching memory.
+_CHECKED = sorted(n for n, (res, args) in _native._SIGNATURES.items()
+                  if res is ctypes.c_int and args and not n.startswith("stb_profile_"))
+# A batch of zero twists is an empty operation, as for an empty torch tensor.
+_EMPTY_OK = {"stb_exp_rt_to_matrix", "stb_exp_rt_to_matrix_backward", "stb_matrix_to_exp_rt"}
+
+
+def _arguments(args, size):
+    out = []
+    for a in args:
+        if a in (ctypes.c_float, ctypes.c_double):
+            out.append(0.0)
+        elif a in (ctypes.c_void_p, ctypes.c_char_p):
+            out.append(None)
+        else:
+            out.append(size)
+    return out
+
+
+@pytest.mark.parametrize("size", [0, 4])
+def test_entry_points_reject_bad_arguments(size):
+    lib = _native.lib()
+    errors = (_native.STB_EINVAL, _native.STB_EDEVICE, _native.STB_EDTYPE)
+    assert len(_CHECKED) >= 25
+    for name in _CHECKED:
+        rc = getattr(lib, name)(*_arguments(_native._SIGNATURES[name][1], size))
+        if size == 0 and name in _EMPTY_OK:
+            assert rc == _native.STB_OK, name
+            continue
+        assert rc in errors, (name, rc)
+        msg = lib.stb_last_error()
+        assert msg.startswith(b"Check failed: "), (name, msg)
+        with pytest.raises(RuntimeError, match="^Check failed: "):
+            _native.check(rc)
+
+
+def test_host_tensors_are_refused():
+    """No CPU fallback: host tensors raise, as the reference's device checks
+    do for the wrong device (error.hpp:12-37)."""
+    import torch
+    from slamtb_gb300.camera import KCamera
+    from slamtb_gb300.registration import ICPOdometry
+    kcam = KCamera(torch.tensor([[50.0, 0, 8], [0, 50, 6], [0, 0, 1]]))
+    pts, nrm = torch.rand(12, 16, 3), torch.rand(12, 16, 3)
+    mask = torch.ones(12, 16, dtype=torch.bool)
+    with pytest.raises(RuntimeError, match="Expected a gpu tensor"):
+        ICPOdometry(3).estimate(kcam, pts.view(-1, 3), nrm.view(-1, 3), mask.view(-1),
+                                target_points=pts, target_normals=nrm, target_mask=mask)
