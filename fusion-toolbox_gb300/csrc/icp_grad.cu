@@ -275,7 +275,8 @@ __device__ __forceinline__ void load_round(const LossArgs &a, size_t po, int npi
   }
 }
 
-// r = (q - Tp) . n of pixel k of a round (the value residual() computes).
+// r = (q - Tp) . n of pixel k of a round (icp_jacobian_geometric.cu:82), with Tp the
+// transformed back-projection of the winner and q, n the target point and normal.
 __device__ __forceinline__ float round_residual(const LossArgs &a, const Pose32 &P,
                                                 const Round &R, int k, float3 &Tp,
                                                 float3 &n) {
