@@ -2,6 +2,7 @@
 import math
 
 import numpy as np
+import pytest
 
 from oracle import icp_oracle as io
 from oracle import port
@@ -11,9 +12,6 @@ from _helpers import synthetic_pair
 def _rel(a, b):
     d = io.se3_log(np.linalg.inv(b) @ a)
     return np.linalg.norm(d) / max(np.linalg.norm(io.se3_log(b)), 1e-3)
-
-
-import pytest
 
 
 @pytest.mark.parametrize("iters,wf", [(6, 0.0), (1, 0.1)])
@@ -36,3 +34,26 @@ def test_port_matches_numpy_oracle(iters, wf):
     assert _rel(p["transform"], o.transform) < 1e-5
     assert p["match_ratio"] == o.match_ratio
     np.testing.assert_allclose(p["information"], o.information, rtol=1e-6)
+
+
+@pytest.mark.parametrize("empty", ["source", "target"])
+def test_port_and_oracle_without_matches(empty):
+    """No valid source (or target) pixel: the first solve fails (JᵀJ = 0), so
+    both stop before any update (icp.py:236-242 `break`) and report no
+    transform, zero match ratio, an infinite residual and a zero
+    information matrix, as the GPU path's empty result does."""
+    d = synthetic_pair(6, width=64, height=48, feature_channels=0)
+    s, t = d["src"], d["tgt"]
+    sm = np.zeros_like(s["mask"]) if empty == "source" else s["mask"]
+    tm = np.zeros_like(t["mask"]) if empty == "target" else t["mask"]
+    kw = dict(num_iters=3, geom_weight=1.0, feat_weight=0.0, distance_threshold=0.1,
+              normals_angle_thresh=math.radians(20))
+    o = io.icp_estimate(d["kcam"], s["points"], s["normals"], sm, t["points"], t["normals"],
+                        tm, **kw)
+    p = port.icp_estimate(d["kcam"], s["points"], s["normals"], sm, t["points"], t["normals"],
+                          tm, threads=2, **kw)
+    assert o.transform is None and p["transform"] is None
+    assert len(o.history) == p["iters"] == 0
+    assert o.match_ratio == p["match_ratio"] == 0.0
+    assert math.isinf(o.residual) and math.isinf(p["residual"])
+    assert not np.any(o.information) and not np.any(p["information"])
