@@ -210,19 +210,9 @@ __host__ __device__ constexpr int tri_lane(int i, int k) { return 6 * k - k * (k
 
 // Maclaurin coefficient n (in t^2) of A = sin t / t (which = 0),
 // B = (1 - cos t) / t^2 (1) or C = (t - sin t) / t^3 (2): (-1)^n / (2n + 1 +
-// which)!, n < 8.  n is a compile-time constant, which a per-lane select.
-template <int n>
-__device__ __forceinline__ double se3_series_coeff(int which) {
-  constexpr double f[18] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0,
-                            3628800.0, 39916800.0, 479001600.0, 6227020800.0, 87178291200.0,
-                            1307674368000.0, 20922789888000.0, 355687428096000.0};
-  constexpr double s = (n & 1) ? -1.0 : 1.0;
-  constexpr double ca = s / f[2 * n + 1], cb = s / f[2 * n + 2], cc = s / f[2 * n + 3];
-  return which == 0 ? ca : (which == 1 ? cb : cc);
-}
-
-// The same coefficient as a double-word constant (hi = the float32
-// rounding, lo = the float32 rounding of the remainder).
+// which)!, n < 8, as a double-word constant (hi = the float32 rounding, lo =
+// the float32 rounding of the remainder).  n is a compile-time constant,
+// which a per-lane select.
 template <int n>
 __device__ __forceinline__ dw se3_series_coeff_dw(int which) {
   constexpr double f[18] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0,

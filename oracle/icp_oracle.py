@@ -245,10 +245,6 @@ def associate32(src_points, src_normals, src_mask, rt, tgt_points,
                        ref.astype(np.int64).reshape(h, w))
 
 
-def ref_map_from_association(assoc):
-    return assoc.ref_map
-
-
 def winners_from_ref_map(ref_map):
     """Source index per target pixel of a reference-layout map
     (``MergeMapAccessor``, merge_map.hpp:91-93): ``map >> 32``."""
