@@ -51,6 +51,14 @@ def load_frame_depth(path=HERE / "frame_depth.npz"):
     return np.cumsum(z["depth_dx"].astype(np.int32), axis=1).astype(np.uint16)
 
 
+def _row_differences(depth):
+    """int16 row-wise first differences of a uint16 image; the loaders undo
+    them with a cumulative sum, so every difference must fit in int16."""
+    dx = np.diff(depth.astype(np.int32), axis=1, prepend=0)
+    assert np.abs(dx).max() <= np.iinfo(np.int16).max, "depth step does not fit int16"
+    return dx.astype(np.int16)
+
+
 def main(reference_root):
     root = pathlib.Path(reference_root) / "test-data" / "rgbd" / "sample2"
     meta = json.load(open(root / "frames.json"))["root"]
@@ -61,8 +69,7 @@ def main(reference_root):
         assert depth.dtype == np.uint16 and depth.shape == (480, 640)
         info = entry["info"]
         # row-wise first differences compress ~2.3x better than raw depth
-        out[f"depth_dx_{i}"] = np.diff(depth.astype(np.int32), axis=1,
-                                       prepend=0).astype(np.int16)
+        out[f"depth_dx_{i}"] = _row_differences(depth)
         out[f"rt_cam_{i}"] = np.array(info["rt_cam"]["matrix"], dtype=np.float64)
         out[f"kcam_{i}"] = np.array(info["kcam"]["matrix"], dtype=np.float32)
         out[f"depth_scale_{i}"] = np.float32(info["depth_scale"])
@@ -72,9 +79,7 @@ def main(reference_root):
     depth = read_png(pathlib.Path(reference_root) / "slamtb" / "_test" / "assets" /
                      "frame_depth.png")
     assert depth.dtype == np.uint16
-    np.savez_compressed(HERE / "frame_depth.npz",
-                        depth_dx=np.diff(depth.astype(np.int32), axis=1,
-                                         prepend=0).astype(np.int16))
+    np.savez_compressed(HERE / "frame_depth.npz", depth_dx=_row_differences(depth))
     print("wrote", HERE / "frame_depth.npz")
 
 
