@@ -1,6 +1,7 @@
 """Self-tests of the CPU oracle (no GPU): SE(3) algebra, the Jacobian sign
-conventions against finite differences, the 6x6 solve, and hand-built
-association cases (ties, bounds, thresholds, NaN angle)."""
+conventions against finite differences, the 6x6 solve, hand-built
+association cases (ties, bounds, thresholds, NaN angle), and the vectorised
+association against a literal per-point loop of the reference's steps."""
 import math
 
 import numpy as np
@@ -396,3 +397,98 @@ def test_fpcl_matcher_oracle_matches_literal_loops():
         np.testing.assert_array_equal(dx[i], [F(j00 * gu), F(j11 * gv),
                                               F(F(j02 * gu) + F(j12 * gv))])
     assert mask.sum() >= 4
+
+
+def _round_half_away(x):
+    """C ``round`` on a float32 value (exact in float64)."""
+    return int(math.copysign(math.floor(abs(float(x)) + 0.5), float(x)))
+
+
+def _associate_literal(sp, sn, sm, rt, tp, tn, tm, kcam, dist_th, angle_th):
+    """Per source point, in index order, the reference's own steps in
+    float32 scalars: ``CorrespondenceMapKernel`` (correspondence_map.cu:39-61)
+    -> ``RigidTransform::Transform/TransformNormal`` (camera.hpp:134-165) ->
+    ``RobustCorrespondence::Match`` (correspondence.hpp:69-89: project,
+    round, bounds, target mask, squared distance, ``GetVectorsAngle``,
+    math.hpp:14-18) -> ``MergeMap::Set`` (merge_map.hpp:37-50: replace when
+    the distance is smaller, so a tie keeps the first, smaller index)."""
+    f = np.float32
+    h, w = tm.shape
+    nm = io.normal_matrix32(rt)
+    d2 = f(float(dist_th) * float(dist_th))
+    ath = f(angle_th)
+    fx, cx, fy, cy = f(kcam[0, 0]), f(kcam[0, 2]), f(kcam[1, 1]), f(kcam[1, 2])
+    best = {}
+    for i in range(sp.shape[0]):
+        if sm.size == sp.shape[0] and not sm[i]:
+            continue
+        p = [((rt[k, 0] * sp[i, 0] + rt[k, 1] * sp[i, 1]) + rt[k, 2] * sp[i, 2]) + rt[k, 3]
+             for k in range(3)]
+        n = [(nm[k, 0] * sn[i, 0] + nm[k, 1] * sn[i, 1]) + nm[k, 2] * sn[i, 2] for k in range(3)]
+        u = (fx * p[0]) / p[2] + cx
+        v = (fy * p[1]) / p[2] + cy
+        ui, vi = _round_half_away(u), _round_half_away(v)
+        if ui < 0 or ui >= w or vi < 0 or vi >= h or not tm[vi, ui]:
+            continue
+        q, m = tp[vi, ui], tn[vi, ui]
+        d = [q[k] - p[k] for k in range(3)]
+        sq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]
+        if sq > d2:
+            continue
+        dot = (n[0] * m[0] + n[1] * m[1]) + n[2] * m[2]
+        na = np.sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])
+        nb = np.sqrt((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2])
+        with np.errstate(invalid="ignore"):
+            angle = abs(np.arccos(dot / (na * nb)))
+        if angle >= ath:
+            continue
+        dist = np.sqrt(sq)
+        if (vi, ui) not in best or dist < best[(vi, ui)][0]:
+            best[(vi, ui)] = (dist, i)
+    return best
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_association_matches_the_reference_steps_point_by_point(seed):
+    """The vectorised float32 association (the bit-exact gate of the GPU
+    kernels) equals a literal per-point loop of the reference's steps:
+    winners, distance bits and the int64 map layout (index << 32 | distance
+    bits, empty = 0x0fffffff7f800000), with duplicated source points so
+    that distance ties occur."""
+    rng = np.random.default_rng(seed)
+    h, w = 18, 24
+    kcam = np.array([[30.0, 0, 11.5], [0, 30.0, 8.5], [0, 0, 1]], dtype=np.float32)
+    vv, uu = np.mgrid[0:h, 0:w].astype(np.float32)
+    z = (1.2 + 0.3 * uu / w + 0.2 * vv / h + rng.normal(0, 0.005, size=(h, w))).astype(np.float32)
+    tp = np.stack([(uu - kcam[0, 2]) * z / kcam[0, 0], (vv - kcam[1, 2]) * z / kcam[1, 1], z],
+                  axis=-1).astype(np.float32)
+    tn = rng.normal(size=(h, w, 3)).astype(np.float32)
+    tn[..., 2] = -np.abs(tn[..., 2]) - 0.5
+    tm = rng.random((h, w)) > 0.15
+    sp = (tp.reshape(-1, 3) + rng.normal(0, 0.03, size=(h * w, 3))).astype(np.float32)
+    sn = (tn.reshape(-1, 3) + rng.normal(0, 0.1, size=(h * w, 3))).astype(np.float32)
+    dup = rng.choice(h * w, size=40, replace=False)
+    sp[dup[20:]], sn[dup[20:]] = sp[dup[:20]], sn[dup[:20]]  # ties
+    sm = rng.random(h * w) > 0.1
+    ang = 0.02 * seed
+    rt = np.array([[math.cos(ang), -math.sin(ang), 0, 0.01], [math.sin(ang), math.cos(ang), 0, 0],
+                   [0, 0, 1, 0.005], [0, 0, 0, 1]], dtype=np.float32)
+    dth, ath = 0.1, math.radians(30)
+    a = io.associate32(sp, sn, sm, rt, tp, tn, tm, kcam, dth, ath)
+    best = _associate_literal(sp, sn, sm, rt, tp, tn, tm, kcam, dth, ath)
+    assert len(best) > 100
+    winners = np.full((h, w), -1, dtype=np.int64)
+    dist = np.full((h, w), np.inf, dtype=np.float32)
+    for (vi, ui), (d, i) in best.items():
+        winners[vi, ui], dist[vi, ui] = i, d
+    np.testing.assert_array_equal(a.winner, winners)
+    np.testing.assert_array_equal(a.dist.view(np.uint32), dist.view(np.uint32))
+    ref = np.where(winners >= 0, (winners << 32) | dist.view(np.uint32).astype(np.int64),
+                   np.int64(io.CORRESP_EMPTY))
+    np.testing.assert_array_equal(a.ref_map, ref)
+    # ties: both copies of a duplicated point valid, so both reach the same
+    # pixel at the same distance; the smaller index holds it
+    won = set(winners[winners >= 0].tolist())
+    ties = [(a, b) for a, b in zip(dup[:20].tolist(), dup[20:].tolist())
+            if sm[a] and sm[b] and (a in won or b in won)]
+    assert ties and all(min(a, b) in won and max(a, b) not in won for a, b in ties)
