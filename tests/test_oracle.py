@@ -1,7 +1,8 @@
 """Self-tests of the CPU oracle (no GPU): SE(3) algebra, the Jacobian sign
 conventions against finite differences, the 6x6 solve, hand-built
 association cases (ties, bounds, thresholds, NaN angle), and the vectorised
-association against a literal per-point loop of the reference's steps."""
+association and feature partials against literal per-point loops of the
+reference's steps."""
 import math
 
 import numpy as np
@@ -492,3 +493,108 @@ def test_association_matches_the_reference_steps_point_by_point(seed):
     ties = [(a, b) for a, b in zip(dup[:20].tolist(), dup[20:].tolist())
             if sm[a] and sm[b] and (a in won or b in won)]
     assert ties and all(min(a, b) in won and max(a, b) not in won for a, b in ties)
+
+
+def _feature_partials_literal(sp, sf, sm, rt, tf, kcam, ref_map, thresh):
+    """Per source point, the reference's ``FeatureJacobianKernel``
+    (icp_jacobian_feature.cu:58-109) in float32 scalars: ``BilinearInterp``
+    with C truncation and zero taps past the right / bottom edge,
+    ``BilinearInterpGrad`` at (u + h, v), (max(u - h, 0), v), ... with the
+    divisor 1 / (2h) (feature_map.hpp:15-63), ``Dx_Project`` (camera.hpp:
+    65-78) and ``SE3ICPJacobian::Compute`` assigning the partials per
+    channel (icp_jacobian_common.hpp:37-61)."""
+    f = np.float32
+    c, h, w = tf.shape
+    n = sp.shape[0]
+    JtJ = np.zeros((n, 6, 6), f)
+    Jtr = np.zeros((n, 6), f)
+    r2 = np.zeros(n, f)
+    fx, cx, fy, cy = f(kcam[0, 0]), f(kcam[0, 2]), f(kcam[1, 1]), f(kcam[1, 2])
+    step = f(0.05)
+    div = f(1) / (f(2) * step)
+    count = 0
+
+    def interp(ch, u, v):
+        ui, vi = int(u), int(v)  # truncation toward zero, as int(scalar_t)
+        ur, vr = u - f(ui), v - f(vi)
+        m = tf[ch]
+        v00 = m[vi, ui]
+        v10 = m[vi, ui + 1] if ui + 1 < w else f(0)
+        v01 = m[vi + 1, ui] if vi + 1 < h else f(0)
+        v11 = m[vi + 1, ui + 1] if ui + 1 < w and vi + 1 < h else f(0)
+        a0 = v00 * (f(1) - ur) + v10 * ur
+        a1 = v01 * (f(1) - ur) + v11 * ur
+        return a0 * (f(1) - vr) + a1 * vr
+
+    for i in range(n):
+        if not sm[i]:
+            continue
+        p = [((rt[k, 0] * sp[i, 0] + rt[k, 1] * sp[i, 1]) + rt[k, 2] * sp[i, 2]) + rt[k, 3]
+             for k in range(3)]
+        u = (fx * p[0]) / p[2] + cx
+        v = (fy * p[1]) / p[2] + cy
+        ui, vi = _round_half_away(u), _round_half_away(v)
+        if ui < 0 or ui >= w or vi < 0 or vi >= h or (int(ref_map[vi, ui]) >> 32) != i:
+            continue
+        z2 = p[2] * p[2]
+        j00, j02 = fx / p[2], (-p[0] * fx) / z2
+        j11, j12 = fy / p[2], (-p[1] * fy) / z2
+        sq = f(0)
+        for ch in range(c):
+            r = interp(ch, u, v) - sf[ch, i]
+            du = (interp(ch, u + step, v) - interp(ch, max(u - step, f(0)), v)) * div
+            dv = (interp(ch, u, v + step) - interp(ch, u, max(v - step, f(0)))) * div
+            g = [du * j00, dv * j11, du * j02 + dv * j12]
+            J = g + [p[1] * g[2] - p[2] * g[1], p[2] * g[0] - p[0] * g[2],
+                     p[0] * g[1] - p[1] * g[0]]
+            for a in range(6):
+                Jtr[i, a] = J[a] * r
+                for b in range(6):
+                    JtJ[i, a, b] = J[b] * J[a]
+            sq = sq + r * r
+        if sq > f(thresh) * f(thresh):
+            JtJ[i], Jtr[i] = 0, 0
+            continue
+        r2[i] = sq
+        count += 1
+    return JtJ, Jtr, r2, count
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_feature_partials_match_the_reference_steps_point_by_point(seed):
+    """The vectorised float32 feature partials equal a literal per-point loop
+    of the reference's kernel bit for bit, on 2 channels (only the last
+    channel's J survives), with projections at the image borders (negative
+    bilinear weights left of column 0, zero taps past the right and bottom
+    edges) and a residual threshold that rejects some matches."""
+    rng = np.random.default_rng(seed)
+    h, w, c = 14, 20, 2
+    kcam = np.array([[24.0, 0, 9.5], [0, 24.0, 6.5], [0, 0, 1]], dtype=np.float32)
+    vv, uu = np.mgrid[0:h, 0:w].astype(np.float32)
+    z = (1.3 + 0.2 * uu / w + 0.1 * vv / h).astype(np.float32)
+    tp = np.stack([(uu - kcam[0, 2]) * z / kcam[0, 0], (vv - kcam[1, 2]) * z / kcam[1, 1], z],
+                  axis=-1).astype(np.float32)
+    tn = np.broadcast_to(np.array([0, 0, -1], np.float32), (h, w, 3)).copy()
+    tm = np.ones((h, w), bool)
+    sp = (tp.reshape(-1, 3) + rng.normal(0, 0.02, size=(h * w, 3))).astype(np.float32)
+    sn = tn.reshape(-1, 3).copy()
+    sm = rng.random(h * w) > 0.05
+    rt = np.eye(4, dtype=np.float32)
+    tf = rng.random((c, h, w)).astype(np.float32)
+    sf = rng.random((c, h * w)).astype(np.float32)
+    thresh = 0.6
+    ref_map = io.associate32(sp, sn, sm, rt, tp, tn, tm, kcam, 0.1, math.radians(30)).ref_map
+    JtJ, Jtr, r2, cnt, passed = io.feature_partials32(sp, sf, sm, rt, tf, kcam, ref_map, thresh)
+    lJtJ, lJtr, lr2, lcnt = _feature_partials_literal(sp, sf, sm, rt, tf, kcam, ref_map, thresh)
+    assert cnt == lcnt > 50
+    np.testing.assert_array_equal(Jtr.view(np.uint32), lJtr.view(np.uint32))
+    np.testing.assert_array_equal(JtJ.view(np.uint32), lJtJ.view(np.uint32))
+    np.testing.assert_array_equal(r2.view(np.uint32), lr2.view(np.uint32))
+    # the border and threshold cases occurred
+    T = io.transform32(rt, sp)
+    u, v = io.project32(kcam, T)
+    winners = set(io.winners_from_ref_map(ref_map)[ref_map != io.CORRESP_EMPTY].tolist())
+    won = np.array(sorted(winners))
+    assert np.any(u[won] < 0) or np.any(v[won] < 0)
+    assert np.any(u[won] + np.float32(0.05) >= w - 1) or np.any(v[won] + np.float32(0.05) >= h - 1)
+    assert cnt < len(won)  # the threshold rejected some matches
