@@ -1,8 +1,8 @@
 """Self-tests of the CPU oracle (no GPU): SE(3) algebra, the Jacobian sign
 conventions against finite differences, the 6x6 solve, hand-built
 association cases (ties, bounds, thresholds, NaN angle), and the vectorised
-association and feature partials against literal per-point loops of the
-reference's steps."""
+association and the geometric, feature and information partials against
+literal per-point loops of the reference's steps."""
 import math
 
 import numpy as np
@@ -598,3 +598,66 @@ def test_feature_partials_match_the_reference_steps_point_by_point(seed):
     assert np.any(u[won] < 0) or np.any(v[won] < 0)
     assert np.any(u[won] + np.float32(0.05) >= w - 1) or np.any(v[won] + np.float32(0.05) >= h - 1)
     assert cnt < len(won)  # the threshold rejected some matches
+
+
+def test_geometric_and_information_partials_match_the_reference_steps():
+    """``GeometricJacobianKernel`` and ``InformationMatrixKernel``
+    (icp_jacobian_geometric.cu:54-85,118-158) as literal per-point loops in
+    float32 scalars equal the vectorised partials bit for bit: r = (q - Tp).n,
+    J = [n; Tp x n] with the partials assigned by
+    ``SE3ICPJacobian::Compute``, and G^T G summed row by row from the
+    matched target point."""
+    f = np.float32
+    rng = np.random.default_rng(4)
+    h, w = 16, 22
+    kcam = np.array([[26.0, 0, 10.5], [0, 26.0, 7.5], [0, 0, 1]], dtype=np.float32)
+    vv, uu = np.mgrid[0:h, 0:w].astype(np.float32)
+    z = (1.1 + 0.3 * uu / w + 0.2 * vv / h).astype(np.float32)
+    tp = np.stack([(uu - kcam[0, 2]) * z / kcam[0, 0], (vv - kcam[1, 2]) * z / kcam[1, 1], z],
+                  axis=-1).astype(np.float32)
+    tn = rng.normal(size=(h, w, 3)).astype(np.float32)
+    tn[..., 2] = -np.abs(tn[..., 2]) - 1.0
+    tm = rng.random((h, w)) > 0.1
+    sp = (tp.reshape(-1, 3) + rng.normal(0, 0.02, size=(h * w, 3))).astype(np.float32)
+    sn = (tn.reshape(-1, 3) + rng.normal(0, 0.05, size=(h * w, 3))).astype(np.float32)
+    sm = rng.random(h * w) > 0.05
+    rt = np.array([[1, -0.01, 0, 0.004], [0.01, 1, 0, -0.002], [0, 0, 1, 0.003], [0, 0, 0, 1]],
+                  dtype=np.float32)
+    ref_map = io.associate32(sp, sn, sm, rt, tp, tn, tm, kcam, 0.1, math.radians(30)).ref_map
+    JtJ, Jtr, r2, cnt = io.geometric_partials32(sp, sm, rt, tp, tn, kcam, ref_map)
+    GtG = io.information_partials32(sp, sm, rt, tp, kcam, ref_map)
+
+    n = sp.shape[0]
+    lJtJ, lJtr, lr2, lG = (np.zeros((n, 6, 6), f), np.zeros((n, 6), f), np.zeros(n, f),
+                           np.zeros((n, 6, 6), f))
+    lcnt = 0
+    fx, cx, fy, cy = f(kcam[0, 0]), f(kcam[0, 2]), f(kcam[1, 1]), f(kcam[1, 2])
+    for i in range(n):
+        if not sm[i]:
+            continue
+        p = [((rt[k, 0] * sp[i, 0] + rt[k, 1] * sp[i, 1]) + rt[k, 2] * sp[i, 2]) + rt[k, 3]
+             for k in range(3)]
+        ui = _round_half_away((fx * p[0]) / p[2] + cx)
+        vi = _round_half_away((fy * p[1]) / p[2] + cy)
+        if ui < 0 or ui >= w or vi < 0 or vi >= h or (int(ref_map[vi, ui]) >> 32) != i:
+            continue
+        q, m = tp[vi, ui], tn[vi, ui]
+        lcnt += 1
+        d = [q[k] - p[k] for k in range(3)]
+        r = (d[0] * m[0] + d[1] * m[1]) + d[2] * m[2]
+        J = [m[0], m[1], m[2], p[1] * m[2] - p[2] * m[1], p[2] * m[0] - p[0] * m[2],
+             p[0] * m[1] - p[1] * m[0]]
+        for a in range(6):
+            lJtr[i, a] = J[a] * r
+            for b in range(6):
+                lJtJ[i, a, b] = J[b] * J[a]
+        lr2[i] = r * r
+        rows = ([f(0), q[2], -q[1], f(1), f(0), f(0)], [-q[2], f(0), q[0], f(0), f(1), f(0)],
+                [q[1], -q[0], f(0), f(0), f(0), f(1)])
+        for a in range(6):
+            for b in range(6):
+                lG[i, a, b] = (rows[0][a] * rows[0][b] + rows[1][a] * rows[1][b]) + \
+                    rows[2][a] * rows[2][b]
+    assert cnt == lcnt > 100
+    for x, y in ((JtJ, lJtJ), (Jtr, lJtr), (r2, lr2), (GtG, lG)):
+        np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
