@@ -661,3 +661,93 @@ def test_geometric_and_information_partials_match_the_reference_steps():
     assert cnt == lcnt > 100
     for x, y in ((JtJ, lJtJ), (Jtr, lJtr), (r2, lr2), (GtG, lG)):
         np.testing.assert_array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_normals_and_xyz_downsample_match_the_reference_steps():
+    """``CentralDifferencesKernel`` (normals.cu:27-100) and the
+    nearest-to-mean XYZ downsample (downsample.cu:25-72) as literal
+    per-pixel loops in float32 scalars equal the vectorised restatements
+    bit for bit, on a surface with depth jumps (both ratio branches) and
+    masked pixels."""
+    f = np.float32
+    rng = np.random.default_rng(5)
+    h, w = 12, 15
+    k = np.array([[20.0, 0, 7.0], [0, 20.0, 5.5], [0, 0, 1]], dtype=np.float32)
+    depth = (1.0 + 0.05 * rng.random((h, w))).astype(np.float32)
+    depth[:, 9:] += f(0.4)  # a step: one-sided differences next to it
+    depth[4, 3] += f(0.2)
+    xyz = fp.depth_to_points(depth, k)
+    mask = rng.random((h, w)) > 0.15
+
+    def v3(r, c):
+        return [xyz[r, c, 0], xyz[r, c, 1], xyz[r, c, 2]]
+
+    def sub(a, b):
+        return [a[0] - b[0], a[1] - b[1], a[2] - b[2]]
+
+    def sq(a):
+        return (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2]
+
+    zero = [f(0), f(0), f(0)]
+    normals = np.zeros((h, w, 3), f)
+    for r in range(h):
+        for c in range(w):
+            if not mask[r, c]:
+                continue
+            ce = v3(r, c)
+            le = v3(r, c - 1) if c > 0 and mask[r, c - 1] else zero
+            ri = v3(r, c + 1) if c < w - 1 and mask[r, c + 1] else zero
+            to = v3(r - 1, c) if r > 0 and mask[r - 1, c] else zero
+            bo = v3(r + 1, c) if r < h - 1 and mask[r + 1, c] else zero
+            t2 = f(2.0) * f(2.0)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                lds, rds = sq(sub(le, ce)), sq(sub(ri, ce))
+                ratio = lds / rds
+                if ratio < t2 and ratio > f(1.0) / t2:
+                    l2r = sub(ri, le)
+                elif lds < rds:
+                    l2r = sub(ce, le)
+                else:
+                    l2r = sub(ri, ce)
+                bds, tds = sq(sub(bo, ce)), sq(sub(to, ce))
+                ratio = bds / tds
+                if ratio < t2 and ratio > f(1.0) / t2:
+                    b2t = sub(to, bo)
+                elif bds < tds:
+                    b2t = sub(ce, bo)
+                else:
+                    b2t = sub(to, ce)
+            n = [l2r[1] * b2t[2] - l2r[2] * b2t[1], l2r[2] * b2t[0] - l2r[0] * b2t[2],
+                 l2r[0] * b2t[1] - l2r[1] * b2t[0]]
+            length = np.sqrt(sq(n))
+            normals[r, c] = [f(0), f(0), f(-1)] if not length > f(1e-6) else \
+                [n[0] / length, n[1] / length, n[2] / length]
+    np.testing.assert_array_equal(fp.estimate_normals(xyz, mask).view(np.uint32),
+                                  normals.view(np.uint32))
+
+    scale = 0.5
+    inv = f(1) / f(scale)
+    dh, dw = int(h * scale), int(w * scale)
+    down = np.zeros((dh, dw, 3), f)
+    taps = ((0, 0), (0, 1), (1, 0), (1, 1))
+    for r in range(dh):
+        for c in range(dw):
+            r0, c0 = int(f(r) * inv), int(f(c) * inv)
+            valid = [(r0 + a, c0 + b) for a, b in taps
+                     if c0 + b < w and r0 + a < h and mask[r0 + a, c0 + b]]
+            mean = zero
+            for rr, cc in valid:
+                mean = [mean[0] + xyz[rr, cc, 0], mean[1] + xyz[rr, cc, 1],
+                        mean[2] + xyz[rr, cc, 2]]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                cnt = f(len(valid))
+                mean = [mean[0] / cnt, mean[1] / cnt, mean[2] / cnt]
+            best = f(np.inf)
+            for rr, cc in valid:
+                d = sq(sub(v3(rr, cc), mean))
+                if d < best:
+                    best, down[r, c] = d, xyz[rr, cc]
+    np.testing.assert_array_equal(fp.downsample_xyz_nearest(xyz, mask, scale).view(np.uint32),
+                                  down.view(np.uint32))
+    assert mask.sum() > 100
+    assert not np.any(np.all(normals == 0, axis=-1) & mask)  # every valid pixel has a normal
