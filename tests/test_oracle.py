@@ -751,3 +751,35 @@ def test_normals_and_xyz_downsample_match_the_reference_steps():
                                   down.view(np.uint32))
     assert mask.sum() > 100
     assert not np.any(np.all(normals == 0, axis=-1) & mask)  # every valid pixel has a normal
+
+
+@pytest.mark.parametrize("scale", [0.5, 0.6])
+def test_feature_and_mask_downsample_match_the_reference_steps(scale):
+    """``DownsampleFeatureKernel`` (downsample.cu:133-168: the taps' sum in
+    order, divided by their count) and the nearest mask downsample
+    (downsample.cu:85-116) as literal loops equal the restatements bit for
+    bit, at an odd width and a scale that is not a power of two."""
+    f = np.float32
+    rng = np.random.default_rng(6)
+    c, h, w = 3, 10, 13
+    feats = rng.random((c, h, w)).astype(np.float32)
+    mask = rng.random((h, w)) > 0.3
+    inv = f(1) / f(scale)
+    dh, dw = int(h * scale), int(w * scale)
+    down = np.zeros((c, dh, dw), f)
+    dmask = np.zeros((dh, dw), bool)
+    for r in range(dh):
+        for col in range(dw):
+            r0, c0 = int(f(r) * inv), int(f(col) * inv)
+            dmask[r, col] = mask[r0, c0]
+            for ch in range(c):
+                total, n = f(0), 0
+                for a, b in ((0, 0), (0, 1), (1, 0), (1, 1)):
+                    if c0 + b >= w:
+                        continue
+                    total = total + feats[ch, r0 + a, c0 + b]
+                    n += 1
+                down[ch, r, col] = total / f(n)
+    got = fp.downsample_features(feats, scale)
+    np.testing.assert_array_equal(got.view(np.uint32), down.view(np.uint32))
+    np.testing.assert_array_equal(fp.downsample_mask(mask, scale), dmask)
