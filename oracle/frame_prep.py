@@ -123,8 +123,9 @@ def downsample_xyz_nearest(xyz, mask, scale):
     For each destination pixel the 2x2 source block at ``int(row / scale)``
     is scanned, the mean of its valid points is taken, and the valid point
     nearest to that mean (first one on ties) is kept; a block without valid
-    points gives (0, 0, 0).  Source rows past the image (odd heights) count
-    as invalid; the reference checks only columns and reads past the end.
+    points gives (0, 0, 0).  Source rows past the image (only reachable with
+    a destination taller than ``int(h * scale)``) count as invalid; the
+    reference checks only columns and would read past the end.
     """
     xyz = np.asarray(xyz, dtype=F32)
     m = np.asarray(mask, dtype=bool)
