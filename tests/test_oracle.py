@@ -783,3 +783,21 @@ def test_feature_and_mask_downsample_match_the_reference_steps(scale):
     got = fp.downsample_features(feats, scale)
     np.testing.assert_array_equal(got.view(np.uint32), down.view(np.uint32))
     np.testing.assert_array_equal(fp.downsample_mask(mask, scale), dmask)
+
+
+def test_erosion_matches_the_reference_steps():
+    """``ErodeMaskKernel`` (erode_mask.cu:18-39) as a literal loop over its
+    neighbourhood table {-1,0}, {0,1}, {0,-1}, {0,1} (the row below never
+    checked; neighbours outside the image ignored) equals the restatement."""
+    rng = np.random.default_rng(7)
+    mask = rng.random((17, 23)) > 0.2
+    table = ((-1, 0), (0, 1), (0, -1), (0, 1))
+    out = np.zeros_like(mask)
+    h, w = mask.shape
+    for r in range(h):
+        for c in range(w):
+            out[r, c] = bool(mask[r, c]) and all(
+                not (0 <= r + dr < h and 0 <= c + dc < w) or mask[r + dr, c + dc]
+                for dr, dc in table)
+    np.testing.assert_array_equal(fp.erode_mask(mask), out)
+    assert out.sum() > 50
