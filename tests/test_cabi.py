@@ -1,5 +1,7 @@
-"""The C-ABI library builds, loads, and exports every function the public
-header declares (no GPU needed: only host-side entry points are called)."""
+"""The C ABI without a GPU: the library builds, loads and exports every
+function the public header declares; the header's constants and struct
+layouts match the Python mirror; every entry point turns bad arguments into
+a status code and a "Check failed:" message before any device work."""
 import ctypes
 import pathlib
 
@@ -81,3 +83,51 @@ def test_host_tensors_are_refused():
     with pytest.raises(RuntimeError, match="Expected a gpu tensor"):
         ICPOdometry(3).estimate(kcam, pts.view(-1, 3), nrm.view(-1, 3), mask.view(-1),
                                 target_points=pts, target_normals=nrm, target_mask=mask)
+
+
+def _python_name(name):
+    """Header constant -> its name in slamtb_gb300._native."""
+    for prefix in ("STB_ST_", "STB_RES_", "STB_HIST_"):
+        if name.startswith(prefix):
+            return name[len("STB_"):]
+    return name
+
+
+def test_header_constants_match_the_python_mirror():
+    """Every integer #define of the header (status codes, element types,
+    status bits, result and history layouts) has the same value in
+    slamtb_gb300._native."""
+    import re
+    defs = re.findall(r"^#define (STB_\w+) (\d+)u?\b", HEADER.read_text(), re.M)
+    assert len(defs) >= 30
+    mismatched = [(n, int(v), getattr(_native, _python_name(n), None)) for n, v in defs
+                  if getattr(_native, _python_name(n), None) != int(v)]
+    assert not mismatched, mismatched
+
+
+def test_struct_layouts_match_the_c_compiler(tmp_path):
+    """The ctypes mirrors of stb_level and stb_level_params have the size
+    and field offsets that a C compiler gives the header's structs."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"stb_level": _native.StbLevel, "stb_level_params": _native.StbLevelParams}
+    lines = ['#include <stdio.h>', '#include "slamtb_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'  printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", str(HEADER.parent), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out.splitlines()}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
