@@ -1,6 +1,7 @@
 """Host-side logic of the package that needs no GPU: the rigid transform and
 Huber loss of AutogradICP's closure, the small host inputs handed to the C
-entry by value, and the unpacking of the FP64 result block."""
+entry by value, the unpacking of the FP64 result block, and the level table
+and argument checks of BatchRegistration."""
 import math
 
 import numpy as np
@@ -80,3 +81,29 @@ def test_result_block_unpacking():
     empty = ICPOdometry._result(out, 1200, torch.float32)
     assert empty.transform is None and empty.information is not None
     assert math.isinf(empty.residual)
+
+
+def test_batch_registration_levels_and_argument_checks():
+    """BatchRegistration takes the multiscale estimator list finest first (as
+    MultiscaleRegistration, multiscale.py:11-67) and hands the kernel the
+    levels coarsest first (the order they run, multiscale.py:52-55), each
+    with its own estimator's parameters; bad arguments raise before any
+    device work."""
+    from slamtb_gb300.registration import BatchRegistration, ICPOdometry
+    b = BatchRegistration([(1.0, ICPOdometry(10, feat_weight=0.1)), (0.5, ICPOdometry(5)),
+                           (0.5, ICPOdometry(3, distance_threshold=0.2))])
+    assert b.scales == [1.0, 0.5, 0.5]
+    params, total = b._params()
+    assert total == 18
+    assert [(p.num_iters, p.distance_thresh, p.feat_weight) for p in params] == [
+        (3, pytest.approx(0.2), 1.0), (5, pytest.approx(0.5), 1.0), (10, pytest.approx(0.5), 0.1)]
+    with pytest.raises(ValueError, match="1 to 4 levels"):
+        BatchRegistration([])
+    with pytest.raises(ValueError, match="1 to 4 levels"):
+        BatchRegistration([(1.0, ICPOdometry(1))] * 5)
+    with pytest.raises(TypeError):
+        BatchRegistration([(1.0, object())])
+    with pytest.raises(ValueError, match="feat_channel_mode"):
+        BatchRegistration([(1.0, ICPOdometry(1))], feat_channel_mode="mean")
+    with pytest.raises(ValueError, match="non-empty"):
+        b.prepare([], [])
