@@ -1,7 +1,8 @@
 """Host-side logic of the package that needs no GPU: the rigid transform and
 Huber loss of AutogradICP's closure, the small host inputs handed to the C
 entry by value, the unpacking of the FP64 result block, and the level table
-and argument checks of BatchRegistration."""
+and argument checks of BatchRegistration, and the level loop of
+MultiscaleRegistration."""
 import math
 
 import numpy as np
@@ -107,3 +108,36 @@ def test_batch_registration_levels_and_argument_checks():
         BatchRegistration([(1.0, ICPOdometry(1))], feat_channel_mode="mean")
     with pytest.raises(ValueError, match="non-empty"):
         b.prepare([], [])
+
+
+def test_multiscale_level_loop_hands_transforms_coarse_to_fine():
+    """MultiscaleRegistration.estimate_pyramid (multiscale.py:52-67): the
+    estimators, listed finest first, run on the pyramid coarsest first; each
+    level starts from the previous level's transform, and a level that
+    failed (transform None) hands None -- the identity -- to the next, as
+    the reference does."""
+    from slamtb_gb300.registration import MultiscaleRegistration
+    from slamtb_gb300.registration.result import RegistrationResult
+
+    calls = []
+
+    class Fake:
+        def __init__(self, name, out):
+            self.name, self.out = name, out
+
+        def estimate_frame(self, source, target, source_feats=None, target_feats=None,
+                           transform=None, device=None):
+            calls.append((self.name, source, target, source_feats, transform))
+            return RegistrationResult(self.out)
+
+    T1 = torch.eye(4, dtype=torch.float64) * 2
+    ms = MultiscaleRegistration([(1.0, Fake("fine", "T_fine")), (0.5, Fake("mid", None)),
+                                 (0.5, Fake("coarse", T1))])
+    res = ms.estimate_pyramid(["s_coarse", "s_mid", "s_fine"], ["t_coarse", "t_mid", "t_fine"],
+                              transform="T0")
+    assert [c[0] for c in calls] == ["coarse", "mid", "fine"]
+    assert [(c[1], c[2]) for c in calls] == [("s_coarse", "t_coarse"), ("s_mid", "t_mid"),
+                                              ("s_fine", "t_fine")]
+    assert calls[0][4] == "T0" and calls[1][4] is T1 and calls[2][4] is None
+    assert all(c[3] is None for c in calls)
+    assert res.transform == "T_fine"
