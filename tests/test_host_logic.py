@@ -1,8 +1,7 @@
 """Host-side logic of the package that needs no GPU: the rigid transform and
 Huber loss of AutogradICP's closure, the small host inputs handed to the C
-entry by value, the unpacking of the FP64 result block, and the level table
-and argument checks of BatchRegistration, and the level loop of
-MultiscaleRegistration."""
+entry by value, the unpacking of the FP64 result block, BatchRegistration's
+level table and argument checks, and MultiscaleRegistration's level loop."""
 import math
 
 import numpy as np
