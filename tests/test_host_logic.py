@@ -1,7 +1,8 @@
 """Host-side logic of the package that needs no GPU: the rigid transform and
 Huber loss of AutogradICP's closure, the small host inputs handed to the C
 entry by value, the unpacking of the FP64 result block, BatchRegistration's
-level table and argument checks, and MultiscaleRegistration's level loop."""
+level table and argument checks, MultiscaleRegistration's level loop, and
+ICPOdometry's defaults and refusals."""
 import math
 
 import numpy as np
@@ -140,3 +141,24 @@ def test_multiscale_level_loop_hands_transforms_coarse_to_fine():
     assert calls[0][4] == "T0" and calls[1][4] is T1 and calls[2][4] is None
     assert all(c[3] is None for c in calls)
     assert res.transform == "T_fine"
+
+
+def test_icp_odometry_constructor_checks():
+    """ICPOdometry keeps the reference's keyword defaults (icp.py:137-139)
+    and refuses what it cannot run: so3=True (the reference's rotation-only
+    path fails with a TypeError, icp.py:71-76), more iterations than the
+    key map's epoch tags, and unknown channel modes or layouts."""
+    from slamtb_gb300.registration import ICPOdometry
+    icp = ICPOdometry(10)
+    assert (icp.geom_weight, icp.feat_weight, icp.so3) == (1.0, 1.0, False)
+    assert icp.distance_threshold == 0.5
+    assert icp.normals_angle_thresh == pytest.approx(math.pi / 4)
+    assert icp.feat_residual_thresh == 2.75
+    with pytest.raises(NotImplementedError, match="so3"):
+        ICPOdometry(10, so3=True)
+    with pytest.raises(ValueError, match="254"):
+        ICPOdometry(255)
+    with pytest.raises(ValueError, match="feat_channel_mode"):
+        ICPOdometry(10, feat_channel_mode="max")
+    with pytest.raises(ValueError, match="feat_layout"):
+        ICPOdometry(10, feat_layout="hwc")
