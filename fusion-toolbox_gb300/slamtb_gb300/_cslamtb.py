@@ -21,6 +21,9 @@ from . import _native as N
 
 
 def _need_cuda(ref, *named):
+    if not ref.is_cuda:
+        raise RuntimeError("Check failed: source points: Expected a gpu tensor "
+                           "(slamtb_gb300 runs on CUDA devices only)")
     dev = ref.device
     for name, t in named:
         if t is None:
@@ -28,9 +31,6 @@ def _need_cuda(ref, *named):
         if not t.is_cuda or t.device != dev:
             raise RuntimeError(f"Check failed: {name}: Expected a gpu tensor on {dev}, "
                                f"got {t.device}")
-    if not ref.is_cuda:
-        raise RuntimeError("Check failed: source points: Expected a gpu tensor "
-                           "(slamtb_gb300 runs on CUDA devices only)")
     return dev
 
 

@@ -83,6 +83,25 @@ def test_host_tensors_are_refused():
     with pytest.raises(RuntimeError, match="Expected a gpu tensor"):
         ICPOdometry(3).estimate(kcam, pts.view(-1, 3), nrm.view(-1, 3), mask.view(-1),
                                 target_points=pts, target_normals=nrm, target_mask=mask)
+    # the _cslamtb shim names the source points first, as the reference's
+    # device checks start from them (correspondence_map.cu:71-79)
+    from slamtb_gb300 import processing
+    from slamtb_gb300._cslamtb import CorrespondenceMap, ICPJacobian
+    k = kcam.matrix
+    merge = torch.full((12, 16), 0x0FFFFFFF7F800000, dtype=torch.int64)
+    with pytest.raises(RuntimeError, match="^Check failed: source points: Expected a gpu"):
+        CorrespondenceMap.compute_correspondence_map(
+            pts.view(-1, 3), nrm.view(-1, 3), mask.view(-1), torch.eye(4), pts, nrm, mask, k,
+            merge, 0.1, 0.5)
+    with pytest.raises(RuntimeError, match="^Check failed: source points: Expected a gpu"):
+        ICPJacobian.estimate_geometric(pts.view(-1, 3), mask.view(-1), torch.eye(4), pts, nrm,
+                                       k, merge, torch.zeros(192, 6, 6), torch.zeros(192, 6),
+                                       torch.zeros(192))
+    for fn, args in ((processing.estimate_normals, (pts, mask)),
+                     (processing.erode_mask, (mask,)),
+                     (processing.bilateral_depth_filter, (pts[..., 2].contiguous(), mask))):
+        with pytest.raises(RuntimeError, match="Expected a gpu tensor"):
+            fn(*args)
 
 
 def _python_name(name):
