@@ -162,3 +162,18 @@ def test_icp_odometry_constructor_checks():
         ICPOdometry(10, feat_channel_mode="max")
     with pytest.raises(ValueError, match="feat_layout"):
         ICPOdometry(10, feat_layout="hwc")
+
+
+def test_point_to_plane_loss_argument_checks():
+    """PointToPlaneLoss refuses host tensors before any device work (it
+    checks every per-pixel input's dtype, device and (B, H, W[, 3]) shape)."""
+    from slamtb_gb300.registration import point_to_plane_loss
+    B, H, W = 2, 6, 8
+    depth = torch.rand(B, H, W)
+    pts = torch.rand(B, H, W, 3)
+    mask = torch.ones(B, H, W, dtype=torch.bool)
+    poses = torch.eye(4, dtype=torch.float64).expand(B, 4, 4)
+    twist = torch.zeros(B, 6, dtype=torch.float64)
+    args = [twist, depth, pts, mask, pts, pts, mask, (50.0, 50.0, 4.0, 3.0), poses, 0.1, 0.5]
+    with pytest.raises(RuntimeError, match="source_depth must be a float32 CUDA tensor"):
+        point_to_plane_loss(*args)
