@@ -119,7 +119,8 @@ __host__ __device__ constexpr int upper_index(int a, int b) {
 }  // namespace stb
 
 // ---------------------------------------------------------------------------
-// Gauss-Newton step by one warp, in double-word arithmetic on the FP32 pipes.
+// Gauss-Newton step by one warp, in double-word arithmetic on the FP32 pipes
+// (opt-in, STB_OPT_DW_SOLVE; the default is the FP64 step further below).
 //
 // On this part every FP64 warp instruction occupies the FP64 pipe of its SM
 // sub-partition for ~64 cycles whatever its lanes or dependences, so a
@@ -232,7 +233,8 @@ __device__ __forceinline__ float2 dw_of_double(double x) {
   return make_float2(h, __double2float_rn(x - (double)h));
 }
 
-// One Gauss-Newton update by one warp (all 32 lanes call it).
+// One Gauss-Newton update by one warp (all 32 lanes call it), in
+// double-words: the opt-in variant of warp_gn_update below.
 //   up: the 21 packed upper-triangle entries of J^T J and bv: J^T r (6),
 //       normalised double-words (hi, lo) in shared memory;
 //   T: the current pose as double-words (16, row-major, shared).
@@ -245,8 +247,8 @@ __device__ __forceinline__ float2 dw_of_double(double x) {
 // that of the FP64 pose.  Returns the solve status (warp-uniform); on success lanes
 // 0..15 hold Tn's entries in tn_out (lane k -> entry k), and every lane
 // holds x rounded to float32 in xs (for the finiteness test).
-__device__ inline bool warp_gn_update(const float2 *up, const float2 *bv, const float2 *T,
-                                      float *xs, float2 &tn_out, int lane) {
+__device__ inline bool warp_gn_update_dw(const float2 *up, const float2 *bv, const float2 *T,
+                                         float *xs, float2 &tn_out, int lane) {
   // this lane's entry (i, k); k == 6 marks the right-hand side
   int ei = 0, ek = 0;
   if (lane < 21) {
@@ -367,6 +369,160 @@ __device__ inline bool warp_gn_update(const float2 *up, const float2 *bv, const 
   if (col == 3) tn = dw_add(tn, tr);
   if (lane >= 12) tn = {(lane == 15) ? 1.f : 0.f, 0.f};
   tn_out = make_float2(tn.hi, tn.lo);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Newton step by one warp in FP64: the default, as the reference's
+// solve (torch.cholesky + cholesky_solve in float64, icp.py:236-251) and its
+// SE(3) update (icp.py:244-247).
+//
+// Every FP64 warp instruction occupies its sub-partition's FP64 pipe for
+// many cycles whatever its lanes, so the layout makes each instruction do
+// the work of many lanes: one lane per entry of the 6x6 lower triangle plus
+// one per right-hand-side entry, an LDL^T factorisation (no square roots)
+// whose column step is one multiply and one FMA for all entries, and the
+// three exponential coefficients at once on three lane groups.
+// ---------------------------------------------------------------------------
+
+// 1 / d for d > 0: rcp.approx.ftz.f64 (relative error below 2^-22) and two
+// Newton-Raphson steps y <- y + y (1 - d y), each of which squares the
+// relative error (2^-44, then below the FP64 rounding): within an ulp or
+// two of the correctly rounded reciprocal.  A subnormal d flushes to an
+// infinite reciprocal, which turns the solution into NaN (flagged by the
+// caller).
+__device__ __forceinline__ double rcp_fp64(double d) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+  y = fma(y, fma(-d, y, 1.0), y);
+  return fma(y, fma(-d, y, 1.0), y);
+}
+
+// d > 0 on the integer bits (false for +-0, negatives and NaN; +inf passes,
+// as the comparison does).
+__device__ __forceinline__ bool positive_bits64(double d) {
+  const long long b = __double_as_longlong(d);
+  return b > 0 && b <= 0x7ff0000000000000ll;
+}
+
+// Maclaurin coefficient n (in t^2) of A = sin t / t (which = 0),
+// B = (1 - cos t) / t^2 (1) or C = (t - sin t) / t^3 (2): (-1)^n / (2n + 1 +
+// which)!, n < 8.  n is a compile-time constant, which a per-lane select.
+template <int n>
+__device__ __forceinline__ double se3_series_coeff(int which) {
+  constexpr double f[18] = {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0,
+                            3628800.0, 39916800.0, 479001600.0, 6227020800.0, 87178291200.0,
+                            1307674368000.0, 20922789888000.0, 355687428096000.0};
+  constexpr double s = (n & 1) ? -1.0 : 1.0;
+  constexpr double ca = s / f[2 * n + 1], cb = s / f[2 * n + 2], cc = s / f[2 * n + 3];
+  return which == 0 ? ca : (which == 1 ? cb : cc);
+}
+
+// One Gauss-Newton update by one warp (all 32 lanes call it), in FP64.
+//   up: the 21 packed upper-triangle entries of J^T J, bv: J^T r (6),
+//   T: the current pose (16, row-major); all in shared memory.
+// Solves J^T J x = J^T r by LDL^T with the failure rule of LAPACK potrf (a
+// pivot that is not > 0, or NaN, fails: the LDL^T pivots are the squares of
+// the Cholesky pivots), then Tn = exp(x) T.  Returns the solve status
+// (warp-uniform); on success lanes 0..15 hold Tn's entries in tn_out (lane
+// k -> entry k), and every lane holds x in xs.
+__device__ inline bool warp_gn_update(const double *up, const double *bv, const double *T,
+                                      double *xs, double &tn_out, int lane) {
+  const unsigned full = 0xffffffffu;
+  // this lane's entry (i, k); k == 6 marks the right-hand side
+  int ei = 0, ek = 0;
+  if (lane < 21) {
+    int k = 0, first = 0;
+    while (lane >= first + (6 - k)) {
+      first += 6 - k;
+      ++k;
+    }
+    ek = k;
+    ei = k + (lane - first);
+  } else if (lane < 27) {
+    ei = lane - 21;
+    ek = 6;
+  }
+  const bool is_rhs = (lane >= 21 && lane < 27);
+  const bool is_tri = lane < 21;
+  double v = 0.0;
+  if (is_tri) v = up[upper_index(ek, ei)];
+  if (is_rhs) v = bv[ei];
+  bool ok = true;
+  // forward: LDL^T factorisation with L z = b and y = D^-1 z fused in
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const double piv = __shfl_sync(full, v, tri_lane(j, j));
+    ok = ok && positive_bits64(piv);
+    const double inv = rcp_fp64(piv);
+    const int src_i = (ei >= j) ? tri_lane(ei, j) : 0;
+    const int src_k = is_rhs ? 21 + j : ((ek >= j && ek < 6) ? tri_lane(ek, j) : 0);
+    const double aij = __shfl_sync(full, v, src_i);
+    const double akj = __shfl_sync(full, v, src_k);
+    const bool own_y = is_rhs && ei == j;
+    const double t = (own_y ? v : aij) * inv;  // L_ij, or y_j on the rhs lane j
+    const bool upd = (is_tri && ek > j && ei >= ek) || (is_rhs && ei > j);
+    const double nv = fma(-t, akj, v);
+    if (upd) v = nv;
+    if ((is_tri && ek == j && ei > j) || own_y) v = t;
+  }
+  if (!ok) return false;
+  // backward: L^T x = y; rhs lane i ends with x_i
+#pragma unroll
+  for (int j = 5; j >= 0; --j) {
+    const double xj = __shfl_sync(full, v, 21 + j);
+    xs[j] = xj;
+    if (j > 0) {
+      const int src = (is_rhs && ei < j) ? tri_lane(j, ei) : 0;
+      const double lji = __shfl_sync(full, v, src);
+      const double nv = fma(-lji, xj, v);
+      if (is_rhs && ei < j) v = nv;
+    }
+  }
+  // exp(x).  Below t = 0.5 the coefficients are their Maclaurin series in
+  // t^2 through t^14 (the first omitted term is below 0.5^16 / 17! < 5e-20
+  // of the sum), A on lanes 0..9, B on 10..19, C on 20..31, by Estrin's
+  // scheme; above, the closed forms of se3_coeffs.
+  const double wx = xs[3], wy = xs[4], wz = xs[5];
+  const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
+  double A, B, C;
+  if (t2 < 0.25) {
+    const int which = lane < 10 ? 0 : (lane < 20 ? 1 : 2);
+    const double u2 = t2 * t2, u4 = u2 * u2;
+    const double a01 = fma(se3_series_coeff<1>(which), t2, se3_series_coeff<0>(which));
+    const double a23 = fma(se3_series_coeff<3>(which), t2, se3_series_coeff<2>(which));
+    const double a45 = fma(se3_series_coeff<5>(which), t2, se3_series_coeff<4>(which));
+    const double a67 = fma(se3_series_coeff<7>(which), t2, se3_series_coeff<6>(which));
+    const double coef = fma(u4, fma(u2, a67, a45), fma(u2, a23, a01));
+    A = __shfl_sync(full, coef, 0);
+    B = __shfl_sync(full, coef, 10);
+    C = __shfl_sync(full, coef, 20);
+  } else {
+    se3_coeffs(t2, A, B, C);
+  }
+  // lanes 0..8 hold R_ac = I + A W + B W^2, lanes 9..17 V_ac = I + B W + C W^2
+  const int e = lane < 9 ? lane : (lane < 18 ? lane - 9 : 0);
+  const int ea = e / 3, ec = e % 3;
+  const double wa = ea == 0 ? wx : (ea == 1 ? wy : wz);
+  const double wc = ec == 0 ? wx : (ec == 1 ? wy : wz);
+  // W = hat(w): W_01 = -wz, W_02 = wy, W_10 = wz, W_12 = -wx, W_20 = -wy, W_21 = wx
+  const double Wac = e == 1 ? -wz : e == 2 ? wy : e == 3 ? wz : e == 5 ? -wx : e == 6 ? -wy
+                   : e == 7 ? wx : 0.0;
+  const bool diag = (ea == ec);
+  const double W2ac = fma(wa, wc, diag ? -t2 : 0.0);  // W^2 = w w^T - |w|^2 I
+  const bool isR = lane < 9;
+  const double val = fma(isR ? A : B, Wac, fma(isR ? B : C, W2ac, diag ? 1.0 : 0.0));
+  // t_a = sum_c V_ac x_c (V row a on lanes 9 + 3a ...)
+  const double v0 = __shfl_sync(full, val, 9 + 3 * ea), v1 = __shfl_sync(full, val, 10 + 3 * ea),
+               v2 = __shfl_sync(full, val, 11 + 3 * ea);
+  const double ta = fma(v0, xs[0], fma(v1, xs[1], v2 * xs[2]));
+  // Tn = [R t] T: lane q = 4 row + col < 12
+  const int row = lane < 12 ? (lane >> 2) : 0, col = lane & 3;
+  const double r0 = __shfl_sync(full, val, 3 * row), r1 = __shfl_sync(full, val, 3 * row + 1),
+               r2 = __shfl_sync(full, val, 3 * row + 2), tr = __shfl_sync(full, ta, 3 * row);
+  double tn = fma(r0, T[col], fma(r1, T[4 + col], fma(r2, T[8 + col], col == 3 ? tr : 0.0)));
+  if (lane >= 12) tn = (lane == 15) ? 1.0 : 0.0;
+  tn_out = tn;
   return true;
 }
 

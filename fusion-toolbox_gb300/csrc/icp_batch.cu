@@ -26,6 +26,7 @@
 
 #include "feature_term.cuh"
 #include "gn_solve.cuh"
+#include "keymap.cuh"
 #include "stb_common.cuh"
 #include "stb_host.hpp"
 
@@ -70,6 +71,7 @@ struct BatchArgs {
   LevelP lp[kMaxLevels];
   const double *init;
   double *results, *history;
+  int solve_dw;    // 1: double-word solve (STB_OPT_DW_SOLVE), 0: FP64
   unsigned *sync;  // [0] arrivals, [1] generation, [2] error
   PairState *ps;
   long long *key_off;   // [B + 1]
@@ -749,13 +751,22 @@ __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const dou
   const double cg = tot[kCountGeomB], cf = tot[kCountFeatB];
   const double count = q.use_geom ? fmax(cg, cf) : cf;
   double *H = a.history ? a.history + ((size_t)p * a.total_iters + s) * STB_HIST_SIZE : nullptr;
-  float xs[6];
-  __shared__ float2 s_tw[16];
-  if (lane < 16) s_tw[lane] = dw_of_double(T[lane]);
-  __syncwarp();
-  float2 tnw;
-  const bool ok = warp_gn_update(totw, totw + kJrB, s_tw, xs, tnw, lane);
-  const double tn = (double)tnw.x + (double)tnw.y;
+  // the solve: FP64 (default) or double-words (STB_OPT_DW_SOLVE)
+  double xs[6];
+  double tn;
+  bool ok;
+  if (a.solve_dw) {
+    __shared__ float2 s_tw[16];
+    if (lane < 16) s_tw[lane] = dw_of_double(T[lane]);
+    __syncwarp();
+    float2 tnw;
+    float xf[6];
+    ok = warp_gn_update_dw(totw, totw + kJrB, s_tw, xf, tnw, lane);
+    tn = (double)tnw.x + (double)tnw.y;
+    for (int k = 0; k < 6; ++k) xs[k] = xf[k];
+  } else {
+    ok = warp_gn_update(tot, tot + kJrB, T, xs, tn, lane);
+  }
   double *R = a.results + (size_t)p * STB_RES_SIZE;
   for (int k = lane; k < 36; k += 32) {
     const int r = k / 6, c = k % 6;
@@ -1184,7 +1195,10 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
     if (feat_dtype < STB_F32 || feat_dtype > STB_BF16_HWC)
       return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
   }
-  if (channel_mode != 0 && channel_mode != 1)
+  if ((channel_mode & ~(0xff | STB_OPT_DW_SOLVE)) != 0)
+    return fail(STB_EINVAL, "Check failed: unknown option bits 0x%x in channel_mode",
+                (unsigned)channel_mode & ~(0xffu | STB_OPT_DW_SOLVE));
+  if ((channel_mode & 0xff) != 0 && (channel_mode & 0xff) != 1)
     return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
   const Layout lay = layout(num_pairs, total_target_pixels);
   if (workspace_bytes < lay.total)
@@ -1207,7 +1221,8 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   a.L = num_levels;
   a.C = any_feat ? channels : 0;
   a.dtype = feat_dtype;
-  a.mode = channel_mode;
+  a.mode = channel_mode & 0xff;
+  a.solve_dw = (channel_mode & STB_OPT_DW_SOLVE) != 0;
   a.total_iters = total_iters;
   // largest pixels per work item: 0 -> default (8192), 1..5 -> 512 ... 8192;
   // each level uses the largest power of two below it that still gives
@@ -1262,4 +1277,38 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
     case STB_F32_HWC: return launch_batch<float, true, true>(a, st);
     default: return launch_batch<__nv_bfloat16, true, true>(a, st);
   }
+}
+
+extern "C" int stb_icp_batch_correspondences(const void *workspace, int32_t num_pairs,
+                                             int64_t total_target_pixels, int32_t pair,
+                                             int32_t height, int32_t width,
+                                             int32_t total_iters, int64_t *merge_map,
+                                             void *stream) {
+  clear_error();
+  if (num_pairs <= 0) return fail(STB_EINVAL, "Check failed: num_pairs must be positive");
+  if (pair < 0 || pair >= num_pairs)
+    return fail(STB_EINVAL, "Check failed: pair must be in [0, %d), got %d", num_pairs, pair);
+  if (height <= 0 || width <= 0)
+    return fail(STB_EINVAL, "Check failed: target size must be positive, got %dx%d",
+                height, width);
+  if ((int64_t)height * width > total_target_pixels)
+    return fail(STB_EINVAL, "Check failed: %dx%d is more than the batch's %lld target pixels",
+                height, width, (long long)total_target_pixels);
+  if (total_iters < 0 || total_iters > 253)
+    return fail(STB_EINVAL, "Check failed: total_iters must be in [0, 253], got %d",
+                total_iters);
+  if (((uintptr_t)workspace & 255) != 0)
+    return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
+  STB_TRY(check_device_ptr(workspace, "workspace"));
+  STB_TRY(check_device_ptr(merge_map, "merge_map"));
+  const Layout lay = layout(num_pairs, total_target_pixels);
+  const char *ws = static_cast<const char *>(workspace);
+  const auto *keys = reinterpret_cast<const unsigned long long *>(ws + lay.keys);
+  const auto *key_off = reinterpret_cast<const long long *>(ws + lay.key_off);
+  const long long npix = (long long)height * width;
+  // the information pass associates at step total_iters (tag btag of it)
+  k_keys_to_merge_map<<<keys_grid(npix), 256, 0, as_stream(stream)>>>(
+      keys, key_off + pair, npix, 254u - (unsigned)total_iters,
+      reinterpret_cast<long long *>(merge_map));
+  return check_launch("stb_icp_batch_correspondences");
 }

@@ -31,6 +31,7 @@
 
 #include "feature_term.cuh"
 #include "gn_solve.cuh"
+#include "keymap.cuh"
 #include "stb_common.cuh"
 #include "stb_host.hpp"
 
@@ -52,10 +53,15 @@ constexpr unsigned long long kMaxSources = 1ull << 24;
 // Accumulator slots.
 constexpr int kJr = 21, kR2 = 27, kCountGeom = 28, kCountFeat = 29;
 
+// The loop state.  The pose and the totals of the last successful step are
+// FP64 (Td, last_totd) under the default FP64 solve, double-words (Tw,
+// last_tot) under the opt-in double-word solve (Job::solve_dw).
 struct State {
-  float2 Tw[16];  // current pose as double-words (within ~1e-14 of FP64)
-  Pose32 pose;    // its float32 view (the high words) + intrinsics
-  float2 last_tot[32];  // totals (double-words) of the last successful step
+  double Td[16];
+  double last_totd[32];
+  float2 Tw[16];  // pose as double-words (within ~1e-14 of FP64)
+  Pose32 pose;    // float32 view of the pose + intrinsics
+  float2 last_tot[32];
   unsigned ticket;
   unsigned stopped;
   unsigned status;
@@ -76,6 +82,7 @@ struct Job {
   const double *init;
   int iters, channel_mode;
   int use_geom, use_feat;
+  int solve_dw;  // 1: double-word solve (STB_OPT_DW_SOLVE), 0: FP64
   float wg1, wg2, wf1, wf2;
   float thr2, cos_max, feat_thr2;
   double *result, *history;
@@ -109,11 +116,11 @@ inline void set_small_inputs(Job &job, const float *kcam, bool kcam_host, const 
 
 constexpr size_t kSlot = 1024;
 
-__host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+__host__ __device__ constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Blocks of the reduction for `threads` threads of kPixelsPerThread pixels;
 // the workspace holds slots for the 256-thread count (the largest grid).
-inline int reduce_blocks(int64_t pixels, int threads = kReduceThreads) {
+constexpr int reduce_blocks(int64_t pixels, int threads = kReduceThreads) {
   const int64_t per_block = (int64_t)threads * kPixelsPerThread;
   int64_t b = (pixels + per_block - 1) / per_block;
   if (b < 1) b = 1;
@@ -125,13 +132,15 @@ constexpr int kSlotAccs = 32;  // accumulator pairs per block slot (>= kAccs)
 
 // Workspace: [Job slot][State slot][block slots: nblocks x kSlotAccs float2]
 // [keys H*W]
-inline size_t workspace_bytes(int64_t pixels) {
-  const int nb = reduce_blocks(pixels);
-  return 2 * kSlot + align256(sizeof(float2) * kSlotAccs * nb) +
-         align256(sizeof(unsigned long long) * pixels);
+constexpr size_t keys_offset(int64_t pixels) {
+  return 2 * kSlot + align256(sizeof(float2) * kSlotAccs * reduce_blocks(pixels));
+}
+constexpr size_t workspace_bytes(int64_t pixels) {
+  return keys_offset(pixels) + align256(sizeof(unsigned long long) * pixels);
 }
 
 __device__ __forceinline__ unsigned tag_of(int epoch) { return 254u - (unsigned)epoch; }
+inline unsigned tag_of_host(int epoch) { return 254u - (unsigned)epoch; }
 
 __device__ __forceinline__ void load_shared_pose(Pose32 &P, const State *S) {
   const float *src = reinterpret_cast<const float *>(&S->pose);
@@ -154,7 +163,10 @@ __global__ void k_begin(Job job, Job *dst) {
   S->pose.fy = job.kcam ? job.kcam[4] : job.kcam_v[2];
   S->pose.cy = job.kcam ? job.kcam[5] : job.kcam_v[3];
   refresh_pose32(S->pose, T);
-  for (int k = 0; k < 16; ++k) S->Tw[k] = dw_of_double(T[k]);
+  for (int k = 0; k < 16; ++k) {
+    S->Td[k] = T[k];
+    S->Tw[k] = dw_of_double(T[k]);
+  }
   S->ticket = 0;
   S->stopped = 0;
   S->status = 0;
@@ -340,27 +352,110 @@ __device__ __forceinline__ void grid_totals(const float2 *part, int nblocks, dou
 // then finds it in shared memory instead of paying an L2 round trip in the
 // serial tail).
 struct StateView {
+  double Td[16];
   float2 Tw[16];
   unsigned status;
   int iters_done;
 };
 
-__device__ __forceinline__ void load_state_view(StateView &V, const State *S) {
-  if (threadIdx.x < 16) V.Tw[threadIdx.x] = S->Tw[threadIdx.x];
+__device__ __forceinline__ void load_state_view(StateView &V, const State *S, bool dw) {
+  if (threadIdx.x < 16) {
+    if (dw)
+      V.Tw[threadIdx.x] = S->Tw[threadIdx.x];
+    else
+      V.Td[threadIdx.x] = S->Td[threadIdx.x];
+  }
   if (threadIdx.x == 16) V.status = S->status;
   if (threadIdx.x == 17) V.iters_done = S->iters_done;
 }
 
-// One Gauss-Newton step from the totals in shared memory, by warp 0 of the
-// last block: the solve on the double-words (warp_gn_update of
-// gn_solve.cuh), then what the next kernel reads (the pose as double-words
-// and as a float32 view with its normal matrix, the status, the stop flag,
-// the iteration count) and the totals of a successful step for the result.
-// No FP64 instruction is on this path: the FP64 result block is written
-// once per registration by the information pass.  When a history is
-// recorded, warp 1 writes this iteration's FP64 record meanwhile and, after
-// the solve status is known (named barrier 1), its pose.
-__device__ void gn_step(const Job *J, const StateView &V, const float2 *totw, int iter) {
+// Status bits of a step (lane 0): what warp_gn_update's verdict, the
+// update's finiteness and the match counts say, and the stop flag.
+__device__ __forceinline__ unsigned step_status(unsigned st, bool ok, bool finite,
+                                                bool no_match, State *S) {
+  if (!ok) {
+    st |= STB_ST_NOT_PD;
+    S->stopped = 1;
+  } else if (!finite) {
+    st |= STB_ST_NAN;
+  }
+  if (no_match) st |= STB_ST_NO_MATCHES;
+  return st;
+}
+
+// One Gauss-Newton step from the FP64 totals in shared memory, by warp 0 of
+// the last block: the FP64 solve and exponential (warp_gn_update of
+// gn_solve.cuh), then what the next kernel reads (the FP64 pose and its
+// float32 view with the normal matrix, the status, the stop flag, the
+// iteration count) and the totals of a successful step for the result.
+// When a history is recorded, warp 1 writes this iteration's record
+// meanwhile and, after the solve status is known (named barrier 1), its
+// pose.
+__device__ void gn_step(const Job *J, const StateView &V, const double *tot, int iter) {
+  __shared__ float rt32[12];
+  __shared__ double s_tn[16];
+  __shared__ int s_ok;
+  const int lane = threadIdx.x & 31;
+  State *S = J->state;
+  double *H = J->history ? J->history + (size_t)iter * STB_HIST_SIZE : nullptr;
+  if (threadIdx.x < 32) {
+    double xs[6];
+    double tn;
+    const bool ok = warp_gn_update(tot, tot + kJr, V.Td, xs, tn, lane);
+    const double cg = tot[kCountGeom], cf = tot[kCountFeat];
+    const bool no_match = (J->use_geom ? fmax(cg, cf) : cf) == 0.0;
+    if (ok) {
+      if (lane < 16) {
+        s_tn[lane] = tn;
+        S->Td[lane] = tn;
+      }
+      if (lane < 12) {
+        const float f = __double2float_rn(tn);  // transform.to(float32)
+        rt32[lane] = f;
+        S->pose.rt[lane] = f;
+      }
+      if (lane < kAccs) S->last_totd[lane] = tot[lane];
+      __syncwarp();
+    }
+    if (lane == 0) {
+      bool finite = true;
+      for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
+      if (ok) {
+        float nm[9];
+        inverse_transpose(rt32, nm);
+        for (int k = 0; k < 9; ++k) S->pose.nm[k] = nm[k];
+        S->iters_done = V.iters_done + 1;
+      }
+      S->status = step_status(V.status, ok, finite, no_match, S);
+      s_ok = ok;
+    }
+    if (H) asm volatile("bar.sync 1, 64;" ::: "memory");
+    return;
+  }
+  if (!H) return;
+  // warp 1: the history record
+  for (int k = lane; k < 36; k += 32) {
+    const int r = k / 6, c = k % 6;
+    H[STB_HIST_JTJ + k] = tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
+  }
+  if (lane < 6) H[STB_HIST_JR + lane] = tot[kJr + lane];
+  if (lane == 0) {
+    H[STB_HIST_R2] = tot[kR2];
+    H[STB_HIST_GEOM_COUNT] = tot[kCountGeom];
+    H[STB_HIST_FEAT_COUNT] = tot[kCountFeat];
+  }
+  asm volatile("bar.sync 1, 64;" ::: "memory");
+  const bool ok = s_ok;
+  if (lane == 0) H[STB_HIST_OK] = ok ? 1.0 : 0.0;
+  if (ok && lane < 16) H[STB_HIST_TRANSFORM + lane] = s_tn[lane];
+}
+
+// The same step in double-words (the opt-in STB_OPT_DW_SOLVE): the solve
+// on the double-words (warp_gn_update_dw of gn_solve.cuh), the pose kept as
+// double-words.  No FP64 instruction is on this path: the FP64 result block
+// is written once per registration by the information pass, the history
+// record by warp 1.
+__device__ void gn_step_dw(const Job *J, const StateView &V, const float2 *totw, int iter) {
   __shared__ float rt32[12];
   __shared__ float2 s_tn[16];
   __shared__ int s_ok;
@@ -371,7 +466,7 @@ __device__ void gn_step(const Job *J, const StateView &V, const float2 *totw, in
   if (threadIdx.x < 32) {
     float xs[6];
     float2 tn;
-    const bool ok = warp_gn_update(totw, totw + kJr, V.Tw, xs, tn, lane);
+    const bool ok = warp_gn_update_dw(totw, totw + kJr, V.Tw, xs, tn, lane);
     // count == 0 on the high words (counts are non-negative)
     const float cg = totw[kCountGeom].x, cf = totw[kCountFeat].x;
     const bool no_match = (J->use_geom ? fmaxf(cg, cf) : cf) == 0.f;
@@ -388,21 +483,15 @@ __device__ void gn_step(const Job *J, const StateView &V, const float2 *totw, in
       __syncwarp();
     }
     if (lane == 0) {
-      unsigned st = V.status;
-      if (!ok) {
-        st |= STB_ST_NOT_PD;
-        S->stopped = 1;
-      } else {
-        bool finite = true;
-        for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
-        if (!finite) st |= STB_ST_NAN;
+      bool finite = true;
+      for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
+      if (ok) {
         float nm[9];
         inverse_transpose(rt32, nm);
         for (int k = 0; k < 9; ++k) S->pose.nm[k] = nm[k];
         S->iters_done = V.iters_done + 1;
       }
-      if (no_match) st |= STB_ST_NO_MATCHES;
-      S->status = st;
+      S->status = step_status(V.status, ok, finite, no_match, S);
       s_ok = ok;
     }
     if (H) asm volatile("bar.sync 1, 64;" ::: "memory");
@@ -446,12 +535,14 @@ __global__ void __launch_bounds__(kT) k_reduce(const Job *__restrict__ J, int ep
   __shared__ float2 bsum[kAccs];
   __shared__ int is_last;
   __shared__ float2 totw[kAccs];
+  __shared__ double tot[kAccs];
   State *S = J->state;
   grid_dependency_wait();  // the association has written the key map
   grid_launch_dependents();
+  const bool solve_dw = J->solve_dw;
   if (threadIdx.x == 0) skip = S->stopped;
   load_shared_pose(P, S);
-  load_state_view(V, S);
+  load_state_view(V, S, solve_dw);
   __syncthreads();
   if (skip) return;
 
@@ -527,10 +618,18 @@ __global__ void __launch_bounds__(kT) k_reduce(const Job *__restrict__ J, int ep
 
   block_reduce<kAccs, kT>(acc, red, bsum);
   if (!publish_slot<kAccs>(bsum, J->part, &S->ticket, &is_last)) return;
-  grid_totals<kAccs, kT>(J->part, gridDim.x, nullptr, totw);
-  if (threadIdx.x < 64) {
-    if (threadIdx.x == 0) S->ticket = 0;
-    gn_step(J, V, totw, epoch);
+  if (solve_dw) {
+    grid_totals<kAccs, kT>(J->part, gridDim.x, nullptr, totw);
+    if (threadIdx.x < 64) {
+      if (threadIdx.x == 0) S->ticket = 0;
+      gn_step_dw(J, V, totw, epoch);
+    }
+  } else {
+    grid_totals<kAccs, kT>(J->part, gridDim.x, tot, nullptr);
+    if (threadIdx.x < 64) {
+      if (threadIdx.x == 0) S->ticket = 0;
+      gn_step(J, V, tot, epoch);
+    }
   }
 }
 
@@ -576,26 +675,31 @@ __global__ void __launch_bounds__(kReduceThreads) k_info(const Job *__restrict__
   // the result of the last successful step (its pose, J^T J, match count,
   // residual r2 / count, icp.py:249-253), once per registration
   const int done = S->iters_done;
+  const bool dw = J->solve_dw;
+  // a total of the last successful step, from the solve's representation
+  auto last = [&](int a) -> double {
+    if (!dw) return S->last_totd[a];
+    const float2 v = S->last_tot[a];
+    return (double)v.x + (double)v.y;
+  };
   if (done > 0) {
     for (int k = threadIdx.x; k < 36; k += blockDim.x) {
       const int r = k / 6, c = k % 6;
-      const float2 a = S->last_tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
-      R[STB_RES_JTJ + k] = (double)a.x + (double)a.y;
+      R[STB_RES_JTJ + k] = last(r <= c ? upper_index(r, c) : upper_index(c, r));
     }
     if (threadIdx.x < 16)
       R[STB_RES_TRANSFORM + threadIdx.x] =
-          (double)S->Tw[threadIdx.x].x + (double)S->Tw[threadIdx.x].y;
+          dw ? (double)S->Tw[threadIdx.x].x + (double)S->Tw[threadIdx.x].y
+             : S->Td[threadIdx.x];
   }
   if (threadIdx.x == 0) {
     S->ticket = 0;
     if (done > 0) {
-      const float2 g = S->last_tot[kCountGeom], f = S->last_tot[kCountFeat],
-                   r2 = S->last_tot[kR2];
-      const double cg = (double)g.x + (double)g.y, cf = (double)f.x + (double)f.y;
+      const double cg = last(kCountGeom), cf = last(kCountFeat);
       const double count = J->use_geom ? fmax(cg, cf) : cf;
       R[STB_RES_MATCHES] = count;
       R[STB_RES_ITERS] = (double)done;
-      R[STB_RES_RESIDUAL] = ((double)r2.x + (double)r2.y) / count;
+      R[STB_RES_RESIDUAL] = last(kR2) / count;
     }
     R[STB_RES_STATUS] = (double)S->status;
   }
@@ -653,7 +757,7 @@ struct Timed {
 // ---------------------------------------------------------------------------
 struct Plan {
   int64_t n;
-  int H, W, C, dtype, iters, use_geom, use_feat, channel_mode, nblocks;
+  int H, W, C, dtype, iters, use_geom, use_feat, channel_mode, solve_dw, nblocks;
   Job *job_dev;
   unsigned long long *keys;
 };
@@ -772,7 +876,8 @@ struct GraphEntry {
   ProfSet *prof = nullptr;  // event pairs captured in the graph (profiling)
 };
 
-using GraphKey = std::tuple<void *, int64_t, int, int, int, int, int, int, int, int, bool, bool>;
+using GraphKey =
+    std::tuple<void *, int64_t, int, int, int, int, int, int, int, int, int, bool, bool>;
 std::mutex g_graph_mutex;
 std::map<GraphKey, GraphEntry> g_graphs;
 
@@ -780,7 +885,8 @@ int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st)
   std::lock_guard<std::mutex> lock(g_graph_mutex);
   const bool prof = g_prof_on;
   const GraphKey key{(void *)p.job_dev, p.n, p.H, p.W, p.C, p.dtype, p.iters,
-                     p.use_geom, p.use_feat, p.channel_mode, with_history, prof};
+                     p.use_geom, p.use_feat, p.channel_mode, p.solve_dw, with_history,
+                     prof};
   auto it = g_graphs.find(key);
   Job job_copy = job;
   Job *dst = p.job_dev;
@@ -852,6 +958,152 @@ extern "C" size_t stb_icp_workspace_bytes(int64_t num_source, int32_t height,
   return workspace_bytes((int64_t)height * width);
 }
 
+namespace stb {
+namespace {
+
+// The arguments of a registration call, as the entry points take them.
+struct EstimateArgs {
+  const float *kcam, *src_points, *src_normals;
+  const uint8_t *src_mask;
+  int64_t num_source;
+  const void *src_feats;
+  const float *tgt_points, *tgt_normals;
+  const uint8_t *tgt_mask;
+  int32_t height, width;
+  const void *tgt_feats;
+  int32_t channels, feat_dtype;
+  const double *init_transform;
+  int32_t num_iters;
+  double geom_weight, feat_weight, distance_thresh, normal_angle_thresh,
+      feat_residual_thresh;
+  int32_t channel_mode;  // channel mode (low byte) | STB_OPT_* bits
+  double *result, *history;
+};
+
+// Checks the arguments shared by both registration entry points (sizes,
+// options, device pointers); tells whether kcam and init_transform are host
+// memory.
+int check_args(const EstimateArgs &a, bool *kcam_host, bool *init_host) {
+  if (a.num_source < 0 || (unsigned long long)a.num_source >= kMaxSources)
+    return fail(STB_EINVAL, "Check failed: num_source must be in [0, 2^24), got %lld",
+                (long long)a.num_source);
+  if (a.height <= 0 || a.width <= 0)
+    return fail(STB_EINVAL, "Check failed: target size must be positive, got %dx%d",
+                a.height, a.width);
+  if (a.num_iters < 0 || a.num_iters > 254)
+    return fail(STB_EINVAL, "Check failed: num_iters must be in [0, 254], got %d",
+                a.num_iters);
+  if ((a.channel_mode & ~(0xff | STB_OPT_DW_SOLVE)) != 0)
+    return fail(STB_EINVAL, "Check failed: unknown option bits 0x%x in channel_mode",
+                (unsigned)a.channel_mode & ~(0xffu | STB_OPT_DW_SOLVE));
+  const int cmode = a.channel_mode & 0xff;
+  const bool use_feat = a.feat_weight > 0.0 && a.src_feats && a.tgt_feats;
+  if (use_feat) {
+    if (a.channels <= 0)
+      return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", a.channels);
+    if (a.feat_dtype < STB_F32 || a.feat_dtype > STB_BF16_HWC)
+      return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
+    if (cmode != 0 && cmode != 1)
+      return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
+  }
+  STB_TRY(check_small_input(a.kcam, "kcam", false, kcam_host));
+  STB_TRY(check_device_ptr(a.src_points, "src_points"));
+  STB_TRY(check_device_ptr(a.src_normals, "src_normals"));
+  STB_TRY(check_device_ptr(a.src_mask, "src_mask"));
+  STB_TRY(check_device_ptr(a.tgt_points, "tgt_points"));
+  STB_TRY(check_device_ptr(a.tgt_normals, "tgt_normals"));
+  STB_TRY(check_device_ptr(a.tgt_mask, "tgt_mask"));
+  if (use_feat) {
+    STB_TRY(check_device_ptr(a.src_feats, "src_feats"));
+    STB_TRY(check_device_ptr(a.tgt_feats, "tgt_feats"));
+  }
+  STB_TRY(check_small_input(a.init_transform, "transform", true, init_host));
+  STB_TRY(check_device_ptr(a.result, "result"));
+  STB_TRY(check_device_ptr(a.history, "history", true));
+  return STB_OK;
+}
+
+// The plan and the Job of a checked call on the workspace at ws.
+void make_plan(const EstimateArgs &a, bool kcam_host, bool init_host, char *ws, Plan &p,
+               Job &job) {
+  const bool use_feat = a.feat_weight > 0.0 && a.src_feats && a.tgt_feats;
+  const bool use_geom = a.geom_weight > 0.0;
+  const int64_t npix = (int64_t)a.height * a.width;
+  p.n = a.num_source;
+  p.H = a.height;
+  p.W = a.width;
+  p.C = use_feat ? a.channels : 0;
+  p.dtype = use_feat ? a.feat_dtype : 0;
+  p.iters = a.num_iters;
+  p.use_geom = use_geom;
+  p.use_feat = use_feat;
+  p.channel_mode = use_feat ? (a.channel_mode & 0xff) : 0;
+  p.solve_dw = (a.channel_mode & STB_OPT_DW_SOLVE) != 0;
+  p.nblocks = reduce_blocks(npix);
+  p.job_dev = reinterpret_cast<Job *>(ws);
+
+  job.sp = a.src_points;
+  job.sn = a.src_normals;
+  job.sm = a.src_mask;
+  job.n = a.num_source;
+  job.sf = a.src_feats;
+  job.tp = a.tgt_points;
+  job.tn = a.tgt_normals;
+  job.tm = a.tgt_mask;
+  job.H = a.height;
+  job.W = a.width;
+  job.tf = a.tgt_feats;
+  job.C = p.C;
+  job.dtype = p.dtype;
+  set_small_inputs(job, a.kcam, kcam_host, a.init_transform, init_host);
+  job.iters = a.num_iters;
+  job.channel_mode = p.channel_mode;
+  job.use_geom = use_geom;
+  job.use_feat = use_feat;
+  job.solve_dw = p.solve_dw;
+  job.wg1 = (float)a.geom_weight;
+  job.wg2 = (float)(a.geom_weight * a.geom_weight);
+  job.wf1 = (float)a.feat_weight;
+  job.wf2 = (float)(a.feat_weight * a.feat_weight);
+  job.thr2 = distance_thresh_sq(a.distance_thresh);
+  job.cos_max = angle_cos_max(a.normal_angle_thresh);
+  {
+    const float t = (float)a.feat_residual_thresh;  // a float in the reference
+    job.feat_thr2 = t * t;
+  }
+  job.result = a.result;
+  job.history = a.history;
+  job.state = reinterpret_cast<State *>(ws + kSlot);
+  job.part = reinterpret_cast<float2 *>(ws + 2 * kSlot);
+  job.keys = reinterpret_cast<unsigned long long *>(ws + keys_offset(npix));
+  job.nblocks = p.nblocks;
+  p.keys = job.keys;
+  static_assert(sizeof(Job) <= kSlot && sizeof(State) <= kSlot, "workspace slots");
+}
+
+}  // namespace
+}  // namespace stb
+
+extern "C" int stb_icp_correspondences(const void *workspace, int32_t height, int32_t width,
+                                       int32_t num_iters, int64_t *merge_map, void *stream) {
+  clear_error();
+  if (height <= 0 || width <= 0)
+    return fail(STB_EINVAL, "Check failed: target size must be positive, got %dx%d",
+                height, width);
+  if (num_iters < 0 || num_iters > 254)
+    return fail(STB_EINVAL, "Check failed: num_iters must be in [0, 254], got %d", num_iters);
+  if (((uintptr_t)workspace & 255) != 0)
+    return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
+  STB_TRY(check_device_ptr(workspace, "workspace"));
+  STB_TRY(check_device_ptr(merge_map, "merge_map"));
+  const int64_t npix = (int64_t)height * width;
+  const auto *keys = reinterpret_cast<const unsigned long long *>(
+      static_cast<const char *>(workspace) + keys_offset(npix));
+  k_keys_to_merge_map<<<keys_grid(npix), 256, 0, as_stream(stream)>>>(
+      keys, nullptr, npix, tag_of_host(num_iters), reinterpret_cast<long long *>(merge_map));
+  return check_launch("stb_icp_correspondences");
+}
+
 extern "C" int stb_icp_estimate(
     const float *kcam, const float *src_points, const float *src_normals,
     const uint8_t *src_mask, int64_t num_source, const void *src_feats,
@@ -863,101 +1115,24 @@ extern "C" int stb_icp_estimate(
     void *workspace, size_t workspace_bytes_, double *result, double *history,
     int32_t use_graph, void *stream) {
   clear_error();
-  if (num_source < 0 || (unsigned long long)num_source >= kMaxSources)
-    return fail(STB_EINVAL, "Check failed: num_source must be in [0, 2^24), got %lld",
-                (long long)num_source);
-  if (height <= 0 || width <= 0)
-    return fail(STB_EINVAL, "Check failed: target size must be positive, got %dx%d",
-                height, width);
-  if (num_iters < 0 || num_iters > 254)
-    return fail(STB_EINVAL, "Check failed: num_iters must be in [0, 254], got %d", num_iters);
+  const EstimateArgs a{kcam, src_points, src_normals, src_mask, num_source, src_feats,
+                       tgt_points, tgt_normals, tgt_mask, height, width, tgt_feats, channels,
+                       feat_dtype, init_transform, num_iters, geom_weight, feat_weight,
+                       distance_thresh, normal_angle_thresh, feat_residual_thresh,
+                       channel_mode, result, history};
+  bool kcam_host, init_host;
+  STB_TRY(check_args(a, &kcam_host, &init_host));
   const int64_t npix = (int64_t)height * width;
   if (workspace_bytes_ < workspace_bytes(npix))
     return fail(STB_EINVAL, "Check failed: workspace of %zu bytes, %zu needed",
                 workspace_bytes_, workspace_bytes(npix));
   if (((uintptr_t)workspace & 255) != 0)
     return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
-  const bool use_feat = feat_weight > 0.0 && src_feats && tgt_feats;
-  const bool use_geom = geom_weight > 0.0;
-  if (use_feat) {
-    if (channels <= 0)
-      return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
-    if (feat_dtype < STB_F32 || feat_dtype > STB_BF16_HWC)
-      return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
-    if (channel_mode != 0 && channel_mode != 1)
-      return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
-  }
-  bool kcam_host, init_host;
-  STB_TRY(check_small_input(kcam, "kcam", false, &kcam_host));
-  STB_TRY(check_device_ptr(src_points, "src_points"));
-  STB_TRY(check_device_ptr(src_normals, "src_normals"));
-  STB_TRY(check_device_ptr(src_mask, "src_mask"));
-  STB_TRY(check_device_ptr(tgt_points, "tgt_points"));
-  STB_TRY(check_device_ptr(tgt_normals, "tgt_normals"));
-  STB_TRY(check_device_ptr(tgt_mask, "tgt_mask"));
-  if (use_feat) {
-    STB_TRY(check_device_ptr(src_feats, "src_feats"));
-    STB_TRY(check_device_ptr(tgt_feats, "tgt_feats"));
-  }
-  STB_TRY(check_small_input(init_transform, "transform", true, &init_host));
   STB_TRY(check_device_ptr(workspace, "workspace"));
-  STB_TRY(check_device_ptr(result, "result"));
-  STB_TRY(check_device_ptr(history, "history", true));
   STB_TRY(prepare_reduce_kernels());
-
-  char *ws = static_cast<char *>(workspace);
   Plan p;
-  p.n = num_source;
-  p.H = height;
-  p.W = width;
-  p.C = use_feat ? channels : 0;
-  p.dtype = use_feat ? feat_dtype : 0;
-  p.iters = num_iters;
-  p.use_geom = use_geom;
-  p.use_feat = use_feat;
-  p.channel_mode = use_feat ? channel_mode : 0;
-  p.nblocks = reduce_blocks(npix);
-  p.job_dev = reinterpret_cast<Job *>(ws);
-
   Job job;
-  job.sp = src_points;
-  job.sn = src_normals;
-  job.sm = src_mask;
-  job.n = num_source;
-  job.sf = src_feats;
-  job.tp = tgt_points;
-  job.tn = tgt_normals;
-  job.tm = tgt_mask;
-  job.H = height;
-  job.W = width;
-  job.tf = tgt_feats;
-  job.C = p.C;
-  job.dtype = p.dtype;
-  set_small_inputs(job, kcam, kcam_host, init_transform, init_host);
-  job.iters = num_iters;
-  job.channel_mode = p.channel_mode;
-  job.use_geom = use_geom;
-  job.use_feat = use_feat;
-  job.wg1 = (float)geom_weight;
-  job.wg2 = (float)(geom_weight * geom_weight);
-  job.wf1 = (float)feat_weight;
-  job.wf2 = (float)(feat_weight * feat_weight);
-  job.thr2 = distance_thresh_sq(distance_thresh);
-  job.cos_max = angle_cos_max(normal_angle_thresh);
-  {
-    const float t = (float)feat_residual_thresh;  // a float in the reference
-    job.feat_thr2 = t * t;
-  }
-  job.result = result;
-  job.history = history;
-  size_t off = 2 * kSlot;
-  job.state = reinterpret_cast<State *>(ws + kSlot);
-  job.part = reinterpret_cast<float2 *>(ws + off);
-  off += align256(sizeof(float2) * kSlotAccs * p.nblocks);
-  job.keys = reinterpret_cast<unsigned long long *>(ws + off);
-  job.nblocks = p.nblocks;
-  p.keys = job.keys;
-  static_assert(sizeof(Job) <= kSlot && sizeof(State) <= kSlot, "workspace slots");
+  make_plan(a, kcam_host, init_host, static_cast<char *>(workspace), p, job);
 
   const cudaStream_t st = as_stream(stream);
   if (use_graph) return run_graph(p, job, history != nullptr, st);
@@ -1018,7 +1193,8 @@ extern "C" int stb_profile_read(double *ms_by_kind, int64_t *launches_by_kind,
 // the process exits.  The first call on a device looks up the array's device
 // address with cudaGetSymbolAddress (host code cannot use the symbol itself:
 // it names a host-side stand-in); make that first call before any stream
-// capture.  All calls share the one array: two calls whose work overlaps on
+// capture.  The address is cached for the life of the process, so a device
+// reset (cudaDeviceReset) ends this entry point's use on that device.  All calls share the one array: two calls whose work overlaps on
 // the GPU race and corrupt each other.  What must start cleared is cleared by
 // every call (the key map and the per-call state), the rest is written
 // before it is read.
@@ -1026,10 +1202,10 @@ extern "C" int stb_profile_read(double *ms_by_kind, int64_t *launches_by_kind,
 namespace stb {
 namespace {
 
-constexpr int64_t kStaticMaxPixels = 1 << 20;  // e.g. 1280x720 fits
-constexpr size_t kStaticWorkspaceBytes =
-    2 * kSlot + 2 * ((sizeof(float) * kAccs * ((kStaticMaxPixels + 1023) / 1024) + 255) & ~size_t(255)) +
-    sizeof(unsigned long long) * kStaticMaxPixels;
+constexpr int64_t kStaticMaxPixels = 1 << 20;  // e.g. 1280x720 and 1024x1024 fit
+// The layout of stb_icp_estimate's workspace at the largest frame: every
+// frame up to kStaticMaxPixels fits (workspace_bytes grows with the pixels).
+constexpr size_t kStaticWorkspaceBytes = workspace_bytes(kStaticMaxPixels);
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_static_workspace[kStaticWorkspaceBytes];
@@ -1079,94 +1255,21 @@ extern "C" int stb_icp_estimate_static(
                 "(its fixed scratch), got %dx%d = %lld; use stb_icp_estimate with a "
                 "caller-provided workspace", (long long)kStaticMaxPixels, height, width,
                 (long long)npix);
-  if (num_source < 0 || (unsigned long long)num_source >= kMaxSources)
-    return fail(STB_EINVAL, "Check failed: num_source must be in [0, 2^24), got %lld",
-                (long long)num_source);
-  if (num_iters < 0 || num_iters > 254)
-    return fail(STB_EINVAL, "Check failed: num_iters must be in [0, 254], got %d", num_iters);
-  const bool use_feat = feat_weight > 0.0 && src_feats && tgt_feats;
-  const bool use_geom = geom_weight > 0.0;
-  if (use_feat) {
-    if (channels <= 0)
-      return fail(STB_EINVAL, "Check failed: channels must be positive, got %d", channels);
-    if (feat_dtype < STB_F32 || feat_dtype > STB_BF16_HWC)
-      return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
-    if (channel_mode != 0 && channel_mode != 1)
-      return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
-  }
+  const EstimateArgs a{kcam, src_points, src_normals, src_mask, num_source, src_feats,
+                       tgt_points, tgt_normals, tgt_mask, height, width, tgt_feats, channels,
+                       feat_dtype, init_transform, num_iters, geom_weight, feat_weight,
+                       distance_thresh, normal_angle_thresh, feat_residual_thresh,
+                       channel_mode, result, history};
   bool kcam_host, init_host;
-  STB_TRY(check_small_input(kcam, "kcam", false, &kcam_host));
-  STB_TRY(check_device_ptr(src_points, "src_points"));
-  STB_TRY(check_device_ptr(src_normals, "src_normals"));
-  STB_TRY(check_device_ptr(src_mask, "src_mask"));
-  STB_TRY(check_device_ptr(tgt_points, "tgt_points"));
-  STB_TRY(check_device_ptr(tgt_normals, "tgt_normals"));
-  STB_TRY(check_device_ptr(tgt_mask, "tgt_mask"));
-  if (use_feat) {
-    STB_TRY(check_device_ptr(src_feats, "src_feats"));
-    STB_TRY(check_device_ptr(tgt_feats, "tgt_feats"));
-  }
-  STB_TRY(check_small_input(init_transform, "transform", true, &init_host));
-  STB_TRY(check_device_ptr(result, "result"));
-  STB_TRY(check_device_ptr(history, "history", true));
+  STB_TRY(check_args(a, &kcam_host, &init_host));
   STB_TRY(prepare_reduce_kernels());
   void *workspace = nullptr;
   STB_TRY(static_workspace(&workspace));
-
-  char *ws = static_cast<char *>(workspace);
-  Plan p;
-  p.n = num_source;
-  p.H = height;
-  p.W = width;
-  p.C = use_feat ? channels : 0;
-  p.dtype = use_feat ? feat_dtype : 0;
-  p.iters = num_iters;
-  p.use_geom = use_geom;
-  p.use_feat = use_feat;
-  p.channel_mode = use_feat ? channel_mode : 0;
-  p.nblocks = reduce_blocks(npix);
-  p.job_dev = reinterpret_cast<Job *>(ws);
-
-  Job job;
-  job.sp = src_points;
-  job.sn = src_normals;
-  job.sm = src_mask;
-  job.n = num_source;
-  job.sf = src_feats;
-  job.tp = tgt_points;
-  job.tn = tgt_normals;
-  job.tm = tgt_mask;
-  job.H = height;
-  job.W = width;
-  job.tf = tgt_feats;
-  job.C = p.C;
-  job.dtype = p.dtype;
-  set_small_inputs(job, kcam, kcam_host, init_transform, init_host);
-  job.iters = num_iters;
-  job.channel_mode = p.channel_mode;
-  job.use_geom = use_geom;
-  job.use_feat = use_feat;
-  job.wg1 = (float)geom_weight;
-  job.wg2 = (float)(geom_weight * geom_weight);
-  job.wf1 = (float)feat_weight;
-  job.wf2 = (float)(feat_weight * feat_weight);
-  job.thr2 = distance_thresh_sq(distance_thresh);
-  job.cos_max = angle_cos_max(normal_angle_thresh);
-  {
-    const float t = (float)feat_residual_thresh;
-    job.feat_thr2 = t * t;
-  }
-  job.result = result;
-  job.history = history;
-  size_t off = 2 * kSlot;
-  job.state = reinterpret_cast<State *>(ws + kSlot);
-  job.part = reinterpret_cast<float2 *>(ws + off);
-  off += align256(sizeof(float2) * kSlotAccs * p.nblocks);
-  job.keys = reinterpret_cast<unsigned long long *>(ws + off);
-  job.nblocks = p.nblocks;
-  p.keys = job.keys;
-  if (off + sizeof(unsigned long long) * (size_t)npix > kStaticWorkspaceBytes)
+  if (workspace_bytes(npix) > kStaticWorkspaceBytes)
     return fail(STB_EINVAL, "Check failed: stb_icp_estimate_static scratch too small");
+  Plan p;
+  Job job;
+  make_plan(a, kcam_host, init_host, static_cast<char *>(workspace), p, job);
 
   // Direct launches only: no graph, no stream and no event is created here.
   const cudaStream_t st = as_stream(stream);

@@ -24,6 +24,7 @@
 #include <math.h>
 
 #include "gn_solve.cuh"
+#include "keymap.cuh"
 #include "stb_common.cuh"
 #include "stb_host.hpp"
 
@@ -599,4 +600,24 @@ extern "C" int stb_icp_loss_backward(const float *src_depth, const float *src_no
                                    reinterpret_cast<unsigned *>(ws + g.tickets), grad_tangent,
                                    grad_depth);
   return check_launch("stb_icp_loss_backward");
+}
+
+extern "C" int stb_icp_loss_correspondences(const void *workspace, int32_t num_pairs,
+                                            int32_t height, int32_t width, int64_t *merge_map,
+                                            void *stream) {
+  clear_error();
+  if (num_pairs <= 0 || height <= 0 || width <= 0)
+    return fail(STB_EINVAL, "Check failed: sizes must be positive, got %d pairs of %dx%d",
+                num_pairs, height, width);
+  if (((uintptr_t)workspace & 255) != 0)
+    return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
+  STB_TRY(check_device_ptr(workspace, "workspace"));
+  STB_TRY(check_device_ptr(merge_map, "merge_map"));
+  const int64_t n = (int64_t)num_pairs * height * width;
+  const GradLayout g = grad_layout(num_pairs, (int64_t)height * width);
+  const auto *keys = reinterpret_cast<const unsigned long long *>(
+      static_cast<const char *>(workspace) + g.keys);
+  k_keys_to_merge_map<<<keys_grid(n), 256, 0, as_stream(stream)>>>(
+      keys, nullptr, n, kTag, reinterpret_cast<long long *>(merge_map));
+  return check_launch("stb_icp_loss_correspondences");
 }

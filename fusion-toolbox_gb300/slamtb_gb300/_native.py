@@ -25,6 +25,8 @@ RES_RESIDUAL, RES_MATCHES, RES_ITERS, RES_STATUS, RES_SIZE = 88, 89, 90, 91, 96
 HIST_TRANSFORM, HIST_JTJ, HIST_JR, HIST_R2 = 0, 16, 52, 58
 HIST_GEOM_COUNT, HIST_FEAT_COUNT, HIST_OK, HIST_SIZE = 59, 60, 61, 64
 ST_NOT_PD, ST_NO_MATCHES, ST_NAN = 1, 2, 4
+# option bits or-ed into the channel_mode argument of the registration calls
+OPT_DW_SOLVE = 0x100
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -51,6 +53,10 @@ _SIGNATURES = {
     "stb_icp_information_partials": (ctypes.c_int, [
         _vp, _vp, _i64, _vp, _vp, _i32, _i32, _vp, _vp, _vp, _vp]),
     "stb_icp_workspace_bytes": (_sz, [_i64, _i32, _i32]),
+    "stb_icp_correspondences": (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _vp]),
+    "stb_icp_batch_correspondences": (ctypes.c_int, [_vp, _i32, _i64, _i32, _i32, _i32, _i32,
+                                                     _vp, _vp]),
+    "stb_icp_loss_correspondences": (ctypes.c_int, [_vp, _i32, _i32, _i32, _vp, _vp]),
     "stb_icp_batch_workspace_bytes": (_sz, [_i32, _i64]),
     "stb_icp_estimate_batch": (ctypes.c_int, [
         _vp, _i32, _i32, _vp, _i32, _i32, _i32, _vp, _i64, _vp, _sz, _vp, _vp, _i32, _vp]),

@@ -30,12 +30,15 @@ class BatchRegistration:
             level, finest first, as ``MultiscaleRegistration``; at most 4
             levels and 253 iterations in total.
         feat_channel_mode (str): "last" (reference) or "sum".
+        solve_precision (str): "fp64" (default: FP64 solve, exponential and
+            pose update) or "dw" (double-word float32, ~48 bits).
         record_history (bool): keep per-iteration records in
             ``self.last_history`` ((pairs, total iterations, 64) float64 CPU,
             iterations numbered over the levels coarsest first).
     """
 
-    def __init__(self, estimators, feat_channel_mode="last", record_history=False):
+    def __init__(self, estimators, feat_channel_mode="last", record_history=False,
+                 solve_precision="fp64"):
         if not 1 <= len(estimators) <= 4:
             raise ValueError("BatchRegistration takes 1 to 4 levels")
         for _, est in estimators:
@@ -43,7 +46,10 @@ class BatchRegistration:
                 raise TypeError("BatchRegistration levels must be ICPOdometry estimators")
         if feat_channel_mode not in ("last", "sum"):
             raise ValueError("feat_channel_mode must be 'last' or 'sum'")
+        if solve_precision not in ("fp64", "dw"):
+            raise ValueError("solve_precision must be 'fp64' or 'dw'")
         self.estimators = estimators
+        self.solve_precision = solve_precision
         self.feat_channel_mode = feat_channel_mode
         self.record_history = record_history
         self.last_history = None
@@ -137,7 +143,8 @@ class BatchRegistration:
                                        dtype=torch.float64, device=device)
         plan.num_source = [sources[p][-1].mask.numel() for p in range(B)]
         plan.keep = keep
-        plan.mode = 0 if self.feat_channel_mode == "last" else 1
+        plan.mode = ((0 if self.feat_channel_mode == "last" else 1)
+                     | (N.OPT_DW_SOLVE if self.solve_precision == "dw" else 0))
         return plan
 
     def run(self, plan, tile_config=None):

@@ -90,6 +90,10 @@ class ICPOdometry:
             from texel-major copies (all channels of a pixel adjacent, built
             on the device per call); "planar" reads the (C, H, W) maps as
             given.  Results are identical.
+        solve_precision (str): "fp64" (default: the 6x6 solve, the SE(3)
+            exponential and the pose update in FP64, as the reference's
+            float64 host solve) or "dw" (double-word float32, ~48 bits, on
+            the FP32 pipes).
         use_graph (bool): replay the launch sequence as a CUDA graph.
         record_history (bool): keep per-iteration records in
             ``self.last_history`` (float64 (num_iters, 64) CPU tensor, layout
@@ -99,7 +103,8 @@ class ICPOdometry:
     def __init__(self, num_iters, geom_weight=1.0, feat_weight=1.0, so3=False,
                  distance_threshold=.5, normals_angle_thresh=math.pi / 4,
                  feat_residual_thresh=2.75, feat_channel_mode="last",
-                 use_graph=True, record_history=False, feat_layout="auto"):
+                 use_graph=True, record_history=False, feat_layout="auto",
+                 solve_precision="fp64"):
         if so3:
             raise NotImplementedError(
                 "so3=True is not supported: the reference's rotation-only path "
@@ -111,6 +116,8 @@ class ICPOdometry:
             raise ValueError("feat_channel_mode must be 'last' or 'sum'")
         if feat_layout not in ("auto", "planar"):
             raise ValueError("feat_layout must be 'auto' or 'planar'")
+        if solve_precision not in ("fp64", "dw"):
+            raise ValueError("solve_precision must be 'fp64' or 'dw'")
         self.num_iters = num_iters
         self.geom_weight = geom_weight
         self.feat_weight = feat_weight
@@ -120,6 +127,7 @@ class ICPOdometry:
         self.feat_residual_thresh = feat_residual_thresh
         self.feat_channel_mode = feat_channel_mode
         self.feat_layout = feat_layout
+        self.solve_precision = solve_precision
         self.use_graph = use_graph
         self.record_history = record_history
         self.last_history = None
@@ -222,7 +230,8 @@ class ICPOdometry:
                 float(self.feat_weight if has_features else 0.0),
                 float(self.distance_threshold), float(self.normals_angle_thresh),
                 float(self.feat_residual_thresh),
-                0 if self.feat_channel_mode == "last" else 1,
+                (0 if self.feat_channel_mode == "last" else 1)
+                | (N.OPT_DW_SOLVE if self.solve_precision == "dw" else 0),
                 N.ptr(ws), ws.numel(), N.ptr(res), N.ptr(hist), int(self.use_graph),
                 N.stream_of(device)))
         del k, init  # kept alive through the call

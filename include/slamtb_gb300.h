@@ -70,6 +70,14 @@ extern "C" {
 #define STB_I32 8
 #define STB_I64 9
 
+/* ---- option bits, or-ed into the channel_mode argument of the
+ * registration entry points (the low byte is the channel mode) ---------- */
+/* Gauss-Newton step in double-word float32 arithmetic (~48 significant
+ * bits, FP32 pipes only) instead of the default FP64 solve, exponential
+ * and pose composition.  No counterpart in the reference (its solve is
+ * FP64 on the host, slamtb/registration/icp.py:236-251). */
+#define STB_OPT_DW_SOLVE 0x100
+
 /* ---- per-registration status bits (result block, STB_RES_STATUS) ------- */
 #define STB_ST_NOT_PD 1u     /* 6x6 J^T J was not positive definite: stopped */
 #define STB_ST_NO_MATCHES 2u /* an iteration found no correspondence        */
@@ -246,6 +254,21 @@ STB_API int stb_icp_estimate(const float *kcam, const float *src_points,
                      void *workspace, size_t workspace_bytes, double *result,
                      double *history, int32_t use_graph, void *stream);
 
+/*
+ * The correspondences of the association at the final pose of the last
+ * stb_icp_estimate call on this workspace (the pass that feeds the
+ * information matrix, icp.py:258-261), in the reference's correspondence-map
+ * layout: merge_map int64 [height, width] = (source index << 32) | float32
+ * bits of the distance, 0x0fffffff7f800000 where no source point matched
+ * (slamtb/registration/correspondence_map.py:5, src/merge_map.hpp:54-98).
+ * height, width and num_iters are those of that call; run it first on the
+ * same stream (or synchronise).  The fused kernels keep an epoch-tagged key
+ * map that no reference function exposes; this entry point decodes it, so
+ * callers that consume the reference's map (FPCLMatcherOp, the partial
+ * entry points above) can reuse the registration's last association.
+ */
+STB_API int stb_icp_correspondences(const void *workspace, int32_t height, int32_t width,
+                                    int32_t num_iters, int64_t *merge_map, void *stream);
 
 /* ======================================================================= *
  * Batched, multiscale registration in one persistent launch
@@ -315,6 +338,19 @@ STB_API int stb_icp_estimate_batch(
     int32_t channel_mode, const double *init_transforms,
     int64_t total_target_pixels, void *workspace, size_t workspace_bytes,
     double *results, double *history, int32_t tile_config, void *stream);
+
+/*
+ * Pair `pair`'s correspondences at its final pose after the last
+ * stb_icp_estimate_batch call on this workspace (the association of the
+ * information pass on the finest level), in the layout of
+ * stb_icp_correspondences.  num_pairs and total_target_pixels are those of
+ * that call; height x width is the pair's finest level; total_iters is the
+ * sum of num_iters over the levels of that call.
+ */
+STB_API int stb_icp_batch_correspondences(const void *workspace, int32_t num_pairs,
+                                          int64_t total_target_pixels, int32_t pair,
+                                          int32_t height, int32_t width, int32_t total_iters,
+                                          int64_t *merge_map, void *stream);
 
 /*
  * Processing::BilateralDepthFilter (src/bilateral_depth_filter.cu:15-110):
@@ -398,6 +434,15 @@ STB_API int stb_icp_loss_forward(const float *src_depth, const float *src_normal
                                  size_t workspace_bytes, double *loss, void *stream);
 
 /*
+ * The correspondences that the last stb_icp_loss_forward call on this
+ * workspace found, for every pair: merge_map int64 [num_pairs][height]
+ * [width] in the layout of stb_icp_correspondences.
+ */
+STB_API int stb_icp_loss_correspondences(const void *workspace, int32_t num_pairs,
+                                         int32_t height, int32_t width, int64_t *merge_map,
+                                         void *stream);
+
+/*
  * Adjoint of stb_icp_loss_forward at the correspondences it found (same
  * inputs, poses and workspace): with g = grad_loss[p],
  *   grad_tangent[p] = g * dL_p/de = -2 g sum r J,  J = [n; Tp x n], for the
@@ -427,9 +472,13 @@ STB_API int stb_icp_loss_backward(const float *src_depth, const float *src_norma
  * pixels (height * width; about 8.6 MB, held by every GPU that loads the
  * library until the process exits); larger frames are rejected with
  * STB_EINVAL.  The first call on a device looks up that array's address
- * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
- * uses the same array: calls whose work overlaps on the GPU race.  Same
- * arguments and results as stb_icp_estimate, minus workspace and graphs.
+ * (cudaGetSymbolAddress), so make it before any stream capture.  The
+ * address is kept for the life of the process: after cudaDeviceReset on a
+ * device, this entry point must not be called on that device again (the
+ * library's module, and the array with it, may be reloaded elsewhere).
+ * Every call uses the same array: calls whose work overlaps on the GPU race.
+ * Same arguments and results as stb_icp_estimate, minus workspace and
+ * graphs.
  */
 STB_API int stb_icp_estimate_static(
     const float *kcam, const float *src_points, const float *src_normals,

@@ -106,7 +106,7 @@ def test_host_tensors_are_refused():
 
 def _python_name(name):
     """Header constant -> its name in slamtb_gb300._native."""
-    for prefix in ("STB_ST_", "STB_RES_", "STB_HIST_"):
+    for prefix in ("STB_ST_", "STB_RES_", "STB_HIST_", "STB_OPT_"):
         if name.startswith(prefix):
             return name[len("STB_"):]
     return name
@@ -117,10 +117,11 @@ def test_header_constants_match_the_python_mirror():
     status bits, result and history layouts) has the same value in
     slamtb_gb300._native."""
     import re
-    defs = re.findall(r"^#define (STB_\w+) (\d+)u?\b", HEADER.read_text(), re.M)
-    assert len(defs) >= 30
-    mismatched = [(n, int(v), getattr(_native, _python_name(n), None)) for n, v in defs
-                  if getattr(_native, _python_name(n), None) != int(v)]
+    defs = re.findall(r"^#define (STB_\w+) (0x[0-9a-fA-F]+|\d+)u?\b", HEADER.read_text(),
+                      re.M)
+    assert len(defs) >= 31 and ("STB_OPT_DW_SOLVE", "0x100") in defs
+    mismatched = [(n, int(v, 0), getattr(_native, _python_name(n), None)) for n, v in defs
+                  if getattr(_native, _python_name(n), None) != int(v, 0)]
     assert not mismatched, mismatched
 
 

@@ -147,7 +147,8 @@ def test_icp_odometry_constructor_checks():
     """ICPOdometry keeps the reference's keyword defaults (icp.py:137-139)
     and refuses what it cannot run: so3=True (the reference's rotation-only
     path fails with a TypeError, icp.py:71-76), more iterations than the
-    key map's epoch tags, and unknown channel modes or layouts."""
+    key map's epoch tags, and unknown channel modes, layouts or solve
+    precisions; the solve is FP64 unless asked otherwise."""
     from slamtb_gb300.registration import ICPOdometry
     icp = ICPOdometry(10)
     assert (icp.geom_weight, icp.feat_weight, icp.so3) == (1.0, 1.0, False)
@@ -162,6 +163,9 @@ def test_icp_odometry_constructor_checks():
         ICPOdometry(10, feat_channel_mode="max")
     with pytest.raises(ValueError, match="feat_layout"):
         ICPOdometry(10, feat_layout="hwc")
+    assert icp.solve_precision == "fp64"
+    with pytest.raises(ValueError, match="solve_precision"):
+        ICPOdometry(10, solve_precision="fp32")
 
 
 def test_point_to_plane_loss_argument_checks():
