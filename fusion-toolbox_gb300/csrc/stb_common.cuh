@@ -21,10 +21,12 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
-// ((a0*b0 + a1*b1) + a2*b2): Eigen's dot/squaredNorm order on 3-vectors.
+// a0*b0 + (a1*b1 + a2*b2): the order in which the reference's Eigen sums
+// the dot product and squared norm of 3-vectors (its unrolled reduction,
+// Eigen/src/Core/Redux.h redux_novec_unroller, splits three terms at one).
 __device__ __forceinline__ float dot3(float a0, float a1, float a2, float b0,
                                       float b1, float b2) {
-  return fadd(fadd(fmul(a0, b0), fmul(a1, b1)), fmul(a2, b2));
+  return fadd(fmul(a0, b0), fadd(fmul(a1, b1), fmul(a2, b2)));
 }
 
 // float32 view of the pose and intrinsics the kernels need:

@@ -50,7 +50,9 @@ def depth_to_points(depth, kcam):
 
 
 def _sqnorm(a):
-    return (a[..., 0] * a[..., 0] + a[..., 1] * a[..., 1]) + a[..., 2] * a[..., 2]
+    """Eigen's ``squaredNorm`` of 3-vectors: ``a0^2 + (a1^2 + a2^2)`` (the
+    unrolled redux of Eigen/src/Core/Redux.h splits three terms at one)."""
+    return a[..., 0] * a[..., 0] + (a[..., 1] * a[..., 1] + a[..., 2] * a[..., 2])
 
 
 def _cross(a, b):

@@ -132,11 +132,16 @@ def pixel_of(kcam, tp, width, height):
 
 
 def sqnorm32(d):
-    return (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+    """Eigen's ``squaredNorm`` of float32 3-vectors: the unrolled redux of
+    Eigen/src/Core/Redux.h (``redux_novec_unroller``) splits the three
+    terms at one, so the sum is ``d0^2 + (d1^2 + d2^2)``."""
+    return d[:, 0] * d[:, 0] + (d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
 
 
 def dot32(a, b):
-    return (a[:, 0] * b[:, 0] + a[:, 1] * b[:, 1]) + a[:, 2] * b[:, 2]
+    """Eigen's ``dot`` of float32 3-vectors, ``a0 b0 + (a1 b1 + a2 b2)``
+    (the redux order of ``sqnorm32``)."""
+    return a[:, 0] * b[:, 0] + (a[:, 1] * b[:, 1] + a[:, 2] * b[:, 2])
 
 
 def cross32(a, b):

@@ -96,8 +96,11 @@ static inline int project_round(const pose32_t *P, const float *p, int W, int H,
   return 1;
 }
 
+/* Eigen's dot / squaredNorm of 3-vectors: its unrolled redux
+ * (Eigen/src/Core/Redux.h, redux_novec_unroller) splits three terms at one,
+ * a0 b0 + (a1 b1 + a2 b2). */
 static inline float dot3(const float *a, const float *b) {
-  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+  return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]);
 }
 
 static float angle_cos_max(double angle) {

@@ -1,9 +1,9 @@
 """Extract the known-answer fixtures from the reference's own test data.
 
-Run in a container where the reference is mounted (it is read here, never
-at test time):
+Run where a copy of the reference tree is available, with its root as the
+only argument (it is read here, never at test time):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference root>
 
 It decodes the 16-bit depth PNGs of ``test-data/rgbd/sample2`` frames used
 by the reference's tests (frames 0 and 3: the synthetic pair of
@@ -84,4 +84,6 @@ def main(reference_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference root>")
+    main(sys.argv[1])

@@ -433,12 +433,12 @@ def _associate_literal(sp, sn, sm, rt, tp, tn, tm, kcam, dist_th, angle_th):
             continue
         q, m = tp[vi, ui], tn[vi, ui]
         d = [q[k] - p[k] for k in range(3)]
-        sq = (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]
+        sq = d[0] * d[0] + (d[1] * d[1] + d[2] * d[2])  # Eigen squaredNorm
         if sq > d2:
             continue
-        dot = (n[0] * m[0] + n[1] * m[1]) + n[2] * m[2]
-        na = np.sqrt((n[0] * n[0] + n[1] * n[1]) + n[2] * n[2])
-        nb = np.sqrt((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2])
+        dot = n[0] * m[0] + (n[1] * m[1] + n[2] * m[2])  # Eigen dot, norm
+        na = np.sqrt(n[0] * n[0] + (n[1] * n[1] + n[2] * n[2]))
+        nb = np.sqrt(m[0] * m[0] + (m[1] * m[1] + m[2] * m[2]))
         with np.errstate(invalid="ignore"):
             angle = abs(np.arccos(dot / (na * nb)))
         if angle >= ath:
@@ -644,7 +644,7 @@ def test_geometric_and_information_partials_match_the_reference_steps():
         q, m = tp[vi, ui], tn[vi, ui]
         lcnt += 1
         d = [q[k] - p[k] for k in range(3)]
-        r = (d[0] * m[0] + d[1] * m[1]) + d[2] * m[2]
+        r = d[0] * m[0] + (d[1] * m[1] + d[2] * m[2])  # Eigen dot
         J = [m[0], m[1], m[2], p[1] * m[2] - p[2] * m[1], p[2] * m[0] - p[0] * m[2],
              p[0] * m[1] - p[1] * m[0]]
         for a in range(6):
@@ -685,8 +685,8 @@ def test_normals_and_xyz_downsample_match_the_reference_steps():
     def sub(a, b):
         return [a[0] - b[0], a[1] - b[1], a[2] - b[2]]
 
-    def sq(a):
-        return (a[0] * a[0] + a[1] * a[1]) + a[2] * a[2]
+    def sq(a):  # Eigen squaredNorm
+        return a[0] * a[0] + (a[1] * a[1] + a[2] * a[2])
 
     zero = [f(0), f(0), f(0)]
     normals = np.zeros((h, w, 3), f)
