@@ -66,7 +66,11 @@ WORKLOAD = ("plain geometric point-to-plane ICP, 1 frame pair 640x480 per rank, 
 # association = source xyz + normal + mask (25) + gathered target xyz +
 # normal + mask (25) + correspondence-map init and update (16);
 # reduction = source xyz + mask (13) + map (8) + target xyz + normal (24).
-ALG_BYTES = {"association": 66, "reduction+solve": 45}
+# The single-launch registration kernel runs ITERS associations and
+# reductions, then the association at the final pose and the information
+# pass (the map 8 + matched target xyz 12).
+ALG_BYTES = {"association": 66, "reduction+solve": 45,
+             "registration": ITERS * (66 + 45) + 66 + 20}
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -79,6 +83,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--secondary-out", default=None,
+                    help="write the full secondary results (JSON) to this file; the JSON "
+                         "line carries their summary")
     ap.add_argument("--profile-case", choices=["batch", "loss", "feature"], default=None,
                     help="run only a small case of one secondary workload (for ncu captures)")
     ap.add_argument("--pairs", type=int, default=8, help="pairs of the --profile-case")
@@ -305,6 +312,67 @@ def _rel_pose(a, b):
         math.hypot(angb, np.linalg.norm(Bb[:3, 3])), 1e-3)
 
 
+def _oracle_worker(job):
+    """One pair's free-running FP64 oracle registration (run in a spawned
+    process: numpy only).  job = (levels coarsest first, estimator keyword
+    dicts finest first, channel mode).  Returns (final transform or None,
+    condition number of the last successful step's J^T J)."""
+    import numpy as np
+    from oracle import icp_oracle as io
+    levels, ests, mode = job
+    res = io.multiscale_estimate(levels, [dict(e, channel_mode=mode) for e in ests])
+    cond = float(np.linalg.cond(res.JtJ)) if res.JtJ is not None else None
+    return (None if res.transform is None else np.asarray(res.transform)), cond
+
+
+def _oracle_jobs(pyrs, iters, wg, wf, mode):
+    """Host copies of device pyramids as oracle jobs (features as float32,
+    what the oracle reads of BF16 maps)."""
+    import torch
+    jobs = []
+    for spyr, tpyr, sfp, tfp in pyrs:
+        levels = []
+        for lv in range(len(spyr)):
+            s, t = spyr[lv], tpyr[lv]
+            d = dict(kcam=s.kcam.matrix.cpu().numpy() if torch.is_tensor(s.kcam.matrix)
+                     else s.kcam.matrix,
+                     src_points=s.points.cpu().numpy(), src_normals=s.normals.cpu().numpy(),
+                     src_mask=s.mask.cpu().numpy(), tgt_points=t.points.cpu().numpy(),
+                     tgt_normals=t.normals.cpu().numpy(), tgt_mask=t.mask.cpu().numpy())
+            if sfp is not None and wf > 0:
+                d["src_feats"] = sfp[lv].float().cpu().numpy().reshape(sfp[lv].size(0), -1)
+                d["tgt_feats"] = tfp[lv].float().cpu().numpy()
+            levels.append(d)
+        ests = [dict(num_iters=n, geom_weight=wg, feat_weight=wf, distance_threshold=DIST,
+                     normals_angle_thresh=ANGLE) for n in iters]
+        jobs.append((levels, ests, mode))
+    return jobs
+
+
+def _oracle_errors(results, jobs, workers):
+    """Each pair's free-running final-pose error of the GPU result against
+    the FP64 oracle's registration from the same start (||log(T_o^-1 T)||
+    over max(||log T_o||, 1e-3)), with the fraction within 1e-5 and the
+    three worst pairs with the condition number of their final J^T J."""
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(workers) as pool:
+        outs = list(pool.imap(_oracle_worker, jobs, chunksize=1))
+    errs = []
+    for k, (r, (To, cond)) in enumerate(zip(results, outs)):
+        if r.transform is None or To is None:
+            errs.append((k, None if (r.transform is None) == (To is None) else math.inf, cond))
+            continue
+        errs.append((k, _rel_pose(r.transform.numpy(), To), cond))
+    vals = [e for _, e, _ in errs if e is not None]
+    worst = sorted([x for x in errs if x[1] is not None], key=lambda x: -x[1])[:3]
+    return {"pairs": len(errs), "both_failed": sum(1 for _, e, _ in errs if e is None),
+            "max": max(vals) if vals else None,
+            "median": statistics.median(vals) if vals else None,
+            "within_1e-5": sum(1 for v in vals if v <= 1e-5) / max(len(vals), 1),
+            "within_1e-3": sum(1 for v in vals if v <= 1e-3) / max(len(vals), 1),
+            "worst": [{"pair": k, "err": e, "cond_JtJ": c} for k, e, c in worst]}
+
+
 def _alg_bytes_batch(pyrs, iters, feat_bytes=0):
     """Algorithmic bytes of one batch run: per level and iteration, the
     association reads 66 B per source pixel and the reduction 45 B (+ the
@@ -363,7 +431,7 @@ def _compare(batch_res, plain_T):
 
 
 def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps_plain,
-                    feat_bytes=0, mode="last"):
+                    feat_bytes=0, mode="last", oracle_workers=0):
     from slamtb_gb300.registration import BatchRegistration, MultiscaleRegistration
     ests = _estimators(iters, scales, wg, wf)
     pyrs = _pyramids(pairs, scales)
@@ -383,6 +451,12 @@ def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps
     peak, kind = measured_peak()
     gt_err = [_rel_pose(r.transform.numpy(), p[4]) if r.transform is not None else None
               for r, p in zip(res, pairs)]
+    vs_oracle = None
+    if oracle_workers:
+        t0 = time.perf_counter()
+        vs_oracle = _oracle_errors(res, _oracle_jobs(pyrs, iters, wg, wf, mode),
+                                   oracle_workers)
+        vs_oracle["wall_s"] = time.perf_counter() - t0
     return {
         "workload": name, "pairs": B, "iters": iters, "scales": scales,
         "weights": {"geometric": wg, "feature": wf},
@@ -394,6 +468,7 @@ def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps
                   "path": "MultiscaleRegistration.estimate_pyramid pair by pair"},
         "speedup_batch_vs_plain": t_plain / t_batch,
         "rel_pose_diff_batch_vs_plain": dict(zip(("max", "median"), _compare(res, plain_T))),
+        "batch_vs_fp64_oracle": vs_oracle,
         "median_rel_pose_err_vs_ground_truth": statistics.median(
             [e for e in gt_err if e is not None]) if any(e is not None for e in gt_err) else None,
         "roofline": {"bound": "hbm", "kernel": "k_batch (whole run)",
@@ -401,6 +476,12 @@ def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps
                      "peak": peak, "peak_source": kind, "unit": "GB/s",
                      "frac": alg / t_batch / 1e9 / peak},
     }
+
+
+def oracle_workers():
+    """Processes of the FP64 oracle's accuracy runs (the host's cores, at
+    most 16)."""
+    return max(1, min(16, len(os.sched_getaffinity(0))))
 
 
 def secondary_multiscale(device, seed):
@@ -416,6 +497,11 @@ def secondary_multiscale(device, seed):
     br.autotune(plan)
     t_b = _time_batch(br, plan, 100, device)
     res = br.results(plan)
+    # both paths' free-running results against the FP64 oracle's
+    jobs = _oracle_jobs(pyrs, iters, 1.0, 0.1, "last")
+    plain_res = MultiscaleRegistration(ests).estimate_pyramid(*pyrs[0])
+    vs_oracle = {"plain": _oracle_errors([plain_res], jobs, 1),
+                 "batch": _oracle_errors(res, jobs, 1)}
     return {"workload": "multiscale hybrid ICP 640x480/320x240/160x120 [10, 5, 3], "
                         "geometric 1.0 + greyscale feature 0.1, 1 pair",
             "plain": {"registrations_per_s": 50 / t_plain,
@@ -427,7 +513,8 @@ def secondary_multiscale(device, seed):
                                       "tile_config": br.tile_config},
             "max_rel_pose_diff_batch_vs_plain": _rel_pose(res[0].transform.numpy(),
                                                           Ts[0].numpy()),
-            "rel_pose_err_vs_ground_truth": _rel_pose(res[0].transform.numpy(), pair[4])}
+            "rel_pose_err_vs_ground_truth": _rel_pose(res[0].transform.numpy(), pair[4]),
+            "vs_fp64_oracle": vs_oracle}
 
 
 def secondary_loss(device, seed, B=32):
@@ -489,7 +576,8 @@ def secondary_batch_uneven(device, seed, B=256):
     pairs = [device_pair(seed + 1000 + k, *sizes[i], device) for k, i in enumerate(pick)]
     out = _batch_vs_plain("batched uneven ICP, 256 pairs from {160x120 ... 1280x720}, "
                           "3 levels [10, 5, 3], geometric", pairs, [10, 5, 3],
-                          [1.0, 0.5, 0.5], 1.0, 0.0, device, 10, 2)
+                          [1.0, 0.5, 0.5], 1.0, 0.0, device, 10, 2,
+                          oracle_workers=oracle_workers())
     out["size_histogram"] = {f"{w}x{h}": int((pick == i).sum()) for i, (w, h) in enumerate(sizes)}
     return out
 
@@ -501,7 +589,8 @@ def secondary_feature_1080p(device, seed, B=16):
              for k in range(B)]
     return _batch_vs_plain("high-resolution feature ICP, 16 pairs 1920x1080, 16 BF16 channels, "
                            "4 levels [10, 8, 5, 3]", pairs, [10, 8, 5, 3],
-                           [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, device, 5, 1, feat_bytes=32)
+                           [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, device, 5, 1, feat_bytes=32,
+                           oracle_workers=oracle_workers())
 
 
 def secondary_bilateral(device, seed, reps=200):
@@ -551,12 +640,13 @@ def secondary_bilateral(device, seed, reps=200):
 
 
 def secondary_plain_sizes(device, seed, reps=20):
-    """The plain path's kernels at larger images (one pair, 10 iterations,
-    geometric): per-launch CUDA-event times of the association and of the
-    reduction with its step (the profiled graph replay), and the fraction
-    of the measured HBM bandwidth their algorithmic bytes reach.  At
-    640x480 an iteration is a latency chain; these show how the same
-    kernels do when there are bytes enough to stream."""
+    """The plain path at larger images (one pair, 10 iterations,
+    geometric): the single-launch registration's time and fraction of the
+    measured HBM bandwidth, and, for the multi-launch sequence, per-launch
+    CUDA-event times of the association and of the reduction with its step
+    (the profiled graph replay) with their fractions.  At 640x480 an
+    iteration is a latency chain; these show how the kernels do when there
+    are bytes enough to stream."""
     import torch
     from slamtb_gb300 import _native as N
     from slamtb_gb300 import synthetic
@@ -569,33 +659,38 @@ def secondary_plain_sizes(device, seed, reps=20):
         k = KCamera(p["kcam"])
         src = FramePointCloud.from_frame(Frame(FrameInfo(k), p["source_depth"]), device)
         tgt = FramePointCloud.from_frame(Frame(FrameInfo(k), p["target_depth"]), device)
-        icp = ICPOdometry(ITERS, geom_weight=1.0, feat_weight=0.0, distance_threshold=DIST,
-                          normals_angle_thresh=ANGLE)
         kc = torch.from_numpy(p["kcam"]).to(device)
         args_ = (kc, src.points.reshape(-1, 3), src.normals.reshape(-1, 3), src.mask.reshape(-1))
         kw = dict(target_points=tgt.points, target_mask=tgt.mask, target_normals=tgt.normals)
-        for _ in range(3):
-            icp.launch(*args_, **kw)
-        torch.cuda.synchronize(device)
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            icp.launch(*args_, **kw)
-        torch.cuda.synchronize(device)
-        reg_ms = (time.perf_counter() - t0) * 1e3 / reps
-        N.profile_enable(True)
-        prof = {kk: [0.0, 0] for kk in N.PROFILE_KINDS}
-        for _ in range(reps):
-            icp.launch(*args_, **kw)
+        case = {}
+        for launch in ("single", "multi"):
+            icp = ICPOdometry(ITERS, geom_weight=1.0, feat_weight=0.0, distance_threshold=DIST,
+                              normals_angle_thresh=ANGLE, launch=launch)
+            for _ in range(3):
+                icp.launch(*args_, **kw)
             torch.cuda.synchronize(device)
-            for kk, (ms, cnt) in N.profile_read().items():
-                prof[kk][0] += ms
-                prof[kk][1] += cnt
-        N.profile_enable(False)
-        case = {"registration_ms": reg_ms, "gn_iters_per_s": ITERS / (reg_ms * 1e-3)}
-        for kk in ("association", "reduction+solve"):
-            us = prof[kk][0] / max(prof[kk][1], 1) * 1e3
-            gbs = ALG_BYTES[kk] * w * h / (us * 1e-6) / 1e9
-            case[kk] = {"us_per_launch": us, "achieved_gbs": gbs, "frac": gbs / peak}
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                icp.launch(*args_, **kw)
+            torch.cuda.synchronize(device)
+            reg_ms = (time.perf_counter() - t0) * 1e3 / reps
+            N.profile_enable(True)
+            prof = {kk: [0.0, 0] for kk in N.PROFILE_KINDS}
+            for _ in range(reps):
+                icp.launch(*args_, **kw)
+                torch.cuda.synchronize(device)
+                for kk, (ms, cnt) in N.profile_read().items():
+                    prof[kk][0] += ms
+                    prof[kk][1] += cnt
+            N.profile_enable(False)
+            c = {"registration_ms": reg_ms, "gn_iters_per_s": ITERS / (reg_ms * 1e-3)}
+            kinds = ("registration",) if launch == "single" else ("association",
+                                                                  "reduction+solve")
+            for kk in kinds:
+                us = prof[kk][0] / max(prof[kk][1], 1) * 1e3
+                gbs = ALG_BYTES[kk] * w * h / (us * 1e-6) / 1e9
+                c[kk] = {"us_per_launch": us, "achieved_gbs": gbs, "frac": gbs / peak}
+            case[launch] = c
         out[f"{w}x{h}"] = case
     return out
 
@@ -729,6 +824,62 @@ def profile_case(args, device):
                       "ms_per_step": 1e3 * (time.perf_counter() - t) / args.steps}))
 
 
+def _r(x, nd=4):
+    """x rounded to nd significant digits (None stays None)."""
+    if x is None or isinstance(x, (str, bool)):
+        return x
+    if isinstance(x, int):
+        return x
+    return float(f"{x:.{nd}g}")
+
+
+def summarize(sec):
+    """The compact per-workload summary carried on the JSON line: rates,
+    speed-ups, roofline fractions and accuracy against the FP64 oracle."""
+    out = {}
+    for name, d in sec.items():
+        if "error" in d:
+            out[name] = {"error": d["error"]}
+            continue
+        if name == "multiscale_hybrid_640x480":
+            vo = d.get("vs_fp64_oracle") or {}
+            out[name] = {"plain_regs_per_s": _r(d["plain"]["registrations_per_s"]),
+                         "batch_regs_per_s": _r(d["batch_kernel_one_pair"]["registrations_per_s"]),
+                         "err_vs_fp64_oracle": {k: _r(v["max"]) for k, v in vo.items()},
+                         "err_vs_ground_truth": _r(d["rel_pose_err_vs_ground_truth"])}
+        elif name in ("batch_uneven_256", "feature_1080p_16ch_bf16"):
+            vo = d.get("batch_vs_fp64_oracle") or {}
+            out[name] = {"pairs": d["pairs"],
+                         "batch_pairs_per_s": _r(d["batch"]["pairs_per_s"]),
+                         "plain_pairs_per_s": _r(d["plain"]["pairs_per_s"]),
+                         "speedup": _r(d["speedup_batch_vs_plain"]),
+                         "frac": _r(d["roofline"]["frac"]),
+                         "batch_vs_plain": {k: _r(v) for k, v in
+                                            d["rel_pose_diff_batch_vs_plain"].items()},
+                         "vs_fp64_oracle": {
+                             "pairs": vo.get("pairs"), "max": _r(vo.get("max")),
+                             "median": _r(vo.get("median")),
+                             "within_1e-5": _r(vo.get("within_1e-5")),
+                             "within_1e-3": _r(vo.get("within_1e-3")),
+                             "worst": [{k: _r(v) for k, v in w.items()}
+                                       for w in vo.get("worst", [])]} if vo else None}
+        elif name == "loss_grad_32x640x480":
+            out[name] = {"pairs_per_s": _r(d["pairs_per_s"]), "frac": _r(d["roofline"]["frac"])}
+        elif name == "plain_kernels_larger_images":
+            out[name] = {size: {launch: {"gn_iters_per_s": _r(c["gn_iters_per_s"]),
+                                         **{k: _r(v["frac"]) for k, v in c.items()
+                                            if isinstance(v, dict)}}
+                                for launch, c in case.items()}
+                         for size, case in d.items() if "x" in size}
+        elif name == "bilateral_depth_filter":
+            out[name] = {k: _r(v["us_per_image"]) for k, v in d["cases"].items()}
+        elif name == "autograd_layer":
+            out[name] = {"exp_rt_mtwists_per_s": _r(d["exp_rt_to_matrix_fwd_bwd"]["mtwists_per_s"]),
+                         "matcher_mpoints_per_s":
+                             _r(d["fpcl_matcher_fwd_bwd_640x480"]["mpoints_per_s"])}
+    return out
+
+
 def run_secondary(device, seed):
     out = {}
     for name, fn in (("multiscale_hybrid_640x480", secondary_multiscale),
@@ -822,7 +973,8 @@ def main():
         for k, (ms, cnt) in N.profile_read().items():
             prof[k][0] += ms
             prof[k][1] += cnt
-    timed(min(args.steps, 200), step, between=read)
+    prof_steps = min(args.steps, 200)
+    timed(prof_steps, step, between=read)
     N.profile_enable(False)
     npix = H * W
     dom = max(ALG_BYTES, key=lambda k: prof[k][0])
@@ -925,7 +1077,7 @@ def main():
         secondary = run_secondary(device, args.seed)
 
     if rank == 0:
-        launches_per_step = 1 + 2 * ITERS + 2
+        launches_per_step = sum(v[1] for v in prof.values()) / max(prof_steps, 1)
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -935,7 +1087,8 @@ def main():
             "config": {"workload": WORKLOAD,
                        "l2": "flushed (512 MB write) before every step; the pair "
                              "(~18 MB) stays L2-resident across its 10 iterations",
-                       "graph": "CUDA graph per registration"},
+                       "launch": "one cooperative kernel per registration "
+                                 "(grid barriers between its phases)"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -948,10 +1101,12 @@ def main():
                     "mode": "double-buffered: upload of step k+1 overlaps step k; wall clock",
                     "one_call_at_a_time": {"value": sync_value, "unit": UNIT,
                                            "ms_per_step": sync_ms / e2e_steps}},
-            "gpu_launches": launches_per_step * args.steps,
+            "gpu_launches": int(round(launches_per_step * args.steps)),
             "clocks": clock_info,
-            "secondary": secondary,
+            "secondary_summary": summarize(secondary) if secondary else None,
         }))
+        if secondary and args.secondary_out:
+            pathlib.Path(args.secondary_out).write_text(json.dumps(secondary, indent=1) + "\n")
     if world > 1:
         dist.destroy_process_group()
 

@@ -72,6 +72,7 @@ struct BatchArgs {
   const double *init;
   double *results, *history;
   int solve_dw;    // 1: double-word solve (STB_OPT_DW_SOLVE), 0: FP64
+  unsigned spin_limit, bar_phantom;  // grid barriers' bounded waits
   unsigned *sync;  // [0] arrivals, [1] generation, [2] error
   PairState *ps;
   long long *key_off;   // [B + 1]
@@ -136,7 +137,9 @@ inline Layout layout(int B, long long total_pixels) {
 // arrival bumps the generation word that the others poll.
 constexpr int kBarGroup = 8;
 
-__device__ bool grid_sync(unsigned *sync) {
+// spin_limit: polls before a wait gives up; phantom: arrivals expected
+// beyond the grid's (0; a test sets more so that the waits run out).
+__device__ bool grid_sync(unsigned *sync, unsigned spin_limit, unsigned phantom) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -152,7 +155,7 @@ __device__ bool grid_sync(unsigned *sync) {
     if (atomicAdd(group, 1u) == gsize - 1) {
       atomicExch(group, 0u);
       __threadfence();
-      if (atomicAdd(root, 1u) == ngroups - 1) {
+      if (atomicAdd(root, 1u) == ngroups - 1 + phantom) {
         atomicExch(root, 0u);
         __threadfence();
         atomicAdd(sync + 1, 1u);
@@ -163,7 +166,7 @@ __device__ bool grid_sync(unsigned *sync) {
       unsigned spins = 0;
       while (*vgen == gen) {
         if (*verr) break;
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           atomicOr(sync + 2, 1u);
           break;
         }
@@ -1019,7 +1022,7 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
   stage_init(ctl);
   // phase 0: offsets (block 0), then pair states, key map, tickets
   if (blockIdx.x == 0) build_offsets(a);
-  if (!grid_sync(a.sync)) return;
+  if (!grid_sync(a.sync, a.spin_limit, a.bar_phantom)) return;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   for (long long p = gtid; p < a.B; p += gthreads) {
@@ -1040,7 +1043,7 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
   const long long nkeys = __ldcg(a.key_off + a.B);
   for (long long k = gtid; k < nkeys; k += gthreads) a.keys[k] = ~0ull;
   for (long long k = gtid; k < a.groups_cap; k += gthreads) a.grp_ticket[k] = 0;
-  if (!grid_sync(a.sync)) return;
+  if (!grid_sync(a.sync, a.spin_limit, a.bar_phantom)) return;
 
   int s = 0;
   int phase = 0;  // tile phases so far (selects the tile counter)
@@ -1070,7 +1073,7 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
       R[STB_RES_ITERS] = 0.0;
       R[STB_RES_RESIDUAL] = INFINITY;
     }
-    if (!grid_sync(a.sync)) return;
+    if (!grid_sync(a.sync, a.spin_limit, a.bar_phantom)) return;
     const size_t row = (size_t)level * (a.B + 1);
     const long long src_tiles = __ldcg(a.src_off + row + a.B);
     const long long tgt_tiles = __ldcg(a.tgt_off + row + a.B);
@@ -1080,13 +1083,13 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
       for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
         assoc_tile<kCh>(a, off, level, t, s, false, tc, ctl, ph);
       });
-      if (!grid_sync(a.sync)) return;
+      if (!grid_sync(a.sync, a.spin_limit, a.bar_phantom)) return;
       off = stage_offsets(a.tgt_off + row, a, s_off);
       reset_cache(tc);
       for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
         reduce_tile<FT, kFeat, false, kHWC, kCh>(a, off, level, t, s, tc, ctl, ph);
       });
-      if (!grid_sync(a.sync)) return;
+      if (!grid_sync(a.sync, a.spin_limit, a.bar_phantom)) return;
     }
   }
   // information matrix at the final pose (finest level)
@@ -1099,7 +1102,7 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
   for_each_tile(a.sync, phase++, src_tiles, [&](long long t) {
     assoc_tile<kCh>(a, off, level, t, s, true, tc, ctl, ph);
   });
-  if (!grid_sync(a.sync)) return;
+  if (!grid_sync(a.sync, a.spin_limit, a.bar_phantom)) return;
   off = stage_offsets(a.tgt_off + row, a, s_off);
   reset_cache(tc);
   for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
@@ -1223,6 +1226,13 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   a.dtype = feat_dtype;
   a.mode = channel_mode & 0xff;
   a.solve_dw = (channel_mode & STB_OPT_DW_SOLVE) != 0;
+  {
+    unsigned limit = 0;
+    int phantom = 0;
+    wait_test_limits(&limit, &phantom);
+    a.spin_limit = limit ? limit : kSpinLimit;
+    a.bar_phantom = (unsigned)phantom;
+  }
   a.total_iters = total_iters;
   // largest pixels per work item: 0 -> default (8192), 1..5 -> 512 ... 8192;
   // each level uses the largest power of two below it that still gives

@@ -30,6 +30,11 @@ int check_launch(const char *what);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// The test limits of the kernels' bounded grid-barrier waits set by
+// stb_set_wait_test_limits: polls before a wait gives up (0: the kernel's
+// default) and phantom arrivals (0: none).
+void wait_test_limits(unsigned *spin_limit, int *phantom);
+
 inline unsigned blocks_for(int64_t n, int threads) {
   return (unsigned)((n + threads - 1) / threads);
 }

@@ -27,6 +27,7 @@ HIST_GEOM_COUNT, HIST_FEAT_COUNT, HIST_OK, HIST_SIZE = 59, 60, 61, 64
 ST_NOT_PD, ST_NO_MATCHES, ST_NAN = 1, 2, 4
 # option bits or-ed into the channel_mode argument of the registration calls
 OPT_DW_SOLVE = 0x100
+OPT_MULTI_LAUNCH = 0x200
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -81,6 +82,7 @@ _SIGNATURES = {
         _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _i32,
         _i32, _vp, _i32, _f64, _f64, _f64, _f64, _f64, _i32, _vp, _vp, _vp]),
     "stb_profile_enable": (ctypes.c_int, [_i32]),
+    "stb_set_wait_test_limits": (ctypes.c_int, [ctypes.c_uint32, _i32]),
     "stb_profile_read": (ctypes.c_int, [ctypes.POINTER(_f64), ctypes.POINTER(_i64), _i32]),
     "stb_depth_to_points": (ctypes.c_int, [_vp, _f32, _f32, _vp, _vp, _vp, _i32, _i32, _vp]),
     "stb_erode_mask": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),
@@ -154,7 +156,7 @@ def stream_of(device):
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 
-PROFILE_KINDS = ("association", "reduction+solve", "information", "setup")
+PROFILE_KINDS = ("association", "reduction+solve", "information", "setup", "registration")
 
 
 def profile_enable(on):

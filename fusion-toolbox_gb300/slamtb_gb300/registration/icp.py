@@ -94,7 +94,11 @@ class ICPOdometry:
             exponential and the pose update in FP64, as the reference's
             float64 host solve) or "dw" (double-word float32, ~48 bits, on
             the FP32 pipes).
-        use_graph (bool): replay the launch sequence as a CUDA graph.
+        launch (str): "single" (default: one cooperative launch runs the
+            whole registration, phases separated by grid barriers) or
+            "multi" (two launches per iteration).
+        use_graph (bool): with launch="multi", replay the launch sequence
+            as a CUDA graph.
         record_history (bool): keep per-iteration records in
             ``self.last_history`` (float64 (num_iters, 64) CPU tensor, layout
             ``STB_HIST_*`` of ``include/slamtb_gb300.h``).
@@ -104,7 +108,7 @@ class ICPOdometry:
                  distance_threshold=.5, normals_angle_thresh=math.pi / 4,
                  feat_residual_thresh=2.75, feat_channel_mode="last",
                  use_graph=True, record_history=False, feat_layout="auto",
-                 solve_precision="fp64"):
+                 solve_precision="fp64", launch="single"):
         if so3:
             raise NotImplementedError(
                 "so3=True is not supported: the reference's rotation-only path "
@@ -118,6 +122,8 @@ class ICPOdometry:
             raise ValueError("feat_layout must be 'auto' or 'planar'")
         if solve_precision not in ("fp64", "dw"):
             raise ValueError("solve_precision must be 'fp64' or 'dw'")
+        if launch not in ("single", "multi"):
+            raise ValueError("launch must be 'single' or 'multi'")
         self.num_iters = num_iters
         self.geom_weight = geom_weight
         self.feat_weight = feat_weight
@@ -128,6 +134,7 @@ class ICPOdometry:
         self.feat_channel_mode = feat_channel_mode
         self.feat_layout = feat_layout
         self.solve_precision = solve_precision
+        self.launch_mode = launch
         self.use_graph = use_graph
         self.record_history = record_history
         self.last_history = None
@@ -231,7 +238,8 @@ class ICPOdometry:
                 float(self.distance_threshold), float(self.normals_angle_thresh),
                 float(self.feat_residual_thresh),
                 (0 if self.feat_channel_mode == "last" else 1)
-                | (N.OPT_DW_SOLVE if self.solve_precision == "dw" else 0),
+                | (N.OPT_DW_SOLVE if self.solve_precision == "dw" else 0)
+                | (N.OPT_MULTI_LAUNCH if self.launch_mode == "multi" else 0),
                 N.ptr(ws), ws.numel(), N.ptr(res), N.ptr(hist), int(self.use_graph),
                 N.stream_of(device)))
         del k, init  # kept alive through the call

@@ -77,6 +77,11 @@ extern "C" {
  * and pose composition.  No counterpart in the reference (its solve is
  * FP64 on the host, slamtb/registration/icp.py:236-251). */
 #define STB_OPT_DW_SOLVE 0x100
+/* stb_icp_estimate(_static): the kernel sequence of two launches per
+ * iteration (association, then reduction with the solve in its last block),
+ * replayable as a CUDA graph, instead of the default single cooperative
+ * launch that runs the whole registration with grid barriers. */
+#define STB_OPT_MULTI_LAUNCH 0x200
 
 /* ---- per-registration status bits (result block, STB_RES_STATUS) ------- */
 #define STB_ST_NOT_PD 1u     /* 6x6 J^T J was not positive definite: stopped */
@@ -218,9 +223,13 @@ STB_API size_t stb_icp_workspace_bytes(int64_t num_source, int32_t height,
  * The whole ICPOdometry.estimate loop (slamtb/registration/icp.py:152-262)
  * on the device, without host synchronisation:
  *   per iteration: association (shared by both terms), fused residual /
- *   Jacobian / normal-equation reduction (compensated float32), 6x6 FP64
- *   Cholesky solve, FP64 SE(3) exponential and left pose update; then the
- *   information matrix at the final pose.
+ *   Jacobian / normal-equation reduction (compensated float32), 6x6 LDL^T
+ *   solve, SE(3) exponential and left pose update in FP64 (double-word
+ *   float32 with STB_OPT_DW_SOLVE); then the information matrix at the
+ *   final pose.  By default one cooperative launch runs it all, its phases
+ *   separated by bounded grid barriers (a wait that runs out sets
+ *   STB_ST_TIMEOUT); STB_OPT_MULTI_LAUNCH selects two launches per
+ *   iteration instead.
  * Weighting follows the reference: J^T J = sum w_t^2 J_t^T J_t,
  * J^T r = w_g J_g^T r_g - w_f J_f^T r_f, residual = sum w_t r_t^2 divided by
  * the larger match count.  A non-positive-definite J^T J stops the loop
@@ -235,11 +244,12 @@ STB_API size_t stb_icp_workspace_bytes(int64_t num_source, int32_t height,
  * carried in the launch parameters (no copy, no synchronisation), so the
  * host buffers can be reused as soon as the call returns.
  * channel_mode: 0 = reference behaviour (last channel's J), 1 = sum over
- * channels.  result: float64 [STB_RES_SIZE] device block.  history: NULL or
+ * channels; or-ed with STB_OPT_* bits.  result: float64 [STB_RES_SIZE] device block.  history: NULL or
  * float64 [num_iters, STB_HIST_SIZE] per-iteration records.
  * num_iters <= 254.  workspace: stb_icp_workspace_bytes() bytes.
- * use_graph != 0 captures the launch sequence in a CUDA graph on first use
- * for this (workspace, sizes, options) and replays it afterwards.
+ * use_graph != 0 (with STB_OPT_MULTI_LAUNCH) captures the launch sequence
+ * in a CUDA graph on first use for this (workspace, sizes, options) and
+ * replays it afterwards; the single launch needs no graph.
  */
 STB_API int stb_icp_estimate(const float *kcam, const float *src_points,
                      const float *src_normals, const uint8_t *src_mask,
@@ -491,6 +501,19 @@ STB_API int stb_icp_estimate_static(
     double *result, double *history, void *stream);
 
 /*
+ * Test hook of the bounded waits of the single-launch registration and of
+ * stb_icp_estimate_batch (no counterpart in the reference): their grid
+ * barriers give up after spin_limit polls (0 restores the defaults) and
+ * expect phantom_arrivals more blocks than the grid has (0 restores the
+ * default).
+ * With phantom_arrivals > 0 no barrier can complete, so every wait runs out
+ * and the registration returns with STB_ST_TIMEOUT in its status instead of
+ * hanging: the way to test that failure path without a faulty GPU.
+ * Process-wide; applies to calls made after it.
+ */
+STB_API int stb_set_wait_test_limits(uint32_t spin_limit, int32_t phantom_arrivals);
+
+/*
  * Measurement hook (no counterpart in the reference, which has no device
  * timers).  stb_profile_enable(1) makes later stb_icp_estimate calls
  * bracket every kernel launch with CUDA events on the launching stream
@@ -498,7 +521,9 @@ STB_API int stb_icp_estimate_static(
  * for profiled and plain calls).  After the stream has completed,
  * stb_profile_read() returns, for the most recent profiled call, the summed
  * event time (ms) and launch count per kernel kind:
- *   0 association, 1 reduction + solve, 2 information, 3 setup.
+ *   0 association, 1 reduction + solve, 2 information, 3 setup (the
+ *   STB_OPT_MULTI_LAUNCH sequence), 4 the single-launch registration.
+ * num_kinds >= 4; kinds at or past num_kinds are not reported.
  */
 STB_API int stb_profile_enable(int32_t on);
 STB_API int stb_profile_read(double *ms_by_kind, int64_t *launches_by_kind,

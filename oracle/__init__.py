@@ -1,9 +1,11 @@
 """CPU oracle for the ICP registration hot path.
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product package imports this
-directory: only ``tests/``, ``__graft_entry__.smoke()`` and the
-``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` use it, and only
-as the checker (or as the timed CPU restatement of the reference's CPU path).
+directory: only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``
+use it, and only as the checker: the ``cpu_baseline`` / ``--impl
+reference`` legs time the C restatement of the reference's CPU path, and
+the accuracy report of the secondary workloads compares the GPU results,
+after their timed runs, with free-running FP64 oracle registrations.
 
 Contents
 --------
@@ -21,17 +23,18 @@ Contents
                  frames (the image has neither cv2 nor PIL).
 ``icp_port.c``   C/OpenMP restatement of the reference's CPU ICP path,
                  timed as the CPU baseline (``kind: "port"``).
+``build_ref``    builds the reference's own registration and frame-
+                 preparation sources (with ``ref_shim``, the project's
+                 Eigen subset, and ``ref_binding.cpp``) into ``_ref/`` where
+                 the reference tree is available.
 
 Parity status
 -------------
-The reference cannot be built or imported here (its native module needs
-Eigen, which is absent, and its Python side needs tenviz/cv2/kornia), so
-no reference-generated vectors exist.  The reference's own tests hold no
-golden vectors for ICP.  The oracle is pinned by the known answers that
-the reference's fixtures do hold: the ground-truth relative poses of the
-``test-data/rgbd/sample2`` frame pairs used by its ICP tests
-(``slamtb/registration/_test/test_icp.py:19-27``), checked in
-``tests/test_oracle_pins.py`` from fixtures extracted by
-``tests/golden/make_golden.py``.  Bit-level parity with the reference's own
-binaries is therefore unpinned; the pins are known-answer pins.
-"""
+The oracle is pinned to the reference's own code: ``tests/test_oracle_ref.py``
+runs the ``build_ref`` module (the reference's CPU path) on the oracle's
+inputs and requires equal bits for correspondence maps, per-point partials,
+match counts and the frame preparation; digests of the reference's outputs
+on its sample2 frames (``tests/golden/ref_vectors.npz``) pin the oracle and
+the GPU kernels where the reference tree is absent.  Not built: the
+reference's Python loop (weighting, solve, tenviz SE(3) exponential) and
+kornia's blur, which stay restatements.

@@ -37,9 +37,19 @@ def test_host_only_entry_points():
 # a status code and a "Check failed:" message (the reference's error prefix,
 # error.hpp) without touching memory.
 _CHECKED = sorted(n for n, (res, args) in _native._SIGNATURES.items()
-                  if res is ctypes.c_int and args and not n.startswith("stb_profile_"))
+                  if res is ctypes.c_int and args
+                  and not n.startswith(("stb_profile_", "stb_set_")))
 # A batch of zero twists is an empty operation, as for an empty torch tensor.
 _EMPTY_OK = {"stb_exp_rt_to_matrix", "stb_exp_rt_to_matrix_backward", "stb_matrix_to_exp_rt"}
+
+
+def test_wait_test_limits_setter():
+    """The test hook of the bounded waits refuses a negative count of phantom
+    arrivals and restores its defaults with (0, 0)."""
+    lib = _native.lib()
+    assert lib.stb_set_wait_test_limits(0, -1) == _native.STB_EINVAL
+    assert lib.stb_last_error().startswith(b"Check failed: ")
+    assert lib.stb_set_wait_test_limits(0, 0) == _native.STB_OK
 
 
 def _arguments(args, size):

@@ -47,7 +47,7 @@ def _oracle_map(d, pose, dist, angle):
                           t["normals"], t["mask"], d["kcam"], dist, angle)
 
 
-def _plain(cuda, d, iters, dist, angle, feats=None, wf=0.0, wg=1.0, init=None):
+def _plain(cuda, d, iters, dist, angle, feats=None, wf=0.0, wg=1.0, init=None, opts=0):
     """Registers d's pair for `iters` iterations through the C ABI and reads
     the correspondences of the final association back; returns (map, pose
     it was taken at)."""
@@ -73,7 +73,7 @@ def _plain(cuda, d, iters, dist, angle, feats=None, wf=0.0, wg=1.0, init=None):
     N.check(lib.stb_icp_estimate(
         N.ptr(kcam), N.ptr(sp), N.ptr(sn), N.ptr(sm), sp.size(0), N.ptr(sf), N.ptr(tp),
         N.ptr(tn), N.ptr(tm), h, w, N.ptr(tf), channels, code, N.ptr(init_t), iters, wg, wf,
-        dist, angle, 2.75, 0, N.ptr(ws), ws_bytes, N.ptr(res), None, 0, stream))
+        dist, angle, 2.75, opts, N.ptr(ws), ws_bytes, N.ptr(res), None, 0, stream))
     m = torch.empty(h, w, dtype=torch.int64, device=cuda)
     N.check(lib.stb_icp_correspondences(N.ptr(ws), h, w, iters, N.ptr(m), stream))
     r = res.cpu().numpy()
@@ -100,9 +100,14 @@ def pair0():
     return synthetic_pair(0, feature_channels=0)
 
 
+@pytest.mark.parametrize("launch", ["single", "multi"])
 @pytest.mark.parametrize("dist,angle", [(0.1, ANGLE_20), (0.5, math.pi / 4)])
-def test_fused_association_every_iteration(cuda, pair0, dist, angle):
-    _check_iterations(cuda, pair0, range(0, 11), dist, angle)
+def test_fused_association_every_iteration(cuda, pair0, dist, angle, launch):
+    """Both launch modes: the single cooperative launch (default) and the
+    two-launches-per-iteration sequence (STB_OPT_MULTI_LAUNCH)."""
+    from slamtb_gb300 import _native as N
+    _check_iterations(cuda, pair0, range(0, 11), dist, angle,
+                      opts=0 if launch == "single" else N.OPT_MULTI_LAUNCH)
 
 
 def test_fused_association_from_an_initial_pose(cuda, pair0):

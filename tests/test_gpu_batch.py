@@ -167,3 +167,27 @@ def test_bf16_sixteen_channel_four_level_batch(cuda, mode):
     for k, pair in enumerate(pairs):
         assert res[k].transform is not None
         _check_pair(br.last_history[k], pair, 1.0, iters=iters, channel_mode=mode, wg=10.0)
+
+
+def test_bounded_waits_give_up_with_a_timeout_status(cuda):
+    """With stb_set_wait_test_limits making every grid barrier expect one
+    block more than the cooperative grid has, no barrier completes: each
+    wait gives up after its poll limit, every pair's status gets
+    STB_ST_TIMEOUT and BatchRegistration.results raises.  Nothing hangs; the
+    next run (limits restored) succeeds."""
+    from slamtb_gb300 import _native as N
+    from slamtb_gb300.registration import BatchRegistration
+    pairs = [_pair(cuda, 53 + k, 160, 120, False) for k in range(2)]
+    br = BatchRegistration(_estimators(0.0))
+    srcs, tgts = [p["src"] for p in pairs], [p["tgt"] for p in pairs]
+    try:
+        N.check(N.lib().stb_set_wait_test_limits(1 << 10, 1))
+        _, _, plan = br.launch(srcs, tgts)
+        status = plan.results[:, N.RES_STATUS].cpu().numpy().astype(np.int64)
+        with pytest.raises(RuntimeError, match="stopped early"):
+            br.results(plan)
+    finally:
+        N.check(N.lib().stb_set_wait_test_limits(0, 0))
+    assert ((status & N.ST_TIMEOUT) != 0).all()
+    res = br.estimate_pyramids(srcs, tgts)
+    assert all(r.transform is not None for r in res)

@@ -91,12 +91,13 @@ def pair0():
     return synthetic_pair(0, feature_channels=0)
 
 
-@pytest.mark.parametrize("use_graph", [False, True])
-def test_geometric_matches_oracle_per_iteration(cuda, pair0, use_graph):
+@pytest.mark.parametrize("launch,use_graph", [("single", False), ("multi", False),
+                                               ("multi", True)])
+def test_geometric_matches_oracle_per_iteration(cuda, pair0, launch, use_graph):
     from slamtb_gb300.registration.icp import ICPOdometry
     x = _dev(pair0, cuda)
     x.pop("sf"), x.pop("tf")
-    icp = ICPOdometry(record_history=True, use_graph=use_graph, **GEOM)
+    icp = ICPOdometry(record_history=True, use_graph=use_graph, launch=launch, **GEOM)
     res = _run_gpu(x, icp)
     ores = _run_oracle(pair0, x, GEOM)
     assert len(ores.history) == 10
@@ -108,22 +109,24 @@ def test_geometric_matches_oracle_per_iteration(cuda, pair0, use_graph):
     assert res.information.dtype == torch.float32
 
 
-def test_hybrid_matches_oracle_per_iteration(cuda, pair0):
+@pytest.mark.parametrize("launch", ["single", "multi"])
+def test_hybrid_matches_oracle_per_iteration(cuda, pair0, launch):
     from slamtb_gb300.registration.icp import ICPOdometry
     kw = dict(GEOM, feat_weight=0.1)
     x = _dev(pair0, cuda)
-    icp = ICPOdometry(record_history=True, **kw)
+    icp = ICPOdometry(record_history=True, launch=launch, **kw)
     _run_gpu(x, icp)
     compare_forced(icp.last_history, pair0, x, kw)
 
 
+@pytest.mark.parametrize("launch", ["single", "multi"])
 @pytest.mark.parametrize("mode", ["last", "sum"])
-def test_bf16_multichannel_features(cuda, mode):
+def test_bf16_multichannel_features(cuda, mode, launch):
     from slamtb_gb300.registration.icp import ICPOdometry
     d = synthetic_pair(3, width=320, height=240, feature_channels=4)
     kw = dict(GEOM, num_iters=6, feat_weight=0.05)
     x = _dev(d, cuda, torch.bfloat16)
-    icp = ICPOdometry(record_history=True, feat_channel_mode=mode, **kw)
+    icp = ICPOdometry(record_history=True, feat_channel_mode=mode, launch=launch, **kw)
     _run_gpu(x, icp)
     compare_forced(icp.last_history, d, x, kw, channel_mode=mode)
 
@@ -146,7 +149,7 @@ def test_deterministic_and_graph_equals_direct(cuda, pair0):
     kw = dict(GEOM, feat_weight=0.1)
     outs = []
     for use_graph in (True, True, False):
-        icp = ICPOdometry(record_history=True, use_graph=use_graph, **kw)
+        icp = ICPOdometry(record_history=True, use_graph=use_graph, launch="multi", **kw)
         res = _run_gpu(x, icp)
         outs.append((res.transform.numpy().copy(), icp.last_history.numpy().copy()))
     for T, H in outs[1:]:

@@ -31,12 +31,13 @@ def _inputs(cuda, seed, width=640, height=480):
                 sf=dev(d["src_feats"]).view(1, -1), tf=dev(d["tgt_feats"]))
 
 
-def _args(x, iters):
+def _args(x, iters, opts=0):
     from slamtb_gb300 import _native as N
     h, w = x["tm"].shape
     return [N.ptr(x["kcam"]), N.ptr(x["sp"]), N.ptr(x["sn"]), N.ptr(x["sm"]), x["sp"].size(0),
             N.ptr(x["sf"]), N.ptr(x["tp"]), N.ptr(x["tn"]), N.ptr(x["tm"]), h, w,
-            N.ptr(x["tf"]), 1, N.STB_F32, None, iters, 1.0, 0.1, 0.1, math.radians(20), 2.75, 0]
+            N.ptr(x["tf"]), 1, N.STB_F32, None, iters, 1.0, 0.1, 0.1, math.radians(20), 2.75,
+            opts]
 
 
 def _check_equal(a_res, b_res, a_hist, b_hist):
@@ -51,10 +52,13 @@ def _check_equal(a_res, b_res, a_hist, b_hist):
     np.testing.assert_array_equal(ha, hb)
 
 
-@pytest.mark.parametrize("width,height", [(640, 480), (1024, 1024)])
-def test_static_entry_point_matches_workspace_entry_point(cuda, width, height):
+@pytest.mark.parametrize("width,height,launch", [(640, 480, "single"), (640, 480, "multi"),
+                                                 (1024, 1024, "single")])
+def test_static_entry_point_matches_workspace_entry_point(cuda, width, height, launch):
+    """Both launch modes (the default single launch and STB_OPT_MULTI_LAUNCH)."""
     from slamtb_gb300 import _native as N
     lib = N.lib()
+    opts = N.OPT_MULTI_LAUNCH if launch == "multi" else 0
     iters = 6
     stream = N.stream_of(cuda)
     ws_bytes = lib.stb_icp_workspace_bytes(width * height, height, width)
@@ -64,13 +68,13 @@ def test_static_entry_point_matches_workspace_entry_point(cuda, width, height):
         x = _inputs(cuda, seed, width, height)
         ref_res = torch.empty(N.RES_SIZE, dtype=torch.float64, device=cuda)
         ref_hist = torch.empty(iters, N.HIST_SIZE, dtype=torch.float64, device=cuda)
-        N.check(lib.stb_icp_estimate(*_args(x, iters), N.ptr(ws), ws_bytes, N.ptr(ref_res),
+        N.check(lib.stb_icp_estimate(*_args(x, iters, opts), N.ptr(ws), ws_bytes, N.ptr(ref_res),
                                      N.ptr(ref_hist), 0, stream))
         for _ in range(2):
             res = torch.full((N.RES_SIZE,), float("nan"), dtype=torch.float64, device=cuda)
             hist = torch.full((iters, N.HIST_SIZE), float("nan"), dtype=torch.float64,
                               device=cuda)
-            N.check(lib.stb_icp_estimate_static(*_args(x, iters), N.ptr(res), N.ptr(hist),
+            N.check(lib.stb_icp_estimate_static(*_args(x, iters, opts), N.ptr(res), N.ptr(hist),
                                                 stream))
             torch.cuda.synchronize(cuda)
             _check_equal(res, ref_res, hist, ref_hist)
