@@ -83,6 +83,7 @@ _SIGNATURES = {
         _i32, _vp, _i32, _f64, _f64, _f64, _f64, _f64, _i32, _vp, _vp, _vp]),
     "stb_profile_enable": (ctypes.c_int, [_i32]),
     "stb_set_wait_test_limits": (ctypes.c_int, [ctypes.c_uint32, _i32]),
+    "stb_verify_registrations": (ctypes.c_int, [_vp, _vp, _i32, _f64, _f64, _f64, _vp, _vp]),
     "stb_profile_read": (ctypes.c_int, [ctypes.POINTER(_f64), ctypes.POINTER(_i64), _i32]),
     "stb_depth_to_points": (ctypes.c_int, [_vp, _f32, _f32, _vp, _vp, _vp, _i32, _i32, _vp]),
     "stb_erode_mask": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),

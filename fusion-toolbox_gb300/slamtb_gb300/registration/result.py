@@ -59,6 +59,30 @@ class RegistrationVerifier:
             return False
         return True
 
+    def verify_batch(self, results, num_source):
+        """Verdicts for many registrations without leaving the device:
+        ``results`` a (B, 96) float64 CUDA tensor of result blocks (what
+        ``BatchRegistration.run`` or ``ICPOdometry.launch`` return),
+        ``num_source`` the B source point counts (a sequence or an int64
+        tensor).  Returns a (B,) bool CUDA tensor (``stb_verify_registrations``:
+        the tests of ``__call__`` on the blocks, the covariance test as an
+        FP64 positive-definiteness test of information - I / threshold)."""
+        from .. import _native as N
+        if results.device.type != "cuda" or results.dtype != torch.float64:
+            raise RuntimeError("Check failed: results must be a float64 CUDA tensor")
+        res = results.reshape(-1, N.RES_SIZE).contiguous()
+        dev = res.device
+        n = torch.as_tensor(num_source, dtype=torch.int64).to(dev).reshape(-1).contiguous()
+        if n.numel() != res.size(0):
+            raise RuntimeError("Check failed: one source count per result block")
+        out = torch.empty(res.size(0), dtype=torch.int32, device=dev)
+        with torch.cuda.device(dev):
+            N.check(N.lib().stb_verify_registrations(
+                N.ptr(res), N.ptr(n), res.size(0), float(self.match_ratio_threshold),
+                float(self.covariance_max_threshold), float(self.residual_threshhold),
+                N.ptr(out), N.stream_of(dev)))
+        return out.bool()
+
     def __str__(self):
         return (f"RegistrationVerifier with: match_ratio_threshold = "
                 f"{self.match_ratio_threshold} covariance_max_threshold = "

@@ -363,6 +363,25 @@ STB_API int stb_icp_batch_correspondences(const void *workspace, int32_t num_pai
                                           int64_t *merge_map, void *stream);
 
 /*
+ * RegistrationVerifier.__call__ (slamtb/registration/result.py:49-95) for
+ * num_results result blocks on the device: verdict[p] = 1 when
+ * residual <= residual_thresh, every eigenvalue of the inverse of the
+ * information matrix is <= covariance_max_thresh and matches /
+ * num_source[p] >= match_ratio_thresh, else 0.  results: float64
+ * [num_results][STB_RES_SIZE] (stb_icp_estimate / stb_icp_estimate_batch
+ * blocks); num_source: int64 [num_results]; verdict: int32 [num_results];
+ * all device arrays.  The covariance test is an FP64 LDL^T of
+ * information - I / covariance_max_thresh (positive definite exactly when
+ * every eigenvalue of the information matrix exceeds 1 / threshold); it
+ * assumes a positive semi-definite information matrix, which G^T G sums
+ * are, and rejects an eigenvalue exactly at the threshold.
+ */
+STB_API int stb_verify_registrations(const double *results, const int64_t *num_source,
+                                     int32_t num_results, double match_ratio_thresh,
+                                     double covariance_max_thresh, double residual_thresh,
+                                     int32_t *verdict, void *stream);
+
+/*
  * Processing::BilateralDepthFilter (src/bilateral_depth_filter.cu:15-110):
  * out[r][c] = 0 where mask[r][c] is 0, else the average of the masked
  * neighbours' depth within filter_width / 2 pixels, weighted by

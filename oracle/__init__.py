@@ -38,3 +38,4 @@ on its sample2 frames (``tests/golden/ref_vectors.npz``) pin the oracle and
 the GPU kernels where the reference tree is absent.  Not built: the
 reference's Python loop (weighting, solve, tenviz SE(3) exponential) and
 kornia's blur, which stay restatements.
+"""

@@ -1,5 +1,5 @@
 """Host-side logic of the package that needs no GPU: the rigid transform and
-Huber loss of AutogradICP's closure, the small host inputs handed to the C
+Huber loss of AutogradICP's cost, the small host inputs handed to the C
 entry by value, the unpacking of the FP64 result block, BatchRegistration's
 level table and argument checks, MultiscaleRegistration's level loop, and
 ICPOdometry's defaults and refusals."""
@@ -33,12 +33,15 @@ def test_rigid_transform_points_and_normals():
 def test_huber_loss_matches_the_reference_formula():
     """autogradicp.py:60-90: mean of the residuals below alpha plus the mean
     of alpha |r| - alpha over the rest (either part may be empty)."""
-    from slamtb_gb300.registration.autogradicp import _HuberLoss
-    h = _HuberLoss(2.0)
+    from slamtb_gb300.registration.autogradicp import robust_feature_cost
     r = torch.tensor([0.5, 1.0, 3.0, 5.0])
-    assert float(h(r)) == pytest.approx(0.75 + ((2 * 3 - 2) + (2 * 5 - 2)) / 2)
-    assert float(h(torch.tensor([0.1, 0.3]))) == pytest.approx(0.2)
-    assert h(torch.tensor([])) == 0
+    assert float(robust_feature_cost(r, 2.0)) == pytest.approx(
+        0.75 + ((2 * 3 - 2) + (2 * 5 - 2)) / 2)
+    assert float(robust_feature_cost(torch.tensor([0.1, 0.3]), 2.0)) == pytest.approx(0.2)
+    assert float(robust_feature_cost(torch.tensor([3.0, 5.0]), 2.0)) == pytest.approx(6.0)
+    assert robust_feature_cost(torch.tensor([]), 2.0) == 0
+    # alpha <= 0: the plain mean (autogradicp.py:183-186)
+    assert float(robust_feature_cost(r, 0.0)) == pytest.approx(float(r.mean()))
 
 
 def test_small_host_inputs_are_passed_by_value():
