@@ -37,8 +37,9 @@ struct State {
   unsigned stopped;
   unsigned status;
   int iters_done;
-  // grid barrier of the persistent kernel: arrivals, generation, error
-  unsigned bar_count, bar_gen, bar_err;
+  // grid barrier of the persistent kernel: arrivals (only grow during a
+  // call) and error
+  unsigned bar_count, bar_err;
 };
 static_assert(sizeof(State) <= 1024, "the workspace's State slot is 1024 bytes");
 

@@ -385,17 +385,18 @@ __device__ inline bool warp_gn_update_dw(const float2 *up, const float2 *bv, con
 // three exponential coefficients at once on three lane groups.
 // ---------------------------------------------------------------------------
 
-// 1 / d for d > 0: rcp.approx.ftz.f64 (relative error below 2^-22) and two
-// Newton-Raphson steps y <- y + y (1 - d y), each of which squares the
-// relative error (2^-44, then below the FP64 rounding): within an ulp or
-// two of the correctly rounded reciprocal.  A subnormal d flushes to an
-// infinite reciprocal, which turns the solution into NaN (flagged by the
-// caller).
+// 1 / d for d > 0: rcp.approx.ftz.f64 (relative error below 2^-22) and one
+// third-order correction: with e = 1 - d y, y (1 + e + e^2) = (1 - e^3) / d,
+// a relative error below 2^-66 before the last rounding, so the result is
+// within an ulp of the correctly rounded reciprocal.  Three FP64
+// instructions (two Newton-Raphson steps take four).  A subnormal d flushes
+// to an infinite reciprocal, which turns the solution into NaN (flagged by
+// the caller).
 __device__ __forceinline__ double rcp_fp64(double d) {
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
-  y = fma(y, fma(-d, y, 1.0), y);
-  return fma(y, fma(-d, y, 1.0), y);
+  const double e = fma(-d, y, 1.0);
+  return fma(y, fma(e, e, e), y);
 }
 
 // d > 0 on the integer bits (false for +-0, negatives and NaN; +inf passes,
@@ -479,14 +480,26 @@ __device__ inline bool warp_gn_update(const double *up, const double *bv, const 
       if (is_rhs && ei < j) v = nv;
     }
   }
-  // exp(x).  Below t = 0.5 the coefficients are their Maclaurin series in
-  // t^2 through t^14 (the first omitted term is below 0.5^16 / 17! < 5e-20
-  // of the sum), A on lanes 0..9, B on 10..19, C on 20..31, by Estrin's
-  // scheme; above, the closed forms of se3_coeffs.
+  // exp(x).  The coefficients A on lanes 0..9, B on 10..19, C on 20..31, by
+  // Estrin's scheme, from their Maclaurin series in t^2: below t^2 = 2^-14
+  // (a rotation update under 0.45 degrees, the usual case after the first
+  // iterations) through t^6, the first omitted term being below
+  // 2^-56 / 9! < 4e-23 of the sum; below t = 0.5 through t^14 (the first
+  // omitted term below 0.5^16 / 17! < 5e-20); above, the closed forms of
+  // se3_coeffs.
   const double wx = xs[3], wy = xs[4], wz = xs[5];
   const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
   double A, B, C;
-  if (t2 < 0.25) {
+  if (t2 < 0x1p-14) {
+    const int which = lane < 10 ? 0 : (lane < 20 ? 1 : 2);
+    const double u2 = t2 * t2;
+    const double a01 = fma(se3_series_coeff<1>(which), t2, se3_series_coeff<0>(which));
+    const double a23 = fma(se3_series_coeff<3>(which), t2, se3_series_coeff<2>(which));
+    const double coef = fma(u2, a23, a01);
+    A = __shfl_sync(full, coef, 0);
+    B = __shfl_sync(full, coef, 10);
+    C = __shfl_sync(full, coef, 20);
+  } else if (t2 < 0.25) {
     const int which = lane < 10 ? 0 : (lane < 20 ? 1 : 2);
     const double u2 = t2 * t2, u4 = u2 * u2;
     const double a01 = fma(se3_series_coeff<1>(which), t2, se3_series_coeff<0>(which));

@@ -31,8 +31,9 @@
 // serial fold-then-solve tail's release: 2 barriers per iteration.
 //
 // Every barrier wait is bounded (Job::spin_limit polls); a wait that gives
-// up sets the error word, every block leaves at its next barrier, and block
-// 0 writes STB_ST_TIMEOUT into the result status.
+// up sets the error word, every block leaves at its next barrier (waiting
+// blocks notice the word within 64 polls), and block 0 writes
+// STB_ST_TIMEOUT into the result status.
 #include <math.h>
 #include <stddef.h>
 
@@ -66,42 +67,51 @@ struct LoopShared {
   int ok;                // verdict of the last solve
 };
 
-// ld.acquire at GPU scope: the barrier's generation word.
+// Loads and atomics of the grid barrier's words at GPU scope.
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_add_release(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
-// Grid barrier with a bounded wait.  All blocks' writes before the barrier
-// (key-map atomics, slot stores) are visible to all blocks after it.
+// Grid barrier number `k` of this launch (counted by every block alike),
+// with a bounded wait.  The arrival counter only grows: barrier k is
+// complete when it reaches (k + 1) x the expected arrivals, so an arrival is
+// one release-add and a wait polls one word (no generation word to read
+// first, no reset).  The release orders the block's writes before the
+// barrier (key-map atomics, slot stores; made block-wide by the preceding
+// __syncthreads), the acquiring poll orders the reads after it.
 // `wait` false: arrive and return at once (the block has no work after the
 // barrier).  Returns false when a wait gave up (here or in another block).
-__device__ __forceinline__ bool grid_barrier(State *S, const Job &J, bool wait) {
+__device__ __forceinline__ bool grid_barrier(State *S, const Job &J, unsigned k, bool wait) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned expected = gridDim.x + (unsigned)J.bar_phantom;
-    const unsigned gen = ld_acquire(&S->bar_gen);
-    __threadfence();
+    const unsigned target = (k + 1) * (gridDim.x + (unsigned)J.bar_phantom);
+    red_add_release(&S->bar_count, 1u);
     bool ok = true;
-    if (atomicAdd(&S->bar_count, 1u) == expected - 1) {
-      S->bar_count = 0;
-      __threadfence();
-      atomicAdd(&S->bar_gen, 1u);
-    } else if (wait) {
+    if (wait) {
       unsigned spins = 0;
-      while (ld_acquire(&S->bar_gen) == gen) {
-        if (ld_acquire(&S->bar_err)) break;
+      while (ld_acquire(&S->bar_count) < target) {
         if (++spins > J.spin_limit) {
           atomicOr(&S->bar_err, 1u);
+          ok = false;
+          break;
+        }
+        // another block's wait gave up: checked every 64 polls
+        if ((spins & 63u) == 0 && ld_relaxed(&S->bar_err)) {
+          ok = false;
           break;
         }
       }
-    }
-    if (wait) {
-      __threadfence();
-      ok = ld_acquire(&S->bar_err) == 0;
     }
     s_ok = ok;
   }
@@ -135,16 +145,31 @@ __device__ __forceinline__ void associate(const Job &J, const Pose32 &P, long lo
   const uint8_t *__restrict__ tm = J.tm;
   unsigned long long *__restrict__ keys = J.keys;
   for (long long base = s0 + threadIdx.x; base < s1; base += (long long)kPT * kPR) {
+    // the source mask, point and normal of every point of the round in one
+    // batch of loads (none depends on another), then the projected target
+    // pixels' in a second: two dependent memory round trips before the
+    // atomic
+    uint8_t msk[kPR];
+    float sxyz[kPR][3], snrm[kPR][3];
+#pragma unroll
+    for (int k = 0; k < kPR; ++k) {
+      const long long i = base + (long long)k * kPT;
+      const long long ic = i < s1 ? i : s0;
+      msk[k] = __ldg(sm + ic);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        sxyz[k][d] = __ldg(sp + 3 * ic + d);
+        snrm[k][d] = __ldg(sn + 3 * ic + d);
+      }
+    }
     float3 Tp[kPR];
     long long pix[kPR];
     bool ok[kPR];
 #pragma unroll
     for (int k = 0; k < kPR; ++k) {
       const long long i = base + (long long)k * kPT;
-      ok[k] = i < s1 && sm[i < s1 ? i : s0];
-      const long long ii = ok[k] ? i : s0;
-      Tp[k] = transform_point(P.rt, __ldg(sp + 3 * ii), __ldg(sp + 3 * ii + 1),
-                              __ldg(sp + 3 * ii + 2));
+      ok[k] = i < s1 && msk[k];
+      Tp[k] = transform_point(P.rt, sxyz[k][0], sxyz[k][1], sxyz[k][2]);
       float u, v;
       project(P, Tp[k], u, v);
       int ui = 0, vi = 0;
@@ -170,8 +195,7 @@ __device__ __forceinline__ void associate(const Job &J, const Pose32 &P, long lo
                   dz = fsub(q[k][2], Tp[k].z);
       const float sq = dot3(dx, dy, dz, dx, dy, dz);
       if (sq > J.thr2) continue;
-      const float3 Tn =
-          transform_normal(P.nm, __ldg(sn + 3 * i), __ldg(sn + 3 * i + 1), __ldg(sn + 3 * i + 2));
+      const float3 Tn = transform_normal(P.nm, snrm[k][0], snrm[k][1], snrm[k][2]);
       const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, m[k][0], m[k][1], m[k][2]),
                            fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
                                 __fsqrt_rn(dot3(m[k][0], m[k][1], m[k][2], m[k][0], m[k][1],
@@ -269,6 +293,13 @@ __device__ __forceinline__ void info_pixels(const Job &J, long long p0, long lon
   }
 }
 
+// isfinite on the exponent bits (integer instructions: on this part every
+// FP64 instruction, comparisons included, costs the FP64 pipe's ~64 cycles
+// per warp).
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
 // The Gauss-Newton step of every block from the totals in L (FP64 or
 // double-word solve); block 0 records the iteration.  Warp 0 only.
 __device__ void persist_step(const Job &J, LoopShared &L, int iter, int lane) {
@@ -286,15 +317,14 @@ __device__ void persist_step(const Job &J, LoopShared &L, int iter, int lane) {
       L.Td[lane] = (double)tn.x + (double)tn.y;
     }
   } else {
+    // (the double-word pose Tw is not kept up to date: only the
+    // double-word solve reads it)
     double xs[6];
     double tn;
     ok = warp_gn_update(L.tot, L.tot + kJr, L.Td, xs, tn, lane);
-    for (int k = 0; k < 6; ++k) finite &= isfinite(xs[k]);
+    for (int k = 0; k < 6; ++k) finite &= finite_bits(xs[k]);
     __syncwarp();
-    if (ok && lane < 16) {
-      L.Td[lane] = tn;
-      L.Tw[lane] = dw_of_double(tn);
-    }
+    if (ok && lane < 16) L.Td[lane] = tn;
   }
   __syncwarp();
   if (ok) {
@@ -302,7 +332,9 @@ __device__ void persist_step(const Job &J, LoopShared &L, int iter, int lane) {
     refresh_view(L, dw, lane);
   }
   const double cg = L.tot[kCountGeom], cf = L.tot[kCountFeat];
-  const bool no_match = (J.use_geom ? fmax(cg, cf) : cf) == 0.0;
+  // the counts are sums of ones (never -0): zero exactly when all bits are
+  const bool no_match = (__double_as_longlong(cf) |
+                         (J.use_geom ? __double_as_longlong(cg) : 0ll)) == 0ll;
   if (lane == 0) {
     unsigned st = L.status;
     if (!ok)
@@ -339,7 +371,9 @@ __device__ __forceinline__ void fold_slots(const Job &J, LoopShared &L) {
   __shared__ float2 wsum[kPW][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   CSum t = {0.f, 0.f};
-  constexpr int kLoads = 4;
+  // slots per warp in one round of loads: a grid of up to 192 blocks is
+  // folded with every load in flight at once
+  constexpr int kLoads = 12;
   for (int b0 = warp; b0 < (int)gridDim.x; b0 += kPW * kLoads) {
     float2 v[kLoads];
 #pragma unroll
@@ -380,7 +414,6 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
   float(*red)[kPT] = reinterpret_cast<float(*)[kPT]>(s_red_p);
   State *S = J.state;
   const int lane = threadIdx.x & 31;
-  const bool dw = J.solve_dw;
   const long long n = J.n, npix = (long long)J.H * J.W;
   const long long G = gridDim.x, b = blockIdx.x;
   const long long sc = (n + G - 1) / G, pc = (npix + G - 1) / G;
@@ -415,17 +448,18 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
     if (lane == 0) inverse_transpose(L.rt32, L.P.nm);
   }
   for (long long pix = p0 + threadIdx.x; pix < p1; pix += kPT) J.keys[pix] = ~0ull;
-  bool alive = grid_barrier(S, J, true);
+  unsigned nbar = 0;  // grid barriers passed
+  bool alive = grid_barrier(S, J, nbar++, true);
 
   for (int iter = 0; alive && iter < J.iters; ++iter) {
     associate(J, L.P, s0, s1, iter);
-    if (!(alive = grid_barrier(S, J, true))) break;
+    if (!(alive = grid_barrier(S, J, nbar++, true))) break;
     float acc[kAccs];
 #pragma unroll
     for (int a = 0; a < kAccs; ++a) acc[a] = 0.f;
     reduce_pixels<FT, kGeom, kFeat, kHWC>(J, L.P, p0, p1, iter, acc);
     write_slot<kAccs>(J, acc, red);
-    if (!(alive = grid_barrier(S, J, true))) break;
+    if (!(alive = grid_barrier(S, J, nbar++, true))) break;
     fold_slots<kAccs>(J, L);
     if (threadIdx.x < 32) persist_step(J, L, iter, lane);
     __syncthreads();
@@ -435,7 +469,7 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
   // the association at the final pose and the information sum
   if (alive) {
     associate(J, L.P, s0, s1, J.iters);
-    alive = grid_barrier(S, J, true);
+    alive = grid_barrier(S, J, nbar++, true);
   }
   if (alive) {
     float acc[kInfoAccs];
@@ -443,7 +477,7 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
     for (int a = 0; a < kInfoAccs; ++a) acc[a] = 0.f;
     info_pixels(J, p0, p1, J.iters, acc);
     write_slot<kInfoAccs>(J, acc, red);
-    alive = grid_barrier(S, J, blockIdx.x == 0);
+    alive = grid_barrier(S, J, nbar++, blockIdx.x == 0);
   }
   if (blockIdx.x != 0) return;
   double *R = J.result;
@@ -573,7 +607,7 @@ int launch_persistent(const Plan &p, Job job, cudaStream_t st) {
 int reset_persistent(const Job &job, cudaStream_t st) {
   // the barrier words start at zero for every call
   if (cudaMemsetAsync(reinterpret_cast<char *>(job.state) + offsetof(State, bar_count), 0,
-                      3 * sizeof(unsigned), st) != cudaSuccess)
+                      2 * sizeof(unsigned), st) != cudaSuccess)
     return check_launch("cudaMemsetAsync");
   return STB_OK;
 }
