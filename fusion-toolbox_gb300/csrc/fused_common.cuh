@@ -62,7 +62,8 @@ struct Job {
   float thr2, cos_max, feat_thr2;
   double *result, *history;
   unsigned long long *keys;
-  float2 *part;  // per block: kSlotAccs (sum, compensation) pairs
+  float2 *part;  // per block: kSlotAccs (sum, compensation) pairs; two
+                 // such buffers (the persistent kernel alternates them)
   int nblocks;
   State *state;
   // intrinsics (fx, cx, fy, cy) and initial pose given as host values
@@ -75,6 +76,8 @@ struct Job {
   // that the waits run out)
   unsigned spin_limit;
   int bar_phantom;
+  // rounds of source points the persistent kernel keeps in shared memory
+  int src_cache_rounds;
 };
 static_assert(sizeof(Job) <= 1024, "the workspace's Job slot is 1024 bytes");
 
@@ -110,10 +113,10 @@ constexpr int reduce_blocks(int64_t pixels, int threads = kReduceThreads) {
 
 constexpr int kSlotAccs = 32;  // accumulator pairs per block slot (>= kAccs)
 
-// Workspace: [Job slot][State slot][block slots: nblocks x kSlotAccs float2]
-// [keys H*W]
+// Workspace: [Job slot][State slot][block slots: 2 x nblocks x kSlotAccs
+// float2][keys H*W]
 constexpr size_t keys_offset(int64_t pixels) {
-  return 2 * kSlot + align256(sizeof(float2) * kSlotAccs * reduce_blocks(pixels));
+  return 2 * kSlot + align256(2 * sizeof(float2) * kSlotAccs * reduce_blocks(pixels));
 }
 constexpr size_t workspace_bytes(int64_t pixels) {
   return keys_offset(pixels) + align256(sizeof(unsigned long long) * pixels);

@@ -962,7 +962,7 @@ extern "C" int stb_profile_read(double *ms_by_kind, int64_t *launches_by_kind,
 // forbid later allocations (cudaMalloc and cudaFree synchronise the device,
 // which stalls a real-time tracking loop sharing the GPU).
 //
-// The scratch is kStaticMaxPixels target pixels' worth (about 8.6 MB) in
+// The scratch is kStaticMaxPixels target pixels' worth (about 8.9 MB) in
 // g_static_workspace, which every GPU that loads this library holds until
 // the process exits.  The first call on a device looks up the array's device
 // address with cudaGetSymbolAddress (host code cannot use the symbol itself:

@@ -57,6 +57,26 @@ __device__ __forceinline__ void inverse_transpose(const float *A, float *r) {
 #undef E
 }
 
+// Entry e < 9 of inverse_transpose's result, computed by one lane: the
+// same operations in the same order as the serial function (entry (i, j) is
+// the (i, j) cofactor, from the rows and columns other than i and j in
+// increasing order, times 1 / det), so the nine lanes of a warp produce
+// its result bit for bit in parallel.
+__device__ __forceinline__ float inverse_transpose_entry(const float *A, int e) {
+#define E(i, j) A[(i)*4 + (j)]
+  const float det =
+      fadd(fsub(fmul(E(0, 0), fsub(fmul(E(1, 1), E(2, 2)), fmul(E(2, 1), E(1, 2)))),
+                fmul(E(0, 1), fsub(fmul(E(1, 0), E(2, 2)), fmul(E(1, 2), E(2, 0))))),
+           fmul(E(0, 2), fsub(fmul(E(1, 0), E(2, 1)), fmul(E(1, 1), E(2, 0)))));
+  const float inv = fdiv(1.0f, det);
+  const int i = e / 3, j = e % 3;
+  const int a = i == 0 ? 1 : 0, b = i == 2 ? 1 : 2;
+  const int c = j == 0 ? 1 : 0, d = j == 2 ? 1 : 2;
+  const float m = fsub(fmul(E(a, c), E(b, d)), fmul(E(a, d), E(b, c)));
+#undef E
+  return fmul(((i + j) & 1) ? -m : m, inv);
+}
+
 // RigidTransform::Transform (camera.hpp:134-145).
 __device__ __forceinline__ float3 transform_point(const float *rt, float x,
                                                   float y, float z) {

@@ -498,7 +498,7 @@ STB_API int stb_icp_loss_backward(const float *src_depth, const float *src_norma
  * their device-memory budget at start-up (cudaMalloc / cudaFree synchronise
  * the device and would stall a real-time loop).  The scratch is a fixed
  * device array inside the library, sized for at most 1,048,576 target
- * pixels (height * width; about 8.6 MB, held by every GPU that loads the
+ * pixels (height * width; about 8.9 MB, held by every GPU that loads the
  * library until the process exits); larger frames are rejected with
  * STB_EINVAL.  The first call on a device looks up that array's address
  * (cudaGetSymbolAddress), so make it before any stream capture.  The
