@@ -26,6 +26,7 @@
 
 #include "feature_term.cuh"
 #include "gn_solve.cuh"
+#include "group_launch.hpp"
 #include "keymap.cuh"
 #include "stb_common.cuh"
 #include "stb_host.hpp"
@@ -90,7 +91,7 @@ __host__ __device__ inline size_t al256(size_t x) { return (x + 255) & ~size_t(2
 
 struct Layout {
   size_t sync, level_tile, ps, key_off, src_off, tgt_off, grp_off, grp_ticket, pair_ticket, tile_part,
-      grp_part, keys, total;
+      grp_part, order, gpart, keys, total;
   long long tiles_cap, groups_cap;
 };
 
@@ -121,6 +122,11 @@ inline Layout layout(int B, long long total_pixels) {
   o += al256(sizeof(float) * kSlotFloats * (size_t)l.tiles_cap);
   l.grp_part = o;
   o += al256(sizeof(float) * kSlotFloats * (size_t)l.groups_cap);
+  // the grouped kernel: its pair queue and its groups' slot buffers
+  l.order = o;
+  o += al256(sizeof(int) * (size_t)B);
+  l.gpart = o;
+  o += al256(sizeof(float2) * 2 * 32 * (size_t)fused::kGroupMaxBlocks);
   l.keys = o;
   // one key per pixel of each pair's largest level, each pair's map rounded
   // up to an even count so that it starts on a 16-byte boundary (bulk copies)
@@ -1198,9 +1204,10 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
     if (feat_dtype < STB_F32 || feat_dtype > STB_BF16_HWC)
       return fail(STB_EDTYPE, "Check failed: feature maps must be float32 or bfloat16");
   }
-  if ((channel_mode & ~(0xff | STB_OPT_DW_SOLVE)) != 0)
+  if ((channel_mode & ~(0xff | STB_OPT_DW_SOLVE | STB_OPT_GROUPS)) != 0)
     return fail(STB_EINVAL, "Check failed: unknown option bits 0x%x in channel_mode",
-                (unsigned)channel_mode & ~(0xffu | STB_OPT_DW_SOLVE));
+                (unsigned)channel_mode & ~(0xffu | STB_OPT_DW_SOLVE | STB_OPT_GROUPS));
+  const bool grouped = (channel_mode & STB_OPT_GROUPS) != 0;
   if ((channel_mode & 0xff) != 0 && (channel_mode & 0xff) != 1)
     return fail(STB_EINVAL, "Check failed: channel_mode must be 0 or 1");
   const Layout lay = layout(num_pairs, total_target_pixels);
@@ -1209,8 +1216,11 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
                 lay.total);
   if (((uintptr_t)workspace & 255) != 0)
     return fail(STB_EINVAL, "Check failed: workspace must be 256-byte aligned");
-  if (tile_config < 0 || tile_config > 5)
+  if (!grouped && (tile_config < 0 || tile_config > 5))
     return fail(STB_EINVAL, "Check failed: tile_config must be in [0, 5]");
+  if (grouped && (tile_config < 1 || tile_config > fused::kMaxGroups))
+    return fail(STB_EINVAL, "Check failed: with STB_OPT_GROUPS, tile_config (the number of "
+                "groups) must be in [1, %d], got %d", fused::kMaxGroups, tile_config);
   STB_TRY(check_device_ptr(levels, "levels"));
   STB_TRY(check_device_ptr(init_transforms, "init_transforms", true));
   STB_TRY(check_device_ptr(workspace, "workspace"));
@@ -1280,6 +1290,35 @@ extern "C" int stb_icp_estimate_batch(const stb_level *levels, int32_t num_pairs
   // barrier counters start at zero for every launch
   if (cudaMemsetAsync(a.sync, 0, kSyncBytes, st) != cudaSuccess)
     return check_launch("cudaMemsetAsync");
+  if (grouped) {
+    fused::GroupLaunch g;
+    g.levels = levels;
+    g.B = a.B;
+    g.L = a.L;
+    g.C = a.C;
+    g.dtype = a.dtype;
+    g.mode = a.mode;
+    g.total_iters = a.total_iters;
+    g.solve_dw = a.solve_dw;
+    for (int l = 0; l < fused::kGroupMaxLevels; ++l) {
+      const LevelP &q = a.lp[l];
+      g.lp[l] = fused::GroupLevelParams{q.iters, q.use_geom, q.use_feat, q.wg1, q.wg2, q.wf1,
+                                        q.wf2, q.thr2, q.cos_max, q.feat_thr2};
+    }
+    g.init = a.init;
+    g.results = a.results;
+    g.history = a.history;
+    g.spin_limit = a.spin_limit;
+    g.bar_phantom = (int)a.bar_phantom;
+    g.sync = a.sync;
+    g.key_off = a.key_off;
+    g.order = reinterpret_cast<int *>(ws + lay.order);
+    g.part = reinterpret_cast<float2 *>(ws + lay.gpart);
+    g.keys = a.keys;
+    g.keys_cap = a.keys_cap;
+    g.groups = tile_config;
+    return fused::launch_grouped(g, st);
+  }
   if (!any_feat) return launch_batch<float, false, false>(a, st);
   switch (feat_dtype) {
     case STB_F32: return launch_batch<float, true, false>(a, st);

@@ -39,332 +39,20 @@
 
 #include <mutex>
 
-#include "feature_term.cuh"
-#include "fused_common.cuh"
-#include "gn_solve.cuh"
-#include "stb_common.cuh"
+#include "persist_phases.cuh"
 #include "stb_host.hpp"
 
 namespace stb {
 namespace fused {
+
+// The single-pair kernel's blocks are the grid; its barrier words are in
+// the workspace's State.
+__device__ __forceinline__ int rank_of(const Job &) { return blockIdx.x; }
+__device__ __forceinline__ int size_of(const Job &) { return gridDim.x; }
+__device__ __forceinline__ unsigned *bar_word(const Job &J) { return &J.state->bar_count; }
+__device__ __forceinline__ unsigned *err_word(const Job &J) { return &J.state->bar_err; }
+
 namespace {
-
-constexpr int kPT = 512;          // threads per block
-constexpr int kPW = kPT / 32;     // warps per block
-constexpr int kPR = 4;            // pixels per thread per round
-
-// Work ownership.  The source points (association) and the target pixels
-// (reduction, information) are cut into chunks of kChunk consecutive units;
-// block b of a grid of G blocks owns chunks b, b + G, b + 2G, ..., so every
-// block's share is spread over the whole frame and content that costs more
-// per unit (valid, matched pixels) is shared evenly (with contiguous ranges
-// the blocks over the middle of a frame finished their association about
-// 1.4 us after the others).  One round of a block covers kChunksPerRound of
-// its chunks: thread t takes unit t % kChunk of chunk slot
-// k (kPT / kChunk) + t / kChunk for k < kPR, so four warps read one chunk,
-// coalesced.
-constexpr int kChunk = 128;
-constexpr int kChunksPerRound = kPT * kPR / kChunk;
-static_assert(kPT % kChunk == 0, "a chunk is a whole number of warps");
-
-struct Share {
-  long long total;  // units in the frame
-  int rounds;       // rounds of this block
-};
-
-__device__ __forceinline__ Share share_of(long long total) {
-  const long long nch = (total + kChunk - 1) / kChunk, b = blockIdx.x, G = gridDim.x;
-  const long long mine = nch > b ? (nch - 1 - b) / G + 1 : 0;
-  return Share{total, (int)((mine + kChunksPerRound - 1) / kChunksPerRound)};
-}
-
-// Unit of this thread's k-th slot in round r (>= the total: no unit).
-__device__ __forceinline__ long long unit_of(int r, int k) {
-  const long long slot =
-      (long long)r * kChunksPerRound + k * (kPT / kChunk) + threadIdx.x / kChunk;
-  return (blockIdx.x + (long long)gridDim.x * slot) * kChunk + (threadIdx.x % kChunk);
-}
-
-// The block's source points of its first Job::src_cache_rounds rounds,
-// copied to shared memory at the start of the registration (they are the
-// same points in every association): the association then reads them
-// there instead of making a memory round trip before its target gathers.
-// Entry (r kPR + k) kPT + t holds the point of thread t's k-th slot in
-// round r; the floats are six arrays of cap entries (x, y, z, nx, ny, nz),
-// then cap mask bytes.
-constexpr int kMaxCacheRounds = 2;
-constexpr int kCachePointBytes = 6 * sizeof(float) + 1;
-
-struct SrcCache {
-  float *f;
-  uint8_t *m;
-  int cap, rounds;
-};
-
-__device__ __forceinline__ int cache_index(int r, int k) { return (r * kPR + k) * kPT + threadIdx.x; }
-
-// Per-block shared state of the loop.
-struct LoopShared {
-  Pose32 P;              // float32 pose view, normal matrix, intrinsics
-  double Td[16];         // pose (FP64 solve)
-  float2 Tw[16];         // pose (double-word solve)
-  double tot[32];        // totals of the current step, FP64
-  float2 totw[32];       // the same as double-words
-  double last_tot[32];   // totals of the last successful step
-  float rt32[12];
-  unsigned status;
-  int done;              // successful iterations
-  int ok;                // verdict of the last solve
-};
-
-// Loads and atomics of the grid barrier's words at GPU scope.
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ unsigned ld_relaxed(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void red_add_release(unsigned *p, unsigned v) {
-  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Grid barrier number `k` of this launch (counted by every block alike),
-// with a bounded wait.  The arrival counter only grows: barrier k is
-// complete when it reaches (k + 1) x the expected arrivals, so an arrival is
-// one release-add and a wait polls one word (no generation word to read
-// first, no reset).  The release orders the block's writes before the
-// barrier (key-map atomics, slot stores; made block-wide by the preceding
-// __syncthreads), the acquiring poll orders the reads after it.
-// `wait` false: arrive and return at once (the block has no work after the
-// barrier).  Returns false when a wait gave up (here or in another block).
-__device__ __forceinline__ bool grid_barrier(State *S, const Job &J, unsigned k, bool wait) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned target = (k + 1) * (gridDim.x + (unsigned)J.bar_phantom);
-    red_add_release(&S->bar_count, 1u);
-    bool ok = true;
-    if (wait) {
-      unsigned spins = 0;
-      while (ld_acquire(&S->bar_count) < target) {
-        if (++spins > J.spin_limit) {
-          atomicOr(&S->bar_err, 1u);
-          ok = false;
-          break;
-        }
-        // another block's wait gave up: checked every 64 polls
-        if ((spins & 63u) == 0 && ld_relaxed(&S->bar_err)) {
-          ok = false;
-          break;
-        }
-      }
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok;
-}
-
-// The float32 view of the pose in Td (or Tw) and its normal matrix, by
-// warp 0 (lanes 0..11 convert, lanes 0..8 form one entry each of the
-// normal matrix).
-__device__ __forceinline__ void refresh_view(LoopShared &L, bool dw, int lane) {
-  if (lane < 12) {
-    const float f = dw ? L.Tw[lane].x : __double2float_rn(L.Td[lane]);
-    L.rt32[lane] = f;
-    L.P.rt[lane] = f;
-  }
-  __syncwarp();
-  if (lane < 9) L.P.nm[lane] = inverse_transpose_entry(L.rt32, lane);
-  __syncwarp();
-}
-
-// Association of this block's share of the source points at epoch e.
-__device__ __forceinline__ void associate(const Job &J, const Pose32 &P, Share sh,
-                                          const SrcCache &C, int e) {
-  const unsigned long long tag = (unsigned long long)(254u - (unsigned)e) << 56;
-  const int H = J.H, W = J.W;
-  const float *__restrict__ sp = J.sp;
-  const float *__restrict__ sn = J.sn;
-  const float *__restrict__ tp = J.tp;
-  const float *__restrict__ tn = J.tn;
-  const uint8_t *__restrict__ sm = J.sm;
-  const uint8_t *__restrict__ tm = J.tm;
-  unsigned long long *__restrict__ keys = J.keys;
-  const long long n = sh.total;
-  for (int r = 0; r < sh.rounds; ++r) {
-    // the source mask, point and normal of every point of the round in one
-    // batch of loads (none depends on another), then the projected target
-    // pixels' in a second: two dependent memory round trips before the
-    // atomic
-    uint8_t msk[kPR];
-    float sxyz[kPR][3], snrm[kPR][3];
-    if (r < C.rounds) {
-#pragma unroll
-      for (int k = 0; k < kPR; ++k) {
-        const int c = cache_index(r, k);
-        msk[k] = C.m[c];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          sxyz[k][d] = C.f[d * C.cap + c];
-          snrm[k][d] = C.f[(3 + d) * C.cap + c];
-        }
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < kPR; ++k) {
-        const long long i = unit_of(r, k);
-        const long long ic = i < n ? i : 0;
-        msk[k] = __ldg(sm + ic);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          sxyz[k][d] = __ldg(sp + 3 * ic + d);
-          snrm[k][d] = __ldg(sn + 3 * ic + d);
-        }
-      }
-    }
-    float3 Tp[kPR];
-    long long pix[kPR];
-    bool ok[kPR];
-#pragma unroll
-    for (int k = 0; k < kPR; ++k) {
-      const long long i = unit_of(r, k);
-      ok[k] = i < n && msk[k];
-      Tp[k] = transform_point(P.rt, sxyz[k][0], sxyz[k][1], sxyz[k][2]);
-      float u, v;
-      project(P, Tp[k], u, v);
-      int ui = 0, vi = 0;
-      ok[k] = ok[k] && round_in(u, W, ui) && round_in(v, H, vi);
-      pix[k] = ok[k] ? (long long)vi * W + ui : 0;
-    }
-    float q[kPR][3], m[kPR][3];
-    bool valid[kPR];
-#pragma unroll
-    for (int k = 0; k < kPR; ++k) {
-      valid[k] = __ldg(tm + pix[k]);
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        q[k][d] = __ldg(tp + 3 * pix[k] + d);
-        m[k][d] = __ldg(tn + 3 * pix[k] + d);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kPR; ++k) {
-      if (!ok[k] || !valid[k]) continue;
-      const long long i = unit_of(r, k);
-      const float dx = fsub(q[k][0], Tp[k].x), dy = fsub(q[k][1], Tp[k].y),
-                  dz = fsub(q[k][2], Tp[k].z);
-      const float sq = dot3(dx, dy, dz, dx, dy, dz);
-      if (sq > J.thr2) continue;
-      const float3 Tn = transform_normal(P.nm, snrm[k][0], snrm[k][1], snrm[k][2]);
-      const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, m[k][0], m[k][1], m[k][2]),
-                           fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
-                                __fsqrt_rn(dot3(m[k][0], m[k][1], m[k][2], m[k][0], m[k][1],
-                                                m[k][2]))));
-      if (c >= -1.0f && c <= J.cos_max) continue;
-      atomicMin(keys + pix[k],
-                tag | ((unsigned long long)__float_as_uint(__fsqrt_rn(sq)) << 24) |
-                    (unsigned long long)i);
-    }
-  }
-}
-
-// Per-thread partials of the normal equations over this block's share of
-// the target pixels at epoch e.
-template <typename FT, bool kGeom, bool kFeat, bool kHWC>
-__device__ __forceinline__ void reduce_pixels(const Job &J, const Pose32 &P, Share sh, int e,
-                                              float *acc) {
-  const unsigned tag = 254u - (unsigned)e;
-  const int H = J.H, W = J.W;
-  const long long npix = (long long)H * W;
-  const unsigned long long *__restrict__ keys = J.keys;
-  const float *__restrict__ sp = J.sp;
-  const float *__restrict__ tp = J.tp;
-  const float *__restrict__ tn = J.tn;
-  for (int r = 0; r < sh.rounds; ++r) {
-    unsigned long long key[kPR];
-    float q[kPR][3], m[kPR][3];
-#pragma unroll
-    for (int k = 0; k < kPR; ++k) {
-      const long long pix = unit_of(r, k);
-      const long long pc = pix < npix ? pix : 0;
-      key[k] = pix < npix ? __ldcg(keys + pix) : 0ull;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        q[k][d] = kGeom ? __ldg(tp + 3 * pc + d) : 0.f;
-        m[k][d] = kGeom ? __ldg(tn + 3 * pc + d) : 0.f;
-      }
-    }
-    float s[kPR][3];
-#pragma unroll
-    for (int k = 0; k < kPR; ++k) {
-      const bool match = (unsigned)(key[k] >> 56) == tag;
-      const long long i = (long long)(key[k] & 0xffffffull);
-#pragma unroll
-      for (int d = 0; d < 3; ++d) s[k][d] = match ? __ldg(sp + 3 * i + d) : 0.f;
-    }
-#pragma unroll
-    for (int k = 0; k < kPR; ++k) {
-      if ((unsigned)(key[k] >> 56) != tag) continue;
-      const long long i = (long long)(key[k] & 0xffffffull);
-      const float3 Tp = transform_point(P.rt, s[k][0], s[k][1], s[k][2]);
-      if (kGeom) {
-        const float nx = m[k][0], ny = m[k][1], nz = m[k][2];
-        const float r = dot3(fsub(q[k][0], Tp.x), fsub(q[k][1], Tp.y), fsub(q[k][2], Tp.z), nx,
-                             ny, nz);
-        const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
-                             fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
-                             fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
-        accumulate_se3(acc, Jv, r, J.wg1, J.wg2);
-        acc[kR2] += J.wg1 * (r * r);
-        acc[kCountGeom] += 1.f;
-      }
-      if (kFeat) {
-        const FeatView<FT, kHWC> tf{static_cast<const FT *>(J.tf), npix, J.C};
-        const FeatView<FT, kHWC> sf{static_cast<const FT *>(J.sf), J.n, J.C};
-        float sq;
-        if (feature_term(tf, sf, i, P, Tp, H, W, J.feat_thr2, J.channel_mode, J.wf1, J.wf2, acc,
-                         sq)) {
-          acc[kR2] += J.wf1 * sq;
-          acc[kCountFeat] += 1.f;
-        }
-      }
-    }
-  }
-}
-
-// Information partials G^T G over this block's share of the target pixels
-// at epoch e.
-__device__ __forceinline__ void info_pixels(const Job &J, Share sh, int e, float *acc) {
-  const unsigned tag = 254u - (unsigned)e;
-  const unsigned long long *__restrict__ keys = J.keys;
-  const float *__restrict__ tp = J.tp;
-  for (int slot = 0; slot < sh.rounds * kPR; ++slot) {
-    const long long pix = unit_of(slot / kPR, slot % kPR);
-    if (pix >= sh.total || (unsigned)(__ldcg(keys + pix) >> 56) != tag) continue;
-    const float qx = __ldg(tp + 3 * pix), qy = __ldg(tp + 3 * pix + 1),
-                qz = __ldg(tp + 3 * pix + 2);
-    const float G0[6] = {0.f, qz, -qy, 1.f, 0.f, 0.f};
-    const float G1[6] = {-qz, 0.f, qx, 0.f, 1.f, 0.f};
-    const float G2[6] = {qy, -qx, 0.f, 0.f, 0.f, 1.f};
-#pragma unroll
-    for (int a = 0; a < 6; ++a)
-#pragma unroll
-      for (int b = a; b < 6; ++b)
-        acc[upper_index(a, b)] += G0[a] * G0[b] + G1[a] * G1[b] + G2[a] * G2[b];
-  }
-}
-
-// isfinite on the exponent bits (integer instructions: on this part every
-// FP64 instruction, comparisons included, costs the FP64 pipe's ~64 cycles
-// per warp).
-__device__ __forceinline__ bool finite_bits(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
-}
 
 // The Gauss-Newton step of every block from the totals in L (FP64 or
 // double-word solve); block 0 records the iteration.  Warp 0 only.
@@ -430,140 +118,22 @@ __device__ void persist_step(const Job &J, LoopShared &L, int iter, int lane) {
   }
 }
 
-// Slot words at GPU scope: relaxed stores by the writing block, relaxed
-// loads by the polling ones (every 32-bit word is written whole, so a load
-// sees either the poison or the new value of each word).
-__device__ __forceinline__ void st_relaxed_f2(float2 *p, float2 v) {
-  asm volatile("st.relaxed.gpu.global.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(v.x), "f"(v.y)
-               : "memory");
-}
-__device__ __forceinline__ float2 ld_relaxed_f2(const float2 *p) {
-  float2 v;
-  asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p)
-               : "memory");
-  return v;
-}
-
-// The slots of the Gauss-Newton sums are double-buffered by iteration
-// parity and carry their own completion: a slot word holds kPoison until
-// its block writes the iteration's value, so the blocks fold the slots as
-// they arrive instead of waiting at a grid barrier first (one L2 round trip
-// less per iteration).  kPoison is a NaN payload that arithmetic never
-// produces (the GPU's arithmetic returns the canonical NaN 0x7fffffff), so
-// no sum can be mistaken for it.  A buffer is poisoned again by its blocks
-// in the next iteration, after the association barrier: by then every
-// block has folded it, and that barrier orders the poison before any
-// block's reads of the buffer's next use.
-constexpr unsigned kPoison = 0x7fbadbadu;
-
-__device__ __forceinline__ float2 *slot_of(const Job &J, int buf, int block) {
-  return J.part + ((size_t)buf * gridDim.x + block) * kSlotAccs;
-}
-
-__device__ __forceinline__ void poison_slot(const Job &J, int buf) {
-  if (threadIdx.x < kSlotAccs)
-    st_relaxed_f2(slot_of(J, buf, blockIdx.x) + threadIdx.x,
-                  make_float2(__uint_as_float(kPoison), __uint_as_float(kPoison)));
-}
-
-// Totals of kN accumulators over the grid's slots of buffer buf into L.tot
-// (FP64) and L.totw (double-words), in every block in the same order: warp
-// w merges slots w, w + 16, ... with lane = accumulator, then the warps'
-// sums are merged in warp order.  poll: the slots may still be arriving
-// (reload a slot while any of its words holds kPoison, at most
-// J.spin_limit times); otherwise a grid barrier has ordered them.  Returns
-// false when a poll gave up (here or, seen on the error word, elsewhere).
-template <int kN>
-__device__ __forceinline__ bool fold_slots(const Job &J, LoopShared &L, State *S, int buf,
-                                           bool poll) {
-  __shared__ float2 wsum[kPW][32];
-  __shared__ int s_fail[kPW];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  CSum t = {0.f, 0.f};
-  bool fail = false;
-  // slots per warp in one round of loads: a grid of up to 192 blocks is
-  // folded with every load in flight at once
-  constexpr int kLoads = 12;
-  for (int b0 = warp; b0 < (int)gridDim.x && !fail; b0 += kPW * kLoads) {
-    float2 v[kLoads];
-#pragma unroll
-    for (int k = 0; k < kLoads; ++k) {
-      const int b = b0 + k * kPW;
-      v[k] = (b < (int)gridDim.x && lane < kN) ? ld_relaxed_f2(slot_of(J, buf, b) + lane)
-                                               : make_float2(0.f, 0.f);
-    }
-    if (poll) {
-      unsigned spins = 0;
-      for (;;) {
-        unsigned pending = 0;
-#pragma unroll
-        for (int k = 0; k < kLoads; ++k) {
-          const bool bad = __float_as_uint(v[k].x) == kPoison || __float_as_uint(v[k].y) == kPoison;
-          if (__any_sync(0xffffffffu, bad)) pending |= 1u << k;
-        }
-        if (!pending) break;
-        if (++spins > J.spin_limit) {
-          if (lane == 0) atomicOr(&S->bar_err, 1u);
-          fail = true;
-          break;
-        }
-        if ((spins & 63u) == 0 && ld_relaxed(&S->bar_err)) {
-          fail = true;
-          break;
-        }
-#pragma unroll
-        for (int k = 0; k < kLoads; ++k)
-          if ((pending & (1u << k)) && lane < kN)
-            v[k] = ld_relaxed_f2(slot_of(J, buf, b0 + k * kPW) + lane);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kLoads; ++k) csum_merge(t, v[k].x, v[k].y);
-  }
-  wsum[warp][lane] = make_float2(t.s, t.c);
-  if (lane == 0) s_fail[warp] = fail;
-  __syncthreads();
-  if (threadIdx.x < kN) {
-    CSum u = {0.f, 0.f};
-#pragma unroll
-    for (int w = 0; w < kPW; ++w) csum_merge(u, wsum[w][threadIdx.x].x, wsum[w][threadIdx.x].y);
-    L.tot[threadIdx.x] = (double)u.s + (double)u.c;
-    L.totw[threadIdx.x] = dw_of_csum(u.s, u.c);
-  }
-  bool any_fail = false;
-#pragma unroll
-  for (int w = 0; w < kPW; ++w) any_fail |= s_fail[w] != 0;
-  __syncthreads();
-  return !any_fail;
-}
-
-// This block's compensated sums of kN per-thread partials into its slot of
-// buffer buf.
-template <int kN>
-__device__ __forceinline__ void write_slot(const Job &J, const float *acc, float (*red)[kPT],
-                                           int buf) {
-  __shared__ float2 bsum[32];
-  block_reduce<kN, kPT>(acc, red, bsum);
-  if (threadIdx.x < kN) st_relaxed_f2(slot_of(J, buf, blockIdx.x) + threadIdx.x, bsum[threadIdx.x]);
-}
-
-extern __shared__ __align__(16) float s_red_p[];
+extern __shared__ __align__(16) float s_dyn_p[];
 
 template <typename FT, bool kGeom, bool kFeat, bool kHWC>
 __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job J) {
   __shared__ LoopShared L;
-  float(*red)[kPT] = reinterpret_cast<float(*)[kPT]>(s_red_p);
-  State *S = J.state;
   const int lane = threadIdx.x & 31;
   const long long n = J.n, npix = (long long)J.H * J.W;
   const long long G = gridDim.x, b = blockIdx.x;
   const long long pc = (npix + G - 1) / G;
   const long long p0 = min(npix, b * pc), p1 = min(npix, p0 + pc);
-  const Share src = share_of(n), tgt = share_of(npix);
+  const Share src = share_of(n, blockIdx.x, gridDim.x);
+  const Share tgt = share_of(npix, blockIdx.x, gridDim.x);
   SrcCache C;
   C.rounds = min(J.src_cache_rounds, src.rounds);
   C.cap = J.src_cache_rounds * kPR * kPT;
-  C.f = s_red_p + kAccs * kPT;
+  C.f = s_dyn_p;
   C.m = reinterpret_cast<uint8_t *>(C.f + 6 * C.cap);
 
   // set-up: the initial pose in every block; this block's key-map range
@@ -573,7 +143,7 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
   for (int r = 0; r < C.rounds; ++r) {
 #pragma unroll
     for (int k = 0; k < kPR; ++k) {
-      const long long i = unit_of(r, k);
+      const long long i = unit_of(r, k, blockIdx.x, gridDim.x);
       const int c = cache_index(r, k);
       const bool in = i < n;
       C.m[c] = in ? __ldg(J.sm + i) : (uint8_t)0;
@@ -613,11 +183,11 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
   }
   for (long long pix = p0 + threadIdx.x; pix < p1; pix += kPT) J.keys[pix] = ~0ull;
   unsigned nbar = 0;  // grid barriers passed
-  bool alive = grid_barrier(S, J, nbar++, true);
+  bool alive = group_barrier(J, nbar++, true);
 
   for (int iter = 0; alive && iter < J.iters; ++iter) {
     associate(J, L.P, src, C, iter);
-    if (!(alive = grid_barrier(S, J, nbar++, true))) break;
+    if (!(alive = group_barrier(J, nbar++, true))) break;
     float acc[kAccs];
 #pragma unroll
     for (int a = 0; a < kAccs; ++a) acc[a] = 0.f;
@@ -625,8 +195,8 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
     // every block has folded the previous iteration's buffer (it passed the
     // barrier above after its fold): poisoned again for the next iteration
     if (iter > 0) poison_slot(J, (iter + 1) & 1);
-    write_slot<kAccs>(J, acc, red, iter & 1);
-    if (!(alive = fold_slots<kAccs>(J, L, S, iter & 1, true))) break;
+    write_slot<kAccs>(J, acc, iter & 1);
+    if (!(alive = fold_slots<kAccs>(J, L, iter & 1, true))) break;
     if (threadIdx.x < 32) persist_step(J, L, iter, lane);
     __syncthreads();
     if (!L.ok) break;  // a failed solve ends the loop (icp.py:241-242 `except: break`)
@@ -635,7 +205,7 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
   // the association at the final pose and the information sum
   if (alive) {
     associate(J, L.P, src, C, J.iters);
-    alive = grid_barrier(S, J, nbar++, true);
+    alive = group_barrier(J, nbar++, true);
   }
   if (alive) {
     float acc[kInfoAccs];
@@ -643,13 +213,13 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
     for (int a = 0; a < kInfoAccs; ++a) acc[a] = 0.f;
     info_pixels(J, tgt, J.iters, acc);
     // (buffer 0: every block has folded the last iteration's sums)
-    write_slot<kInfoAccs>(J, acc, red, 0);
-    alive = grid_barrier(S, J, nbar++, blockIdx.x == 0);
+    write_slot<kInfoAccs>(J, acc, 0);
+    alive = group_barrier(J, nbar++, blockIdx.x == 0);
   }
   if (blockIdx.x != 0) return;
   double *R = J.result;
   if (alive) {
-    fold_slots<kInfoAccs>(J, L, S, 0, false);
+    fold_slots<kInfoAccs>(J, L, 0, false);
     for (int k = threadIdx.x; k < 36; k += kPT) {
       const int r = k / 6, c = k % 6;
       R[STB_RES_INFO + k] = L.tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
@@ -702,13 +272,12 @@ PersistFn pick_persist(const Plan &p) {
   }
 }
 
-// Dynamic shared memory: the block reduction's transpose (kAccs x kPT
-// floats), then the source-point cache of Job::src_cache_rounds rounds.
-constexpr size_t kRedSmem = sizeof(float) * kAccs * kPT;
+// Dynamic shared memory: the source-point cache of Job::src_cache_rounds
+// rounds.
 constexpr size_t cache_smem(int rounds) {
   return ((size_t)rounds * kPR * kPT * kCachePointBytes + 15) & ~size_t(15);
 }
-constexpr size_t kPersistSmem = kRedSmem + cache_smem(kMaxCacheRounds);
+constexpr size_t kPersistSmem = cache_smem(kMaxCacheRounds);
 static_assert(kPersistSmem + sizeof(LoopShared) + 8192 <= 227 * 1024,
               "the persistent kernel's shared memory fits one block per SM");
 
@@ -770,7 +339,7 @@ int launch_persistent(const Plan &p, Job job, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(kPT);
-  cfg.dynamicSmemBytes = kRedSmem + cache_smem(job.src_cache_rounds);
+  cfg.dynamicSmemBytes = cache_smem(job.src_cache_rounds);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

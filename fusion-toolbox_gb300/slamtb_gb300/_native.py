@@ -28,6 +28,7 @@ ST_NOT_PD, ST_NO_MATCHES, ST_NAN = 1, 2, 4
 # option bits or-ed into the channel_mode argument of the registration calls
 OPT_DW_SOLVE = 0x100
 OPT_MULTI_LAUNCH = 0x200
+OPT_GROUPS = 0x400
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64

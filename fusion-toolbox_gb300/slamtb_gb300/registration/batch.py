@@ -18,6 +18,12 @@ from ..processing import feature_pyramid
 from .icp import ICPOdometry
 from .result import RegistrationResult
 
+# Schedules of stb_icp_estimate_batch as BatchRegistration numbers them:
+# 0..5 the lock-step kernel's work-item sizes, GROUPED + g the grouped
+# kernel with g groups.
+GROUPED = 100
+TUNE_CONFIGS = (0, 1, 2, 3, 4, 5, GROUPED + 2, GROUPED + 4, GROUPED + 8, GROUPED + 19)
+
 
 class BatchPlan:
     """A prepared batch (``BatchRegistration.prepare``): device level table,
@@ -53,7 +59,10 @@ class BatchRegistration:
         self.feat_channel_mode = feat_channel_mode
         self.record_history = record_history
         self.last_history = None
-        self.tile_config = 0  # largest pixels per work item: 0 -> 8192; 1..5 -> 512 ... 8192
+        # schedule: 0..5 the lock-step kernel with its largest work item
+        # (0 -> 8192 pixels; 1..5 -> 512 ... 8192); GROUPED + g the grouped
+        # kernel with g groups (stb_icp_estimate_batch, STB_OPT_GROUPS)
+        self.tile_config = 0
         self.feat_layout = "auto"  # "auto": texel-major feature copies when C > 1; "planar"
 
     @property
@@ -149,20 +158,26 @@ class BatchRegistration:
 
     def run(self, plan, tile_config=None):
         """Enqueue ``plan`` on the current stream (one cooperative launch);
-        returns (results (B, 96) device tensor, history or None)."""
-        cfg = self.tile_config if tile_config is None else tile_config
+        returns (results (B, 96) device tensor, history or None).
+        ``tile_config``: the schedule (see ``self.tile_config``), default the
+        tuned one."""
+        cfg = int(self.tile_config if tile_config is None else tile_config)
+        mode, arg = plan.mode, cfg
+        if cfg >= GROUPED:
+            mode, arg = mode | N.OPT_GROUPS, cfg - GROUPED
         with torch.cuda.device(plan.device):
             N.check(N.lib().stb_icp_estimate_batch(
                 N.ptr(plan.levels), plan.B, plan.L, ctypes.cast(plan.params, ctypes.c_void_p),
-                plan.channels, plan.code, plan.mode, N.ptr(plan.init), plan.total_px,
+                plan.channels, plan.code, mode, N.ptr(plan.init), plan.total_px,
                 N.ptr(plan.ws), plan.ws.numel(), N.ptr(plan.results), N.ptr(plan.history),
-                int(cfg), N.stream_of(plan.device)))
+                arg, N.stream_of(plan.device)))
         return plan.results, plan.history
 
-    def autotune(self, plan, configs=(0, 1, 2, 3, 4, 5), reps=3):
-        """Times ``plan`` under each tile configuration (largest pixels per
-        work item: 0 -> 8192, 1..5 -> 512 ... 8192) with CUDA events and
-        keeps the fastest in ``self.tile_config``.  Returns {config: ms}."""
+    def autotune(self, plan, configs=TUNE_CONFIGS, reps=3):
+        """Times ``plan`` under each schedule (lock-step kernel with its
+        largest work item 0 -> 8192, 1..5 -> 512 ... 8192 pixels; grouped
+        kernel with GROUPED + g for g groups) with CUDA events and keeps the
+        fastest in ``self.tile_config``.  Returns {config: ms}."""
         stream = torch.cuda.current_stream(plan.device)
         times = {}
         for cfg in configs:

@@ -82,6 +82,14 @@ extern "C" {
  * replayable as a CUDA graph, instead of the default single cooperative
  * launch that runs the whole registration with grid barriers. */
 #define STB_OPT_MULTI_LAUNCH 0x200
+/* stb_icp_estimate_batch: the grouped schedule instead of the lock-step
+ * one.  The grid is split into tile_config groups (1 .. 96) of equal size;
+ * each group registers whole pairs (all levels and iterations, then the
+ * information matrix), one after the other, largest pairs first, with
+ * barriers of its own, so a pair's frames stay in L2 across its iterations
+ * and the groups' serial steps overlap.  Results are those of the
+ * lock-step schedule up to the order of float32 sums. */
+#define STB_OPT_GROUPS 0x400
 
 /* ---- per-registration status bits (result block, STB_RES_STATUS) ------- */
 #define STB_ST_NOT_PD 1u     /* 6x6 J^T J was not positive definite: stopped */
@@ -340,7 +348,9 @@ STB_API size_t stb_icp_batch_workspace_bytes(int32_t num_pairs,
  * history: NULL or device float64 [num_pairs][sum of num_iters][STB_HIST_SIZE].
  * tile_config: largest pixels per work item, 0 = 8192, 1..5 = 512 <<
  * (tile_config - 1); every level uses the largest power of two up to it that
- * still gives half of the blocks a work item per phase.
+ * still gives half of the blocks a work item per phase.  With
+ * STB_OPT_GROUPS in channel_mode, tile_config is the number of groups of
+ * the grouped schedule (1 .. 96).
  */
 STB_API int stb_icp_estimate_batch(
     const stb_level *levels, int32_t num_pairs, int32_t num_levels,

