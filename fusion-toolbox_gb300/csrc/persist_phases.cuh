@@ -274,11 +274,30 @@ __device__ __forceinline__ void associate(const X &J, const Pose32 &P, Share sh,
   }
 }
 
+// Unit of thread t's k-th slot in round r of block `rank` of `size` (as
+// unit_of, for another thread of the block).
+__device__ __forceinline__ long long unit_of_thread(int r, int k, int t, int rank, int size) {
+  const long long slot = (long long)r * kChunksPerRound + k * (kPT / kChunk) + t / kChunk;
+  return (rank + (long long)size * slot) * kChunk + (t % kChunk);
+}
+
 // Per-thread partials of the normal equations over this block's share of
 // the target pixels at epoch e.
+//
+// Only the pixels whose key carries the epoch's tag (about one in ten at
+// 640x480) contribute, and they are scattered over the warp's lanes: a
+// warp that ran the residual and Jacobian on its own lanes' pixels would
+// execute them for almost every pixel slot with a few lanes active.  So a
+// round first reads the keys of the warp's kPR x 32 pixels, packs the
+// matched ones (their slot and winning source index) into a per-warp list
+// in ballot order, and then the warp's lanes take the list's entries in
+// turn: the target point, normal and source point loads of all of a lane's
+// entries are issued before the first use, and the arithmetic runs with
+// full lanes.  The list order is fixed, so the sums are deterministic.
 template <typename FT, bool kGeom, bool kFeat, bool kHWC, class X>
 __device__ __forceinline__ void reduce_pixels(const X &J, const Pose32 &P, Share sh, int e,
                                               float *acc) {
+  __shared__ unsigned s_list[kPW][kPR * 32];  // (source index << 8) | (slot << 5) | lane
   const unsigned tag = 254u - (unsigned)e;
   const int H = J.H, W = J.W;
   const long long npix = (long long)H * W;
@@ -287,37 +306,56 @@ __device__ __forceinline__ void reduce_pixels(const X &J, const Pose32 &P, Share
   const float *__restrict__ tp = J.tp;
   const float *__restrict__ tn = J.tn;
   const bool unit_w = J.wg1 == 1.f && J.wg2 == 1.f;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rank = rank_of(J), size = size_of(J);
+  unsigned *list = s_list[warp];
   for (int r = 0; r < sh.rounds; ++r) {
     unsigned long long key[kPR];
-    float q[kPR][3], m[kPR][3];
 #pragma unroll
     for (int k = 0; k < kPR; ++k) {
-      const long long pix = unit_of(r, k, rank_of(J), size_of(J));
-      const long long pc = pix < npix ? pix : 0;
+      const long long pix = unit_of(r, k, rank, size);
       key[k] = pix < npix ? __ldcg(keys + pix) : 0ull;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        q[k][d] = kGeom ? __ldg(tp + 3 * pc + d) : 0.f;
-        m[k][d] = kGeom ? __ldg(tn + 3 * pc + d) : 0.f;
-      }
     }
-    float s[kPR][3];
+    int count = 0;
 #pragma unroll
     for (int k = 0; k < kPR; ++k) {
       const bool match = (unsigned)(key[k] >> 56) == tag;
-      const long long i = (long long)(key[k] & 0xffffffull);
+      const unsigned bal = __ballot_sync(0xffffffffu, match);
+      if (match)
+        list[count + __popc(bal & ((1u << lane) - 1u))] =
+            ((unsigned)(key[k] & 0xffffffull) << 8) | ((unsigned)k << 5) | (unsigned)lane;
+      count += __popc(bal);
+    }
+    __syncwarp();
+    const int rounds = (count + 31) >> 5;  // warp-uniform, at most kPR
+    int src[kPR];  // the entry's winning source point, -1 past the list
+    float q[kPR][3], m[kPR][3], s[kPR][3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) s[k][d] = match ? __ldg(sp + 3 * i + d) : 0.f;
+    for (int j = 0; j < kPR; ++j) {
+      if (j >= rounds) break;
+      const int d = lane + 32 * j;
+      const unsigned ent = d < count ? list[d] : 0u;
+      const long long pc =
+          d < count ? unit_of_thread(r, (ent >> 5) & 7u, warp * 32 + (ent & 31u), rank, size) : 0;
+      src[j] = d < count ? (int)(ent >> 8) : -1;
+      const long long ic = ent >> 8;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        q[j][c] = kGeom ? __ldg(tp + 3 * pc + c) : 0.f;
+        m[j][c] = kGeom ? __ldg(tn + 3 * pc + c) : 0.f;
+        s[j][c] = __ldg(sp + 3 * ic + c);
+      }
     }
 #pragma unroll
-    for (int k = 0; k < kPR; ++k) {
-      if ((unsigned)(key[k] >> 56) != tag) continue;
-      const long long i = (long long)(key[k] & 0xffffffull);
-      const float3 Tp = transform_point(P.rt, s[k][0], s[k][1], s[k][2]);
+    for (int j = 0; j < kPR; ++j) {
+      if (j >= rounds) break;
+      if (src[j] < 0) continue;
+      const long long i = src[j];
+      const float3 Tp = transform_point(P.rt, s[j][0], s[j][1], s[j][2]);
       if (kGeom) {
-        const float nx = m[k][0], ny = m[k][1], nz = m[k][2];
-        const float r = dot3(fsub(q[k][0], Tp.x), fsub(q[k][1], Tp.y), fsub(q[k][2], Tp.z), nx,
-                             ny, nz);
+        const float nx = m[j][0], ny = m[j][1], nz = m[j][2];
+        const float rr = dot3(fsub(q[j][0], Tp.x), fsub(q[j][1], Tp.y), fsub(q[j][2], Tp.z), nx,
+                              ny, nz);
         const float Jv[6] = {nx, ny, nz, fsub(fmul(Tp.y, nz), fmul(Tp.z, ny)),
                              fsub(fmul(Tp.z, nx), fmul(Tp.x, nz)),
                              fsub(fmul(Tp.x, ny), fmul(Tp.y, nx))};
@@ -331,11 +369,11 @@ __device__ __forceinline__ void reduce_pixels(const X &J, const Pose32 &P, Share
             for (int c = a; c < 6; ++c)
               acc[upper_index(a, c)] = fmaf(Jv[a], Jv[c], acc[upper_index(a, c)]);
 #pragma unroll
-          for (int a = 0; a < 6; ++a) acc[kJr + a] = fmaf(Jv[a], r, acc[kJr + a]);
-          acc[kR2] = fmaf(r, r, acc[kR2]);
+          for (int a = 0; a < 6; ++a) acc[kJr + a] = fmaf(Jv[a], rr, acc[kJr + a]);
+          acc[kR2] = fmaf(rr, rr, acc[kR2]);
         } else {
-          accumulate_se3(acc, Jv, r, J.wg1, J.wg2);
-          acc[kR2] += J.wg1 * (r * r);
+          accumulate_se3(acc, Jv, rr, J.wg1, J.wg2);
+          acc[kR2] += J.wg1 * (rr * rr);
         }
         acc[kCountGeom] += 1.f;
       }
@@ -350,6 +388,7 @@ __device__ __forceinline__ void reduce_pixels(const X &J, const Pose32 &P, Share
         }
       }
     }
+    __syncwarp();  // the list is rewritten by the next round
   }
 }
 
