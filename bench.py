@@ -188,6 +188,15 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def run_config():
+    """The workload's config, the same on the GPU and reference arms."""
+    return {"workload": WORKLOAD,
+            "l2": "GPU arm: flushed (512 MB write) before every step; the pair (~18 MB) "
+                  "stays L2-resident across its 10 iterations",
+            "launch": "GPU arm: one cooperative kernel per registration (grid barriers "
+                      "between its phases); reference arm: the CPU path on the host cores"}
+
+
 def run_reference(args, rank, world):
     """CPU arm: the C/OpenMP restatement of the reference's CPU ICP path on
     the host cores, on the same workload; rank 0 only."""
@@ -227,8 +236,7 @@ def run_reference(args, rank, world):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD,
-                   "iters_per_step": iters},
+        "config": run_config(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -1084,11 +1092,7 @@ def main():
             "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD,
-                       "l2": "flushed (512 MB write) before every step; the pair "
-                             "(~18 MB) stays L2-resident across its 10 iterations",
-                       "launch": "one cooperative kernel per registration "
-                                 "(grid barriers between its phases)"},
+            "config": run_config(),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,

@@ -639,12 +639,34 @@ struct GraphEntry {
   cudaGraphNode_t begin_node = nullptr;
   cudaKernelNodeParams begin_params{};
   ProfSet *prof = nullptr;  // event pairs captured in the graph (profiling)
+  unsigned long long last_use = 0;
 };
+
+// Graphs kept at most; past it the least recently replayed one is
+// destroyed (an executable graph destroyed while a replay is in flight is
+// freed when that replay completes).
+constexpr size_t kMaxGraphs = 64;
 
 using GraphKey =
     std::tuple<void *, int64_t, int, int, int, int, int, int, int, int, int, bool, bool>;
 std::mutex g_graph_mutex;
 std::map<GraphKey, GraphEntry> g_graphs;
+unsigned long long g_graph_tick = 0;
+
+void evict_oldest_graph() {
+  auto oldest = g_graphs.begin();
+  for (auto it = g_graphs.begin(); it != g_graphs.end(); ++it)
+    if (it->second.last_use < oldest->second.last_use) oldest = it;
+  GraphEntry &e = oldest->second;
+  {
+    std::lock_guard<std::mutex> plock(g_prof_mutex);
+    if (g_prof_last == e.prof) g_prof_last = nullptr;
+  }
+  cudaGraphExecDestroy(e.exec);
+  cudaGraphDestroy(e.graph);
+  delete e.prof;
+  g_graphs.erase(oldest);
+}
 
 int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st) {
   std::lock_guard<std::mutex> lock(g_graph_mutex);
@@ -657,6 +679,7 @@ int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st)
   Job *dst = p.job_dev;
   void *args[] = {&job_copy, &dst};
   if (it == g_graphs.end()) {
+    if (g_graphs.size() >= kMaxGraphs) evict_oldest_graph();
     cudaStream_t cap;
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess)
       return check_launch("cudaStreamCreate");
@@ -699,6 +722,7 @@ int run_graph(const Plan &p, const Job &job, bool with_history, cudaStream_t st)
     it = g_graphs.emplace(key, e).first;
   }
   GraphEntry &e = it->second;
+  e.last_use = ++g_graph_tick;
   if (e.prof) {
     std::lock_guard<std::mutex> plock(g_prof_mutex);
     g_prof_last = e.prof;
