@@ -569,6 +569,16 @@ __device__ __forceinline__ void stage_init(StageCtl &ctl) {
 
 // Copies the streams of one sub-chunk into stage st.  All threads call it
 // (after a __syncthreads that ends every read of the stage).
+// One 4-byte word global -> shared, asynchronously (waited by
+// cp_async_wait_all in the same thread).
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
 __device__ __forceinline__ void stage_issue(const StageStream *ss, int count, int st,
                                             StageCtl &ctl) {
   unsigned bulk[3];
@@ -737,10 +747,7 @@ __device__ __forceinline__ void assoc_tile(const BatchArgs &a, const long long *
       const float sq = dot3(dx, dy, dz, dx, dy, dz);
       if (sq > q.thr2) continue;
       const float3 Tn = transform_normal(P.nm, sn[3 * j], sn[3 * j + 1], sn[3 * j + 2]);
-      const float cs = fdiv(dot3(Tn.x, Tn.y, Tn.z, mx[k], my[k], mz[k]),
-                            fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
-                                 __fsqrt_rn(dot3(mx[k], my[k], mz[k], mx[k], my[k], mz[k]))));
-      if (cs >= -1.0f && cs <= q.cos_max) continue;
+      if (normal_angle_rejects(Tn, mx[k], my[k], mz[k], q.cos_max)) continue;
       const float dist = __fsqrt_rn(sq);
       atomicMin(keys + pix[k], tag | ((unsigned long long)__float_as_uint(dist) << 24) |
                                    (unsigned long long)(b0 + j));
@@ -837,8 +844,11 @@ __device__ void pair_step(const BatchArgs &a, int p, int level, int s, const dou
 // ---------------------------------------------------------------------------
 // phase B: reduction of one target tile (+ group / pair folds and the step)
 // ---------------------------------------------------------------------------
+// match_list: the block's per-warp lists of matched pixels (kThreads / 32
+// lists of kCh x 32 entries, shared memory)
 template <typename FT, bool kFeat, bool kInfo, bool kHWC, int kCh>
-__device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long *off, int level,
+__device__ __forceinline__ void reduce_tile(unsigned *match_list, const BatchArgs &a,
+                                            const long long *off, int level,
                                             long long t, int s, TileCache &tc, StageCtl &ctl,
                                             unsigned &ph) {
   constexpr int kN = kInfo ? 21 : kAccsB;
@@ -847,6 +857,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   __shared__ float bs[32], bc[32];
   __shared__ double tot[32];
   __shared__ float2 totw[32];
+  static_assert(kCh <= 4, "the match list packs the slot in two bits");
   const int p = cache_pair(a, off, level, t, !kInfo, tc);
   if (tc.skip) return;
   const Pose32 &P = tc.P;
@@ -874,39 +885,75 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
   const long long end = min((lt + 1) * tile, npix);
   const int nsub = start < end ? (int)((end - start + kSub - 1) / kSub) : 0;
   const bool need_n = !kInfo && q.use_geom;
-  // stage layout: keys [kSub] | target xyz [kSub][3] | target normal [kSub][3]
+  // stage layout: keys [kSub] | target xyz [kSub][3] | target normal [kSub][3].
+  // Only the keys are staged for every pixel; the target point and normal
+  // of the (about one in ten) matched pixels are gathered into their slots
+  // by the lanes that process them (cp.async, 4 bytes a word), so the
+  // reduction reads 8 B per pixel plus ~2.4 B of targets instead of 32 B.
   auto issue = [&](int c) {
     const long long b0 = start + (long long)c * kSub;
     const unsigned n = (unsigned)min((long long)kSub, end - b0);
     unsigned char *buf = stage_buf<kCh>(c & 1);
-    const StageStream ss[3] = {{buf, keys + b0, 8u * n, 8},
-                               {buf + kSub * 8, lv.tgt_points + 3 * b0, 12u * n, 4},
-                               {buf + kSub * 20, lv.tgt_normals + 3 * b0, need_n ? 12u * n : 0u, 4}};
-    stage_issue(ss, 3, c & 1, ctl);
+    const StageStream ss[1] = {{buf, keys + b0, 8u * n, 8}};
+    stage_issue(ss, 1, c & 1, ctl);
   };
   auto compute = [&](int c, int st) {
     const long long b0 = start + (long long)c * kSub;
     const int nn = (int)min((long long)kSub, end - b0);
     const unsigned long long *skeys = reinterpret_cast<const unsigned long long *>(stage_buf<kCh>(st));
-    const float *stq = reinterpret_cast<const float *>(stage_buf<kCh>(st) + kSub * 8);
-    const float *stn = reinterpret_cast<const float *>(stage_buf<kCh>(st) + kSub * 20);
-    // pass 1: the winners' source points (the gathers that remain)
-    unsigned long long key[kCh];
+    float *stq = reinterpret_cast<float *>(stage_buf<kCh>(st) + kSub * 8);
+    float *stn = reinterpret_cast<float *>(stage_buf<kCh>(st) + kSub * 20);
+    // pass 1: the warp's matched pixels of the sub-chunk packed into its
+    // list in ballot order ((source index << 7) | (slot << 5) | lane), so
+    // that the arithmetic below runs with full lanes (about one pixel in
+    // ten matches); then each lane's entries' target points and normals
+    // (into their stage slots) and source points, all issued before the
+    // first use
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned *list = match_list + warp * (kCh * 32);
+    int count = 0;
+#pragma unroll
+    for (int k = 0; k < kCh; ++k) {
+      const int j = k * kThreads + threadIdx.x;
+      const unsigned long long key = j < nn ? skeys[j] : 0ull;
+      const bool m = (unsigned)(key >> 56) == tag;
+      const unsigned bal = __ballot_sync(0xffffffffu, m);
+      if (m)
+        list[count + __popc(bal & ((1u << lane) - 1u))] =
+            ((unsigned)(key & 0xffffffull) << 7) | ((unsigned)k << 5) | (unsigned)lane;
+      count += __popc(bal);
+    }
+    __syncwarp();
+    const int rounds = (count + 31) >> 5;  // warp-uniform, at most kCh
+    int jj[kCh];
+    long long ii[kCh];
     float spt[kCh][3];
 #pragma unroll
     for (int k = 0; k < kCh; ++k) {
-      const int j = k * kThreads + threadIdx.x;
-      key[k] = j < nn ? skeys[j] : 0ull;
-      const bool m = (unsigned)(key[k] >> 56) == tag;
-      const long long i = (m && !kInfo) ? (long long)(key[k] & 0xffffffull) : 0;
+      if (k >= rounds) break;
+      const int d = lane + 32 * k;
+      const unsigned ent = d < count ? list[d] : 0u;
+      jj[k] = d < count ? (int)((ent >> 5) & 3u) * kThreads + warp * 32 + (int)(ent & 31u) : -1;
+      ii[k] = (long long)(ent >> 7);
+      if (jj[k] >= 0) {
+        const long long g = b0 + jj[k];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) spt[k][d] = kInfo ? 0.f : __ldg(lv.src_points + 3 * i + d);
+        for (int c = 0; c < 3; ++c) {
+          cp_async4(stq + 3 * jj[k] + c, lv.tgt_points + 3 * g + c);
+          if (need_n) cp_async4(stn + 3 * jj[k] + c, lv.tgt_normals + 3 * g + c);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        spt[k][c] = kInfo ? 0.f : __ldg(lv.src_points + 3 * ii[k] + c);
     }
+    cp_async_wait_all();  // this lane's gathers (each lane reads only its own)
     // pass 2: residuals, Jacobians and the per-thread sums
 #pragma unroll
     for (int k = 0; k < kCh; ++k) {
-      if ((unsigned)(key[k] >> 56) != tag) continue;
-      const int j = k * kThreads + threadIdx.x;
+      if (k >= rounds) break;
+      if (jj[k] < 0) continue;
+      const int j = jj[k];
       const float qx = stq[3 * j], qy = stq[3 * j + 1], qz = stq[3 * j + 2];
       if (kInfo) {
         const float G0[6] = {0.f, qz, -qy, 1.f, 0.f, 0.f};
@@ -919,7 +966,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
             acc[upper_index(i, j)] += G0[i] * G0[j] + G1[i] * G1[j] + G2[i] * G2[j];
         continue;
       }
-      const long long i = (long long)(key[k] & 0xffffffull);
+      const long long i = ii[k];
       const float3 Tp = transform_point(P.rt, spt[k][0], spt[k][1], spt[k][2]);
       if (q.use_geom) {
         const float nx = stn[3 * j], ny = stn[3 * j + 1], nz = stn[3 * j + 2];
@@ -941,6 +988,7 @@ __device__ __forceinline__ void reduce_tile(const BatchArgs &a, const long long 
         }
       }
     }
+    __syncwarp();  // the list is rewritten by the next sub-chunk
   };
   stage_pipeline(nsub, ctl, ph, a.sync + 2, issue, compute);
 
@@ -1022,6 +1070,7 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
   __shared__ BatchArgs a;
   __shared__ TileCache tc;
   __shared__ StageCtl ctl;
+  __shared__ unsigned s_match[(kThreads / 32) * kCh * 32];
   unsigned ph = 0;  // expected parities of the two staging barriers
   for (int k = threadIdx.x; k < (int)(sizeof(BatchArgs) / sizeof(int)); k += blockDim.x)
     reinterpret_cast<int *>(&a)[k] = reinterpret_cast<const int *>(&args)[k];
@@ -1093,7 +1142,7 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
       off = stage_offsets(a.tgt_off + row, a, s_off);
       reset_cache(tc);
       for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
-        reduce_tile<FT, kFeat, false, kHWC, kCh>(a, off, level, t, s, tc, ctl, ph);
+        reduce_tile<FT, kFeat, false, kHWC, kCh>(s_match, a, off, level, t, s, tc, ctl, ph);
       });
       if (!grid_sync(a.sync, a.spin_limit, a.bar_phantom)) return;
     }
@@ -1112,7 +1161,7 @@ __global__ void __launch_bounds__(kThreads, BatchShape<kFeat>::kBlocksPerSM)
   off = stage_offsets(a.tgt_off + row, a, s_off);
   reset_cache(tc);
   for_each_tile(a.sync, phase++, tgt_tiles, [&](long long t) {
-    reduce_tile<FT, false, true, false, kCh>(a, off, level, t, s, tc, ctl, ph);
+    reduce_tile<FT, false, true, false, kCh>(s_match, a, off, level, t, s, tc, ctl, ph);
   });
 }
 

@@ -163,30 +163,6 @@ __device__ __forceinline__ void refresh_view(LoopShared &L, bool dw, int lane) {
   __syncwarp();
 }
 
-// The normal-angle gate of the association (correspondence.hpp:69-89):
-// with c = (Tn . m) / (sqrt(Tn . Tn) sqrt(m . m)) in the reference's
-// float32 operations, the pair is rejected when -1 <= c <= cos_max.  Only
-// the outcome matters, so c is first estimated as (Tn . m) rsqrt((Tn . Tn)
-// (m . m)): the dot products are the same bits, rsqrtf is within 2 ulp and
-// the two products add one rounding each, so the estimate is within
-// 2^-22 + 2^-23 of c relative, and c's own four roundings within 2^-22:
-// |estimate - c| < 6e-7 for |c| <= 1.  Where the estimate is at least 2e-6
-// from cos_max and 4e-6 above -1 (and the norms are normal, finite
-// floats), it decides as c would; otherwise c is formed exactly.
-__device__ __forceinline__ bool normal_angle_rejects(const float3 &Tn, float mx, float my,
-                                                     float mz, float cos_max) {
-  const float d = dot3(Tn.x, Tn.y, Tn.z, mx, my, mz);
-  const float nn = dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z);
-  const float mm = dot3(mx, my, mz, mx, my, mz);
-  const float pm = nn * mm;
-  if (pm > 1e-30f && pm < 1e30f) {
-    const float ce = d * rsqrtf(pm);
-    if (fabsf(ce - cos_max) > 2e-6f && ce > -1.0f + 4e-6f && ce < 2.0f) return ce <= cos_max;
-  }
-  const float c = fdiv(d, fmul(__fsqrt_rn(nn), __fsqrt_rn(mm)));
-  return c >= -1.0f && c <= cos_max;
-}
-
 // Association of this block's share of the source points at epoch e.
 template <class X>
 __device__ __forceinline__ void associate(const X &J, const Pose32 &P, Share sh,
