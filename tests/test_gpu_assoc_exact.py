@@ -187,11 +187,13 @@ def _batch_pairs(cuda):
     return pairs
 
 
+@pytest.mark.parametrize("schedule", [0, 103])
 @pytest.mark.parametrize("levels", [1, 2, 3])
-def test_batch_association_every_level(cuda, levels):
+def test_batch_association_every_level(cuda, levels, schedule):
     """The coarsest `levels` levels of three uneven pairs in one batch; the
     last of them runs k iterations, so the final association is at that
-    level's k-th pose."""
+    level's k-th pose.  Under the lock-step schedule and the grouped one
+    (three groups)."""
     from slamtb_gb300 import _native as N
     from slamtb_gb300.registration import BatchRegistration, ICPOdometry
     pairs = _batch_pairs(cuda)
@@ -202,6 +204,7 @@ def test_batch_association_every_level(cuda, levels):
                                 normals_angle_thresh=ANGLE_20))
                 for s, n in zip(SCALES[len(SCALES) - levels:], its)]
         br = BatchRegistration(ests)
+        br.tile_config = schedule
         srcs = [p["src"][:levels] for p in pairs]
         tgts = [p["tgt"][:levels] for p in pairs]
         res, _, plan = br.launch(srcs, tgts)
@@ -222,7 +225,7 @@ def test_batch_association_every_level(cuda, levels):
                 pose = r[N.RES_TRANSFORM:N.RES_TRANSFORM + 16].reshape(4, 4)
             else:
                 assert k == 0
-                pose = _start_pose(cuda, pairs, q, levels)
+                pose = _start_pose(cuda, pairs, q, levels, schedule)
             d = dict(kcam=sl.kcam, src=dict(points=sl.points, normals=sl.normals, mask=sl.mask),
                      tgt=dict(points=tl.points, normals=tl.normals, mask=tl.mask))
             a = _oracle_map(d, pose, 0.1, ANGLE_20)
@@ -231,9 +234,10 @@ def test_batch_association_every_level(cuda, levels):
                                           err_msg=f"pair {q}, {levels} levels, {k} iterations")
 
 
-def _start_pose(cuda, pairs, q, levels):
+def _start_pose(cuda, pairs, q, levels, schedule):
     """Pose pair q starts its `levels`-th level from: the result of the
-    coarser levels' batch (identity for the coarsest level)."""
+    coarser levels' batch under the same schedule (identity for the
+    coarsest level)."""
     from slamtb_gb300 import _native as N
     from slamtb_gb300.registration import BatchRegistration, ICPOdometry
     if levels == 1:
@@ -242,8 +246,10 @@ def _start_pose(cuda, pairs, q, levels):
     ests = [(s, ICPOdometry(n, geom_weight=1.0, feat_weight=0.0, distance_threshold=0.1,
                             normals_angle_thresh=ANGLE_20))
             for s, n in zip(SCALES[len(SCALES) - levels + 1:], its)]
-    res, _, _ = BatchRegistration(ests).launch([p["src"][:levels - 1] for p in pairs],
-                                               [p["tgt"][:levels - 1] for p in pairs])
+    br = BatchRegistration(ests)
+    br.tile_config = schedule
+    res, _, _ = br.launch([p["src"][:levels - 1] for p in pairs],
+                          [p["tgt"][:levels - 1] for p in pairs])
     r = res.cpu().numpy()[q]
     return r[N.RES_TRANSFORM:N.RES_TRANSFORM + 16].reshape(4, 4) if r[N.RES_ITERS] > 0 \
         else np.eye(4)

@@ -113,6 +113,40 @@ def test_batch_registration_levels_and_argument_checks():
         b.prepare([], [])
 
 
+def test_batch_schedule_encoding(monkeypatch):
+    """BatchRegistration.run passes the lock-step schedules (0..5) as the
+    entry's tile_config and the grouped ones (GROUPED + g) as
+    STB_OPT_GROUPS in channel_mode with g groups; the tuned default covers
+    both kinds."""
+    import types
+
+    import torch
+
+    from slamtb_gb300 import _native as N
+    from slamtb_gb300.registration import BatchRegistration, ICPOdometry
+    from slamtb_gb300.registration import batch as bmod
+    calls = []
+
+    class FakeLib:
+        def stb_icp_estimate_batch(self, *args):
+            calls.append(args)
+            return 0
+
+    monkeypatch.setattr(N, "lib", lambda: FakeLib())
+    monkeypatch.setattr(N, "stream_of", lambda device: None)
+    monkeypatch.setattr(torch.cuda, "device", lambda d: __import__("contextlib").nullcontext())
+    b = BatchRegistration([(1.0, ICPOdometry(3))])
+    plan = types.SimpleNamespace(
+        device="cuda:0", levels=None, B=2, L=1, params=b._params()[0], channels=0, code=0,
+        mode=1, init=None, total_px=100, ws=torch.empty(1), results=None, history=None)
+    b.run(plan, 3)
+    b.run(plan, bmod.GROUPED + 8)
+    assert calls[0][6] == 1 and calls[0][13] == 3
+    assert calls[1][6] == 1 | N.OPT_GROUPS and calls[1][13] == 8
+    assert any(c < bmod.GROUPED for c in bmod.TUNE_CONFIGS)
+    assert any(c > bmod.GROUPED for c in bmod.TUNE_CONFIGS)
+
+
 def test_multiscale_level_loop_hands_transforms_coarse_to_fine():
     """MultiscaleRegistration.estimate_pyramid (multiscale.py:52-67): the
     estimators, listed finest first, run on the pyramid coarsest first; each
