@@ -421,7 +421,7 @@ def _time_batch(br, plan, reps, device):
           for _ in range(reps)]
     for a, b in ev:
         a.record(stream)
-        br.run(plan)
+        br.run(plan, graph=True)
         b.record(stream)
     torch.cuda.synchronize(device)
     ms = [a.elapsed_time(b) for a, b in ev]

@@ -135,6 +135,7 @@ class BatchRegistration:
             total_px += biggest
         plan = BatchPlan()
         plan.B, plan.L, plan.device = B, L, device
+        plan.graphs = {}  # schedule -> CUDA graph of its launch sequence
         plan.levels = torch.frombuffer(bytearray(bytes(lv)), dtype=torch.uint8).to(device)
         plan.params, plan.total_iters = self._params()
         plan.channels, plan.code, plan.total_px = channels, code, total_px
@@ -156,12 +157,33 @@ class BatchRegistration:
                      | (N.OPT_DW_SOLVE if self.solve_precision == "dw" else 0))
         return plan
 
-    def run(self, plan, tile_config=None):
+    def run(self, plan, tile_config=None, graph=False):
         """Enqueue ``plan`` on the current stream (one cooperative launch);
         returns (results (B, 96) device tensor, history or None).
         ``tile_config``: the schedule (see ``self.tile_config``), default the
-        tuned one."""
+        tuned one.  ``graph``: replay the launch sequence (barrier-word
+        memset, the persistent kernel with every level and Gauss-Newton
+        iteration of every pair, the status pass) as a CUDA graph captured
+        on the plan's first call with this schedule; the plan's buffers are
+        the graph's, so the results are the same."""
         cfg = int(self.tile_config if tile_config is None else tile_config)
+        if graph:
+            g = plan.graphs.get(cfg)
+            if g is None:
+                g = torch.cuda.CUDAGraph()
+                cur = torch.cuda.current_stream(plan.device)
+                side = torch.cuda.Stream(plan.device)
+                side.wait_stream(cur)
+                with torch.cuda.stream(side), torch.cuda.graph(g, stream=side):
+                    self._launch(plan, cfg)
+                cur.wait_stream(side)
+                plan.graphs[cfg] = g
+            g.replay()
+            return plan.results, plan.history
+        self._launch(plan, cfg)
+        return plan.results, plan.history
+
+    def _launch(self, plan, cfg):
         mode, arg = plan.mode, cfg
         if cfg >= GROUPED:
             mode, arg = mode | N.OPT_GROUPS, cfg - GROUPED
@@ -171,7 +193,6 @@ class BatchRegistration:
                 plan.channels, plan.code, mode, N.ptr(plan.init), plan.total_px,
                 N.ptr(plan.ws), plan.ws.numel(), N.ptr(plan.results), N.ptr(plan.history),
                 arg, N.stream_of(plan.device)))
-        return plan.results, plan.history
 
     def autotune(self, plan, configs=TUNE_CONFIGS, reps=3):
         """Times ``plan`` under each schedule (lock-step kernel with its

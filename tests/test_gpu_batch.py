@@ -206,3 +206,21 @@ def test_bounded_waits_give_up_with_a_timeout_status(cuda, schedule):
     assert ((status & N.ST_TIMEOUT) != 0).all()
     res = br.estimate_pyramids(srcs, tgts)
     assert all(r.transform is not None for r in res)
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_graph_replay_equals_direct(cuda, schedule):
+    """BatchRegistration.run(graph=True) captures the launch sequence once
+    per schedule and replays it: every replay gives the direct launch's
+    result block bit for bit."""
+    from slamtb_gb300.registration import BatchRegistration
+    pairs = [_pair(cuda, 90 + k, w, h, False) for k, (w, h) in enumerate([(320, 240), (160, 120)])]
+    br = BatchRegistration(_estimators(0.0))
+    br.tile_config = schedule
+    plan = br.prepare([p["src"] for p in pairs], [p["tgt"] for p in pairs])
+    direct = br.run(plan)[0].clone()
+    for _ in range(2):
+        replay = br.run(plan, graph=True)[0]
+        torch.cuda.synchronize()
+        assert torch.equal(replay, direct)
+    assert list(plan.graphs) == [schedule]
