@@ -182,9 +182,23 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
     if (lane == 0) inverse_transpose(L.rt32, L.P.nm);
   }
   for (long long pix = p0 + threadIdx.x; pix < p1; pix += kPT) J.keys[pix] = ~0ull;
+  // this block's range of the target frame into L2 (128-byte lines): the
+  // first association's gathers then hit L2 instead of memory
+  if (p1 > p0) {
+    const char *pt = reinterpret_cast<const char *>(J.tp + 3 * p0);
+    const char *pn = reinterpret_cast<const char *>(J.tn + 3 * p0);
+    const long long nb = 12 * (p1 - p0);
+    for (long long off = 128ll * threadIdx.x; off < nb; off += 128ll * kPT) {
+      prefetch_l2(pt + off);
+      prefetch_l2(pn + off);
+    }
+    for (long long off = 128ll * threadIdx.x; off < p1 - p0; off += 128ll * kPT)
+      prefetch_l2(J.tm + p0 + off);
+  }
   unsigned nbar = 0;  // grid barriers passed
   bool alive = group_barrier(J, nbar++, true);
 
+  int used = 0;  // iterations that wrote and folded their slots
   for (int iter = 0; alive && iter < J.iters; ++iter) {
     associate(J, L.P, src, C, iter);
     if (!(alive = group_barrier(J, nbar++, true))) break;
@@ -197,6 +211,7 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
     if (iter > 0) poison_slot(J, (iter + 1) & 1);
     write_slot<kAccs>(J, acc, iter & 1);
     if (!(alive = fold_slots<kAccs>(J, L, iter & 1, true))) break;
+    ++used;
     if (threadIdx.x < 32) persist_step(J, L, iter, lane);
     __syncthreads();
     if (!L.ok) break;  // a failed solve ends the loop (icp.py:241-242 `except: break`)
@@ -207,19 +222,21 @@ __global__ void __launch_bounds__(kPT, 1) k_persist(const __grid_constant__ Job 
     associate(J, L.P, src, C, J.iters);
     alive = group_barrier(J, nbar++, true);
   }
+  // the information sums go to the slot buffer the next iteration would
+  // have used: poisoned (at the set-up, or after the last iteration's
+  // association barrier), so block 0 folds them as they land and no block
+  // waits at a last barrier
   if (alive) {
     float acc[kInfoAccs];
 #pragma unroll
     for (int a = 0; a < kInfoAccs; ++a) acc[a] = 0.f;
     info_pixels(J, tgt, J.iters, acc);
-    // (buffer 0: every block has folded the last iteration's sums)
-    write_slot<kInfoAccs>(J, acc, 0);
-    alive = group_barrier(J, nbar++, blockIdx.x == 0);
+    write_slot<kInfoAccs>(J, acc, used & 1);
   }
   if (blockIdx.x != 0) return;
   double *R = J.result;
+  if (alive) alive = fold_slots<kInfoAccs>(J, L, used & 1, true);
   if (alive) {
-    fold_slots<kInfoAccs>(J, L, 0, false);
     for (int k = threadIdx.x; k < 36; k += kPT) {
       const int r = k / 6, c = k % 6;
       R[STB_RES_INFO + k] = L.tot[r <= c ? upper_index(r, c) : upper_index(c, r)];
