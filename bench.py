@@ -89,6 +89,9 @@ def parse():
     ap.add_argument("--profile-case", choices=["batch", "loss", "feature"], default=None,
                     help="run only a small case of one secondary workload (for ncu captures)")
     ap.add_argument("--pairs", type=int, default=8, help="pairs of the --profile-case")
+    ap.add_argument("--schedule", type=int, default=0,
+                    help="batch schedule of the --profile-case (BatchRegistration.tile_config: "
+                         "0..5 lock-step, 100 + g grouped with g groups)")
     return ap.parse_args()
 
 
@@ -802,6 +805,7 @@ def profile_case(args, device):
             iters, scales, wg, wf, feats = [10, 8, 5, 3], [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, True
         pyrs = _pyramids(pairs, scales)
         br = BatchRegistration(_estimators(iters, scales, wg, wf))
+        br.tile_config = args.schedule
         plan = br.prepare([p[0] for p in pyrs], [p[1] for p in pyrs],
                           [p[2] for p in pyrs] if feats else None,
                           [p[3] for p in pyrs] if feats else None)

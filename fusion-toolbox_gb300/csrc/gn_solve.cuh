@@ -381,9 +381,10 @@ __device__ inline bool warp_gn_update_dw(const float2 *up, const float2 *bv, con
 // Every FP64 warp instruction occupies its sub-partition's FP64 pipe for
 // many cycles whatever its lanes, so the layout makes each instruction do
 // the work of many lanes: one lane per entry of the 6x6 lower triangle plus
-// one per right-hand-side entry, an LDL^T factorisation (no square roots)
-// whose column step is one multiply and one FMA for all entries, and the
-// three exponential coefficients at once on three lane groups.
+// one per right-hand-side entry, a division-free symmetric elimination
+// whose column step is one multiply and one FMA for all entries (the six
+// reciprocals taken at once at the end), and the three exponential
+// coefficients at once on three lane groups.
 // ---------------------------------------------------------------------------
 
 // 1 / d for d > 0: rcp.approx.ftz.f64 (relative error below 2^-22) and one
@@ -400,13 +401,6 @@ __device__ __forceinline__ double rcp_fp64(double d) {
   return fma(y, fma(e, e, e), y);
 }
 
-// d > 0 on the integer bits (false for +-0, negatives and NaN; +inf passes,
-// as the comparison does).
-__device__ __forceinline__ bool positive_bits64(double d) {
-  const long long b = __double_as_longlong(d);
-  return b > 0 && b <= 0x7ff0000000000000ll;
-}
-
 // Maclaurin coefficient n (in t^2) of A = sin t / t (which = 0),
 // B = (1 - cos t) / t^2 (1) or C = (t - sin t) / t^3 (2): (-1)^n / (2n + 1 +
 // which)!, n < 8.  n is a compile-time constant, which a per-lane select.
@@ -420,14 +414,44 @@ __device__ __forceinline__ double se3_series_coeff(int which) {
   return which == 0 ? ca : (which == 1 ? cb : cc);
 }
 
+// v * 2^-e on the bits (integer instructions only): exact for a normal v
+// whose result stays normal; zeros, subnormals, infinities and NaN pass
+// unchanged, a result below the normal range flushes to a signed zero and
+// one above it becomes a signed infinity.
+__device__ __forceinline__ double scale_pow2(double v, int e) {
+  int hi = __double2hiint(v), lo = __double2loint(v);
+  const int ef = (hi >> 20) & 0x7ff, nf = ef - e;
+  if (ef != 0 && ef != 0x7ff) {
+    if (nf <= 0) {
+      hi &= (int)0x80000000u;
+      lo = 0;
+    } else if (nf >= 0x7ff) {
+      hi = (hi & (int)0x80000000u) | 0x7ff00000;
+      lo = 0;
+    } else {
+      hi -= e * (1 << 20);
+    }
+  }
+  return __hiloint2double(hi, lo);
+}
+
 // One Gauss-Newton update by one warp (all 32 lanes call it), in FP64.
 //   up: the 21 packed upper-triangle entries of J^T J, bv: J^T r (6),
 //   T: the current pose (16, row-major); all in shared memory.
-// Solves J^T J x = J^T r by LDL^T with the failure rule of LAPACK potrf (a
-// pivot that is not > 0, or NaN, fails: the LDL^T pivots are the squares of
-// the Cholesky pivots), then Tn = exp(x) T.  Returns the solve status
-// (warp-uniform); on success lanes 0..15 hold Tn's entries in tn_out (lane
-// k -> entry k), and every lane holds x in xs.
+// Solves J^T J x = J^T r, then Tn = exp(x) T.  The solve is Gaussian
+// elimination in its division-free symmetric form: column j replaces every
+// later row i by p_j row_i - a_ij row_j (p_j the pivot), which keeps the
+// trailing block symmetric (p_j times the Schur complement of LDL^T), and
+// scales the block by the power of two nearest below p_j so its entries stay
+// near the Schur complement's size.  So each column costs one multiply and
+// one FMA, and the pivots differ from the LDL^T pivots (the squares of the
+// Cholesky pivots) by positive factors only: the failure rule stays that of
+// LAPACK potrf (a pivot that is not > 0, or NaN, fails; one below the
+// normal range fails too).  The six rows are then divided by their pivots
+// at once (one reciprocal for all), and back substitution runs on the unit
+// upper triangle.  Returns the solve status (warp-uniform); on success
+// lanes 0..15 hold Tn's entries in tn_out (lane k -> entry k), and every
+// lane holds x in xs.
 __device__ inline bool warp_gn_update(const double *up, const double *bv, const double *T,
                                       double *xs, double &tn_out, int lane) {
   const unsigned full = 0xffffffffu;
@@ -451,25 +475,38 @@ __device__ inline bool warp_gn_update(const double *up, const double *bv, const 
   if (is_tri) v = up[upper_index(ek, ei)];
   if (is_rhs) v = bv[ei];
   bool ok = true;
-  // forward: LDL^T factorisation with L z = b and y = D^-1 z fused in
+  // forward: division-free elimination of the lower triangle and the
+  // right-hand side (column j's entries keep their values: they are row j of
+  // the upper triangle)
 #pragma unroll
   for (int j = 0; j < 6; ++j) {
     const double piv = __shfl_sync(full, v, tri_lane(j, j));
-    ok = ok && positive_bits64(piv);
-    const double inv = rcp_fp64(piv);
+    const long long pb = __double_as_longlong(piv);
+    ok = ok && pb >= 0x0010000000000000ll && pb < 0x7ff0000000000000ll;
+    if (j == 5) break;
     const int src_i = (ei >= j) ? tri_lane(ei, j) : 0;
     const int src_k = is_rhs ? 21 + j : ((ek >= j && ek < 6) ? tri_lane(ek, j) : 0);
     const double aij = __shfl_sync(full, v, src_i);
     const double akj = __shfl_sync(full, v, src_k);
-    const bool own_y = is_rhs && ei == j;
-    const double t = (own_y ? v : aij) * inv;  // L_ij, or y_j on the rhs lane j
     const bool upd = (is_tri && ek > j && ei >= ek) || (is_rhs && ei > j);
-    const double nv = fma(-t, akj, v);
+    // (piv v - aij akj) 2^-pe with piv in [2^pe, 2^(pe+1)): the pivot's
+    // exponent field set to 1023 and aij scaled on the bits while the
+    // multiply runs
+    const int pe = (int)(pb >> 52) - 1023;
+    const double pn = __longlong_as_double((pb & 0x000fffffffffffffll) | 0x3ff0000000000000ll);
+    const double nv = fma(-scale_pow2(aij, pe), akj, pn * v);
     if (upd) v = nv;
-    if ((is_tri && ek == j && ei > j) || own_y) v = t;
   }
   if (!ok) return false;
-  // backward: L^T x = y; rhs lane i ends with x_i
+  // rows to unit pivots: lane (i, k) of the triangle holds U_ki, the right-
+  // hand-side lane i holds c_i; both divide by row k's (or i's) pivot
+  {
+    const double rr = rcp_fp64(v);  // meaningful on the diagonal lanes
+    const int row = is_rhs ? ei : ek;
+    const double r = __shfl_sync(full, rr, tri_lane(row, row));
+    v *= r;
+  }
+  // backward: U x = c on the unit upper triangle; rhs lane i ends with x_i
 #pragma unroll
   for (int j = 5; j >= 0; --j) {
     const double xj = __shfl_sync(full, v, 21 + j);
@@ -481,13 +518,14 @@ __device__ inline bool warp_gn_update(const double *up, const double *bv, const 
       if (is_rhs && ei < j) v = nv;
     }
   }
-  // exp(x).  The coefficients A on lanes 0..9, B on 10..19, C on 20..31, by
-  // Estrin's scheme, from their Maclaurin series in t^2: below t^2 = 2^-14
-  // (a rotation update under 0.45 degrees, the usual case after the first
-  // iterations) through t^6, the first omitted term being below
-  // 2^-56 / 9! < 4e-23 of the sum; below t = 0.5 through t^14 (the first
-  // omitted term below 0.5^16 / 17! < 5e-20); above, the closed forms of
-  // se3_coeffs.
+  // exp(x).  The coefficients A on lanes 0..9, B on 10..19, C on 20..31,
+  // from their Maclaurin series in t^2: below t^2 = 2^-14 (a rotation
+  // update under 0.45 degrees, the usual case after the first iterations)
+  // through t^4 by Horner's rule, the series alternating and the first
+  // omitted term (t^6 / 7!, t^6 / 8!, t^6 / 9!) below 2^-42 / 5040 < 4.6e-17,
+  // under half an ulp of A, B and C (A near 1, B near 1/2, C near 1/6);
+  // below t = 0.5 through t^14 by Estrin's scheme (the first omitted term
+  // below 0.5^16 / 17! < 5e-20); above, the closed forms of se3_coeffs.
   const double wx = xs[3], wy = xs[4], wz = xs[5];
   const double t2 = fma(wx, wx, fma(wy, wy, wz * wz));
   double A, B, C;
@@ -496,10 +534,8 @@ __device__ inline bool warp_gn_update(const double *up, const double *bv, const 
   const long long t2b = __double_as_longlong(t2);
   if (t2b < 0x3F10000000000000ll) {  // t2 < 2^-14
     const int which = lane < 10 ? 0 : (lane < 20 ? 1 : 2);
-    const double u2 = t2 * t2;
-    const double a01 = fma(se3_series_coeff<1>(which), t2, se3_series_coeff<0>(which));
-    const double a23 = fma(se3_series_coeff<3>(which), t2, se3_series_coeff<2>(which));
-    const double coef = fma(u2, a23, a01);
+    const double coef = fma(fma(se3_series_coeff<2>(which), t2, se3_series_coeff<1>(which)), t2,
+                            se3_series_coeff<0>(which));
     A = __shfl_sync(full, coef, 0);
     B = __shfl_sync(full, coef, 10);
     C = __shfl_sync(full, coef, 20);

@@ -62,11 +62,15 @@ def rel_pose(a, b):
     return np.linalg.norm(d) / max(np.linalg.norm(io.se3_log(b)), 1e-3)
 
 
-def compare_forced(hist, d, x, kw, init=None, channel_mode="last", tol=1e-5):
+def compare_forced(hist, d, x, kw, init=None, channel_mode="last", tol=1e-5, step_tol=1e-11):
     """Teacher-forced comparison of a GPU history (``ICPOdometry.last_history``)
     with the oracle's step evaluated at the GPU's previous pose; ``x`` holds
-    the device feature maps as used (``sf``/``tf``).  Returns the worst pose
-    error."""
+    the device feature maps as used (``sf``/``tf``).  Each iteration's device
+    solve and update are also checked on their own inputs: the oracle's FP64
+    Cholesky solve and exponential of the device's recorded J^T J and J^T r,
+    applied to the device's previous pose, must give the device's pose within
+    ``step_tol`` (largest entry difference over the largest entry).  Returns
+    the worst pose error."""
     from oracle import icp_oracle as io
     from slamtb_gb300 import _native as N
     s, t = d["src"], d["tgt"]
@@ -94,6 +98,11 @@ def compare_forced(hist, d, x, kw, init=None, channel_mode="last", tol=1e-5):
         assert abs(g[N.HIST_R2] - o["r2"]) <= tol * o["r2"], k
         err = rel_pose(T, o["transform"])
         assert err <= tol, (k, err)
+        ok_own, x_own = io.cholesky_solve6(A, b)
+        assert ok_own, k
+        T_own = io.se3_exp(x_own) @ T_prev
+        step_err = np.abs(T - T_own).max() / np.abs(T_own).max()
+        assert step_err <= step_tol, (k, step_err)
         worst = max(worst, err)
         T_prev = T
     return worst

@@ -110,6 +110,19 @@ def test_geometric_matches_oracle_per_iteration(cuda, pair0, launch, use_graph):
 
 
 @pytest.mark.parametrize("launch", ["single", "multi"])
+def test_double_word_solve_option(cuda, pair0, launch):
+    """solve_precision="dw" (STB_OPT_DW_SOLVE): the Gauss-Newton step in
+    double-word float32 (~48 bits) stays within the 1e-5 gate, and within
+    1e-9 of the FP64 step on its own sums."""
+    from slamtb_gb300.registration.icp import ICPOdometry
+    x = _dev(pair0, cuda)
+    x.pop("sf"), x.pop("tf")
+    icp = ICPOdometry(record_history=True, launch=launch, solve_precision="dw", **GEOM)
+    _run_gpu(x, icp)
+    compare_forced(icp.last_history, pair0, x, GEOM, step_tol=1e-9)
+
+
+@pytest.mark.parametrize("launch", ["single", "multi"])
 def test_hybrid_matches_oracle_per_iteration(cuda, pair0, launch):
     from slamtb_gb300.registration.icp import ICPOdometry
     kw = dict(GEOM, feat_weight=0.1)
