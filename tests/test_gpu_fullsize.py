@@ -10,6 +10,10 @@ do not need the oracle to run every pair:
   [10, 8, 5, 3]: every pair registers and pair 0 passes the gate on the
   three coarse levels and the first two iterations of the finest.
 
+Both run under the lock-step schedule (BatchRegistration's default) and
+under the grouped schedule the autotuner picks for each in the benchmark
+(19 groups for the uneven pairs, 4 for the 1080p pairs).
+
 Inputs are rendered and prepared on the device; the oracle sees the same
 float32 point grids and the BF16 feature values as float32.
 """
@@ -76,7 +80,8 @@ def _estimators(iters, scales, wg, wf):
                             normals_angle_thresh=ANGLE)) for s, n in zip(scales, iters)]
 
 
-def test_256_uneven_pairs_full_size(cuda):
+@pytest.mark.parametrize("schedule", [0, 119])
+def test_256_uneven_pairs_full_size(cuda, schedule):
     from slamtb_gb300.registration import BatchRegistration
     rng = np.random.default_rng(7)
     sizes = [(160, 120), (320, 240), (640, 480), (848, 480), (1280, 720)]
@@ -84,6 +89,7 @@ def test_256_uneven_pairs_full_size(cuda):
     pairs = [_device_pair(cuda, 1000 + k, *sizes[i]) for k, i in enumerate(pick)]
     iters, scales = [10, 5, 3], [1.0, 0.5, 0.5]
     br = BatchRegistration(_estimators(iters, scales, 1.0, 0.0), record_history=True)
+    br.tile_config = schedule
     spyrs = [p["src"].pyramid(scales) for p in pairs]
     tpyrs = [p["tgt"].pyramid(scales) for p in pairs]
     res = br.estimate_pyramids(spyrs, tpyrs)
@@ -97,13 +103,15 @@ def test_256_uneven_pairs_full_size(cuda):
         _check(br.last_history[k], spyrs[k], tpyrs[k], iters, kw)
 
 
-def test_16_pairs_1080p_16_channel_bf16_full_size(cuda):
+@pytest.mark.parametrize("schedule", [0, 104])
+def test_16_pairs_1080p_16_channel_bf16_full_size(cuda, schedule):
     from slamtb_gb300.processing import feature_pyramid
     from slamtb_gb300.registration import BatchRegistration
     iters, scales = [10, 8, 5, 3], [1.0, 0.5, 0.5, 0.5]
     pairs = [_device_pair(cuda, 2000 + k, 1920, 1080, channels=16, max_rot_deg=10.0,
                           max_trans=0.1) for k in range(16)]
     br = BatchRegistration(_estimators(iters, scales, 10.0, 1.0), record_history=True)
+    br.tile_config = schedule
     spyrs = [p["src"].pyramid(scales) for p in pairs]
     tpyrs = [p["tgt"].pyramid(scales) for p in pairs]
     sfps = [feature_pyramid(p["sf"], scales) for p in pairs]
