@@ -22,8 +22,8 @@ from .result import RegistrationResult
 # 0..5 the lock-step kernel's work-item sizes, GROUPED + g the grouped
 # kernel with g groups.
 GROUPED = 100
-TUNE_CONFIGS = (0, 1, 2, 3, 4, 5, GROUPED + 2, GROUPED + 4, GROUPED + 8, GROUPED + 19,
-                GROUPED + 38, GROUPED + 76)
+TUNE_CONFIGS = (0, 1, 2, 3, 4, 5, GROUPED + 1, GROUPED + 2, GROUPED + 4, GROUPED + 8,
+                GROUPED + 19, GROUPED + 38, GROUPED + 76)
 
 
 class BatchPlan:
