@@ -5,10 +5,11 @@ GPU's own previous pose (teacher forcing, the 1e-5 gate of
 ``_helpers.compare_forced``), for uneven resolutions, three levels and the
 hybrid geometric + feature term; failures stay inside their pair; the
 reference's level hand-over (identity after a failed first iteration,
-multiscale.py:64-65) is reproduced.  Each check runs under three schedules:
-the lock-step kernel, and the grouped kernel with three groups (so that
-the grid's blocks past the last whole group stay idle) and with 76 groups
-of two blocks (more groups than pairs).
+multiscale.py:64-65) is reproduced.  Each check runs under four schedules:
+the lock-step kernel, and the grouped kernel with one group (the whole
+grid on each pair in turn), three groups (so that the grid's blocks past
+the last whole group stay idle) and 76 groups of two blocks (more groups
+than pairs).
 """
 import math
 
@@ -24,7 +25,7 @@ pytestmark = pytest.mark.gpu
 
 SCALES = [1.0, 0.5, 0.5]
 ITERS = [6, 4, 3]  # finest first
-SCHEDULES = [0, 103, 176]  # lock-step (8192-pixel work items); grouped, 3 and 76 groups
+SCHEDULES = [0, 101, 103, 176]  # lock-step (8192-pixel work items); grouped, 1, 3 and 76 groups
 
 
 def _kw(n, wf, wg=1.0):
