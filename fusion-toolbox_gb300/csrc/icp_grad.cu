@@ -109,7 +109,7 @@ __device__ __forceinline__ float3 source_point(const LossArgs &a, float z, int i
 // gather round trip per round instead of one per pixel.  The pixels of a
 // thread keep the grid-stride order, so sums are the same bits.  Two
 // pixels keep 4-5 blocks of 256 resident per SM (the register caps of the
-// launch bounds: k_g_assoc 64 without one, k_g_adjoint 64, k_g_loss 48);
+// launch bounds: k_g_assoc 64, k_g_adjoint 64, k_g_loss 48);
 // four pixels need about 115 registers and halve the occupancy, which
 // costs more than the extra loads in flight win.
 constexpr int kP = 2;
@@ -132,7 +132,7 @@ __device__ __forceinline__ void load_sources(const LossArgs &a, size_t po, int n
   }
 }
 
-__global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long long *keys_all,
+__global__ void __launch_bounds__(kT, 4) k_g_assoc(const LossArgs a, unsigned long long *keys_all,
                                                 float thr2, float cos_max) {
   __shared__ Pose32 P;
   const double pose_entry = pose_load(a);
@@ -164,15 +164,19 @@ __global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long 
       ok[k] = S.ok[k] && round_in(u, W, ui) && round_in(v, H, vi);
       pix[k] = ok[k] ? vi * W + ui : 0;
     }
-    float q[kP][3], m[kP][3];
+    // (the source normals go out with the gathers: one round trip)
+    float q[kP][3], m[kP][3], ns[kP][3];
     bool tv[kP];
 #pragma unroll
     for (int k = 0; k < kP; ++k) {
+      const int i = i0 + k * stride;
+      const int ic = i < npix ? i : 0;
       tv[k] = tm[pix[k]];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         q[k][d] = tp[3 * pix[k] + d];
         m[k][d] = tn[3 * pix[k] + d];
+        ns[k][d] = sn[3 * ic + d];
       }
     }
     // the gates and the z-buffer
@@ -184,12 +188,8 @@ __global__ void __launch_bounds__(kT) k_g_assoc(const LossArgs a, unsigned long 
                   dz = fsub(q[k][2], Tp[k].z);
       const float sq = dot3(dx, dy, dz, dx, dy, dz);
       if (sq > thr2) continue;
-      const float3 Tn = transform_normal(P.nm, sn[3 * i], sn[3 * i + 1], sn[3 * i + 2]);
-      const float nx = m[k][0], ny = m[k][1], nz = m[k][2];
-      const float c = fdiv(dot3(Tn.x, Tn.y, Tn.z, nx, ny, nz),
-                           fmul(__fsqrt_rn(dot3(Tn.x, Tn.y, Tn.z, Tn.x, Tn.y, Tn.z)),
-                                __fsqrt_rn(dot3(nx, ny, nz, nx, ny, nz))));
-      if (c >= -1.0f && c <= cos_max) continue;
+      const float3 Tn = transform_normal(P.nm, ns[k][0], ns[k][1], ns[k][2]);
+      if (normal_angle_rejects(Tn, m[k][0], m[k][1], m[k][2], cos_max)) continue;
       atomicMin(keys + pix[k], ((unsigned long long)kTag << 56) |
                                    ((unsigned long long)__float_as_uint(__fsqrt_rn(sq)) << 24) |
                                    (unsigned long long)i);
