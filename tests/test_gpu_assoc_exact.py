@@ -20,7 +20,8 @@ frames (0 -> 3, and 0 / 13 with the thresholds of its
 ``test_correspondence_map.py``), a BF16 16-channel hybrid registration, ties
 between duplicated source points (the smaller index wins), source points of
 NaN depth (never match), three pairs of an uneven multiscale batch at every
-level, and a batch of the differentiable loss.
+level, a 1280x960 pair with more source rounds than the shared-memory
+cache holds, and a batch of the differentiable loss.
 """
 import math
 
@@ -163,6 +164,15 @@ def test_fused_association_ties_and_nan_sources(cuda, pair0):
         assert not ((rows >= 100) & (rows < 140)).any()
 
 
+def test_fused_association_streamed_rounds(cuda):
+    """1280x960 (1,228,800 source points, four rounds of 2048 points a block
+    on 152 blocks): more rounds than the source cache holds, so the rounds
+    past it read their source points from global memory; the maps at
+    iterations 0, 1 and 3 against the oracle."""
+    d = synthetic_pair(5, width=1280, height=960)
+    _check_iterations(cuda, d, [0, 1, 3], 0.1, ANGLE_20)
+
+
 # ---------------------------------------------------------------------------
 # batched persistent kernel
 # ---------------------------------------------------------------------------
@@ -187,13 +197,14 @@ def _batch_pairs(cuda):
     return pairs
 
 
-@pytest.mark.parametrize("schedule", [0, 103])
+@pytest.mark.parametrize("schedule", [0, 103, 176])
 @pytest.mark.parametrize("levels", [1, 2, 3])
 def test_batch_association_every_level(cuda, levels, schedule):
     """The coarsest `levels` levels of three uneven pairs in one batch; the
     last of them runs k iterations, so the final association is at that
     level's k-th pose.  Under the lock-step schedule and the grouped one
-    (three groups)."""
+    (three groups of 50 blocks; 76 groups of 2, where a 640x480 level
+    spans 75 rounds a block, past the source cache)."""
     from slamtb_gb300 import _native as N
     from slamtb_gb300.registration import BatchRegistration, ICPOdometry
     pairs = _batch_pairs(cuda)
