@@ -360,20 +360,28 @@ def _oracle_jobs(pyrs, iters, wg, wf, mode):
     return jobs
 
 
-def _oracle_errors(results, jobs, workers):
-    """Each pair's free-running final-pose error of the GPU result against
-    the FP64 oracle's registration from the same start (||log(T_o^-1 T)||
-    over max(||log T_o||, 1e-3)), with the fraction within 1e-5 and the
-    three worst pairs with the condition number of their final J^T J."""
+def _oracle_runs(jobs, workers):
+    """The FP64 oracle's free-running registration of every job, in spawned
+    processes: [(final transform or None, cond(J^T J))]."""
     import multiprocessing as mp
     with mp.get_context("spawn").Pool(workers) as pool:
-        outs = list(pool.imap(_oracle_worker, jobs, chunksize=1))
+        return list(pool.imap(_oracle_worker, jobs, chunksize=1))
+
+
+def _error_table(transforms, outs):
+    """Each pair's free-running final-pose error against the FP64 oracle's
+    registration from the same start (||log(T_o^-1 T)|| over
+    max(||log T_o||, 1e-3)), with the fractions within 1e-5 and 1e-3 and the
+    three worst pairs with the condition number of their final J^T J.
+    ``transforms``: 4x4 arrays or tensors (None for a failed pair), pair k
+    against outs[k]."""
+    import numpy as np
     errs = []
-    for k, (r, (To, cond)) in enumerate(zip(results, outs)):
-        if r.transform is None or To is None:
-            errs.append((k, None if (r.transform is None) == (To is None) else math.inf, cond))
+    for k, (T, (To, cond)) in enumerate(zip(transforms, outs)):
+        if T is None or To is None:
+            errs.append((k, None if (T is None) == (To is None) else math.inf, cond))
             continue
-        errs.append((k, _rel_pose(r.transform.numpy(), To), cond))
+        errs.append((k, _rel_pose(np.asarray(T, dtype=np.float64), To), cond))
     vals = [e for _, e, _ in errs if e is not None]
     worst = sorted([x for x in errs if x[1] is not None], key=lambda x: -x[1])[:3]
     return {"pairs": len(errs), "both_failed": sum(1 for _, e, _ in errs if e is None),
@@ -382,6 +390,31 @@ def _oracle_errors(results, jobs, workers):
             "within_1e-5": sum(1 for v in vals if v <= 1e-5) / max(len(vals), 1),
             "within_1e-3": sum(1 for v in vals if v <= 1e-3) / max(len(vals), 1),
             "worst": [{"pair": k, "err": e, "cond_JtJ": c} for k, e, c in worst]}
+
+
+def _reference_arithmetic(jobs, outs, max_pairs):
+    """The reference CPU path's own free-running accuracy on the first
+    ``max_pairs`` jobs: the C/OpenMP port (float32 per-point partials in the
+    reference's operation order, FP64 sums and solve) registers each pair
+    from the same start, and its final pose is compared with the FP64
+    oracle's as the GPU results are.  This is the floor a drop-in that
+    reproduces the reference's float32 arithmetic starts from."""
+    from oracle import port
+    t0 = time.perf_counter()
+    Ts = []
+    for levels, ests, mode in jobs[:max_pairs]:
+        r = port.multiscale_estimate(levels, [dict(e, channel_mode=mode) for e in ests])
+        Ts.append(r["transform"])
+    table = _error_table(Ts, outs[:max_pairs])
+    table["wall_s"] = time.perf_counter() - t0
+    table["threads"] = port.max_threads()
+    return table
+
+
+def _oracle_errors(results, jobs, workers):
+    """_error_table of registration results (objects with .transform)
+    against a fresh FP64 oracle run of the jobs."""
+    return _error_table([r.transform for r in results], _oracle_runs(jobs, workers))
 
 
 def _alg_bytes_batch(pyrs, iters, feat_bytes=0):
@@ -442,7 +475,7 @@ def _compare(batch_res, plain_T):
 
 
 def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps_plain,
-                    feat_bytes=0, mode="last", oracle_workers=0):
+                    feat_bytes=0, mode="last", oracle_workers=0, reference_pairs=0):
     from slamtb_gb300.registration import BatchRegistration, MultiscaleRegistration
     ests = _estimators(iters, scales, wg, wf)
     pyrs = _pyramids(pairs, scales)
@@ -462,12 +495,16 @@ def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps
     peak, kind = measured_peak()
     gt_err = [_rel_pose(r.transform.numpy(), p[4]) if r.transform is not None else None
               for r, p in zip(res, pairs)]
-    vs_oracle = None
+    vs_oracle = plain_vs_oracle = ref_vs_oracle = None
     if oracle_workers:
         t0 = time.perf_counter()
-        vs_oracle = _oracle_errors(res, _oracle_jobs(pyrs, iters, wg, wf, mode),
-                                   oracle_workers)
+        jobs = _oracle_jobs(pyrs, iters, wg, wf, mode)
+        outs = _oracle_runs(jobs, oracle_workers)
+        vs_oracle = _error_table([r.transform for r in res], outs)
         vs_oracle["wall_s"] = time.perf_counter() - t0
+        plain_vs_oracle = _error_table(plain_T, outs)
+        if reference_pairs:
+            ref_vs_oracle = _reference_arithmetic(jobs, outs, reference_pairs)
     return {
         "workload": name, "pairs": B, "iters": iters, "scales": scales,
         "weights": {"geometric": wg, "feature": wf},
@@ -480,6 +517,8 @@ def _batch_vs_plain(name, pairs, iters, scales, wg, wf, device, reps_batch, reps
         "speedup_batch_vs_plain": t_plain / t_batch,
         "rel_pose_diff_batch_vs_plain": dict(zip(("max", "median"), _compare(res, plain_T))),
         "batch_vs_fp64_oracle": vs_oracle,
+        "plain_vs_fp64_oracle": plain_vs_oracle,
+        "reference_cpu_arithmetic_vs_fp64_oracle": ref_vs_oracle,
         "median_rel_pose_err_vs_ground_truth": statistics.median(
             [e for e in gt_err if e is not None]) if any(e is not None for e in gt_err) else None,
         "roofline": {"bound": "hbm", "kernel": "k_batch (whole run)",
@@ -511,8 +550,10 @@ def secondary_multiscale(device, seed):
     # both paths' free-running results against the FP64 oracle's
     jobs = _oracle_jobs(pyrs, iters, 1.0, 0.1, "last")
     plain_res = MultiscaleRegistration(ests).estimate_pyramid(*pyrs[0])
-    vs_oracle = {"plain": _oracle_errors([plain_res], jobs, 1),
-                 "batch": _oracle_errors(res, jobs, 1)}
+    outs = _oracle_runs(jobs, 1)
+    vs_oracle = {"plain": _error_table([plain_res.transform], outs),
+                 "batch": _error_table([res[0].transform], outs),
+                 "reference_cpu_arithmetic": _reference_arithmetic(jobs, outs, 1)}
     return {"workload": "multiscale hybrid ICP 640x480/320x240/160x120 [10, 5, 3], "
                         "geometric 1.0 + greyscale feature 0.1, 1 pair",
             "plain": {"registrations_per_s": 50 / t_plain,
@@ -588,7 +629,7 @@ def secondary_batch_uneven(device, seed, B=256):
     out = _batch_vs_plain("batched uneven ICP, 256 pairs from {160x120 ... 1280x720}, "
                           "3 levels [10, 5, 3], geometric", pairs, [10, 5, 3],
                           [1.0, 0.5, 0.5], 1.0, 0.0, device, 10, 2,
-                          oracle_workers=oracle_workers())
+                          oracle_workers=oracle_workers(), reference_pairs=B)
     out["size_histogram"] = {f"{w}x{h}": int((pick == i).sum()) for i, (w, h) in enumerate(sizes)}
     return out
 
@@ -601,7 +642,7 @@ def secondary_feature_1080p(device, seed, B=16):
     return _batch_vs_plain("high-resolution feature ICP, 16 pairs 1920x1080, 16 BF16 channels, "
                            "4 levels [10, 8, 5, 3]", pairs, [10, 8, 5, 3],
                            [1.0, 0.5, 0.5, 0.5], 10.0, 1.0, device, 5, 1, feat_bytes=32,
-                           oracle_workers=oracle_workers())
+                           oracle_workers=oracle_workers(), reference_pairs=4)
 
 
 def secondary_bilateral(device, seed, reps=200):
@@ -875,6 +916,15 @@ def summarize(sec):
                              "within_1e-3": _r(vo.get("within_1e-3")),
                              "worst": [{k: _r(v) for k, v in w.items()}
                                        for w in vo.get("worst", [])]} if vo else None}
+            # the same table, max / median / within 1e-5, for the plain path
+            # and for the reference CPU path's arithmetic (the port)
+            for key, src in (("plain_vs_fp64_oracle", "plain_vs_fp64_oracle"),
+                             ("reference_arith_vs_fp64_oracle",
+                              "reference_cpu_arithmetic_vs_fp64_oracle")):
+                t = d.get(src)
+                out[name][key] = {"pairs": t["pairs"], "max": _r(t["max"]),
+                                  "median": _r(t["median"]),
+                                  "within_1e-5": _r(t["within_1e-5"])} if t else None
         elif name == "loss_grad_32x640x480":
             out[name] = {"pairs_per_s": _r(d["pairs_per_s"]), "frac": _r(d["roofline"]["frac"])}
         elif name == "plain_kernels_larger_images":

@@ -54,3 +54,22 @@ def icp_estimate(kcam, src_points, src_normals, src_mask, tgt_points, tgt_normal
     return dict(transform=T.reshape(4, 4) if iters.value else None,
                 information=info.reshape(6, 6), residual=res.value, match_ratio=ratio.value,
                 iters=iters.value)
+
+
+def multiscale_estimate(levels, estimators, transform=None, threads=0):
+    """``MultiscaleRegistration.estimate_frame`` (multiscale.py:30-67) on the
+    port: ``levels`` coarsest first, ``estimators`` finest first, as
+    ``icp_oracle.multiscale_estimate``, with the same hand-over (a level
+    whose first iteration fails passes identity on, multiscale.py:64-65).
+    The port computes the reference's float32 per-point partials, so its
+    free-running result carries the reference's own arithmetic; the numpy
+    oracle's FP64 terms are the error reference it is compared with.
+    Returns the finest level's result dict."""
+    result = None
+    for level, est in zip(levels, estimators[::-1]):
+        kw = {k: v for k, v in est.items() if k != "channel_mode"}
+        if est.get("channel_mode", "last") != "last":
+            raise ValueError("the port follows the reference's 'last' channel mode only")
+        result = icp_estimate(transform=transform, threads=threads, **level, **kw)
+        transform = result["transform"]
+    return result
