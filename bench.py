@@ -607,9 +607,10 @@ def secondary_loss(device, seed, B=32):
     t = a.elapsed_time(b) / 1e3 / reps
     npx = B * H * W
     # forward: assoc 50 B/px (depth, normal, masks, target point+normal,
-    # key) + key init 8 + loss 36; backward: 36 + depth-gradient init and
-    # write 8
-    alg = npx * (50 + 8 + 36 + 44)
+    # key) + key init 8 + the loss with its adjoint at a unit output
+    # gradient 36 (key, winner depth, target point + normal) + the depth
+    # adjoint's init 4; backward: the depth adjoint scaled, read 4 + write 4
+    alg = npx * (50 + 8 + 36 + 4 + 8)
     peak, kind = measured_peak()
     return {"workload": f"point-to-plane loss forward + backward, {B} pairs 640x480 at the "
                         "poses of 5 GN iterations", "pairs": B,

@@ -288,17 +288,29 @@ __device__ __forceinline__ float round_residual(const LossArgs &a, const Pose32 
               n.z);
 }
 
-__global__ void __launch_bounds__(kT, 5) k_g_loss(const LossArgs a,
-                                               const unsigned long long *keys_all, float *part,
-                                               unsigned *tickets, double *loss) {
+// The loss of every pair, and with kAdj its adjoint at a unit output
+// gradient in the same pass (the tangent sums -2 sum r J and the depth
+// adjoint -2 r (R^T n).d at each matched source pixel), so that a backward
+// pass only scales them by dL/dL_p (k_g_scale) instead of reading the
+// correspondences, the gathers and the target frame again.  The adjoint
+// terms use k_g_adjoint's expressions with its factor -2 g at g = 1, so at
+// a unit output gradient the two give the same bits.
+template <bool kAdj>
+__global__ void __launch_bounds__(kT, kAdj ? 4 : 5)
+    k_g_loss(const LossArgs a, const unsigned long long *keys_all, float *part,
+             unsigned *tickets, double *loss, double *tangent, float *depth_adj) {
   __shared__ Pose32 P;
   __shared__ double tot[8];
+  constexpr int kN = kAdj ? 7 : 1;
   const double pose_entry = pose_load(a);
   const int npix = a.H * a.W;
   const size_t po = (size_t)blockIdx.y * npix;
   const unsigned long long *keys = keys_all + po;
+  float *gz = (kAdj && depth_adj) ? depth_adj + po : nullptr;
   const int stride = gridDim.x * kT;
-  CSum acc[1] = {{0.f, 0.f}};
+  CSum acc[kN];
+#pragma unroll
+  for (int k = 0; k < kN; ++k) acc[k] = {0.f, 0.f};
   int p0 = blockIdx.x * kT + threadIdx.x;
   Round R;
   load_round(a, po, npix, keys, p0, stride, R);  // in flight across the barrier
@@ -310,12 +322,63 @@ __global__ void __launch_bounds__(kT, 5) k_g_loss(const LossArgs a,
       float3 Tp, n;
       const float r = round_residual(a, P, R, k, Tp, n);
       csum_add(acc[0], r * r);
+      if (kAdj) {
+        const int i = R.i[k];
+        const float Jv[6] = {n.x, n.y, n.z, Tp.y * n.z - Tp.z * n.y, Tp.z * n.x - Tp.x * n.z,
+                             Tp.x * n.y - Tp.y * n.x};
+        const float s = -2.f * r;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) csum_add(acc[1 + c], s * Jv[c]);
+        if (gz) {
+          const float *Rt = P.rt;
+          const float rn0 = Rt[0] * n.x + Rt[4] * n.y + Rt[8] * n.z;
+          const float rn1 = Rt[1] * n.x + Rt[5] * n.y + Rt[9] * n.z;
+          const float rn2 = Rt[2] * n.x + Rt[6] * n.y + Rt[10] * n.z;
+          const float d0 = ((float)(i % a.W) - P.cx) / P.fx,
+                      d1 = ((float)(i / a.W) - P.cy) / P.fy;
+          gz[i] = s * (rn0 * d0 + rn1 * d1 + rn2);
+        }
+      }
     }
     p0 += stride * kP;
     if (p0 >= npix) break;
     load_round(a, po, npix, keys, p0, stride, R);
   }
-  if (pair_fold<1>(acc, part, tickets, tot) && threadIdx.x == 0) loss[blockIdx.y] = tot[0];
+  if (pair_fold<kN>(acc, part, tickets, tot)) {
+    if (threadIdx.x == 0) loss[blockIdx.y] = tot[0];
+    if (kAdj && threadIdx.x < 6) tangent[blockIdx.y * 6 + threadIdx.x] = tot[1 + threadIdx.x];
+  }
+}
+
+// Backward of the fused forward: grad_tangent[p] = g_p tangent[p] (FP64) and
+// grad_depth[p][i] = (float)g_p depth_adj[p][i], g_p = grad_loss[p]; 16-byte
+// vectors where a pair's pixels start on a 16-byte boundary.
+__global__ void k_g_scale(const double *grad_loss, const double *tangent,
+                          const float *depth_adj, int npix, double *grad_tangent,
+                          float *grad_depth) {
+  const int p = blockIdx.y;
+  const double g = grad_loss[p];
+  if (grad_tangent && blockIdx.x == 0 && threadIdx.x < 6)
+    grad_tangent[p * 6 + threadIdx.x] = g * tangent[p * 6 + threadIdx.x];
+  if (!grad_depth) return;
+  const float gf = (float)g;
+  const size_t po = (size_t)p * npix;
+  const float *src = depth_adj + po;
+  float *dst = grad_depth + po;
+  const int stride = gridDim.x * blockDim.x;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((((uintptr_t)src | (uintptr_t)dst) & 15) == 0) {
+    const int n4 = npix >> 2;
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+    float4 *d4 = reinterpret_cast<float4 *>(dst);
+    for (int k = t; k < n4; k += stride) {
+      const float4 v = __ldcs(s4 + k);
+      __stcs(d4 + k, make_float4(gf * v.x, gf * v.y, gf * v.z, gf * v.w));
+    }
+    for (int k = 4 * n4 + t; k < npix; k += stride) dst[k] = gf * src[k];
+  } else {
+    for (int k = t; k < npix; k += stride) dst[k] = gf * src[k];
+  }
 }
 
 __global__ void __launch_bounds__(kT, 4) k_g_adjoint(const LossArgs a,
@@ -569,9 +632,65 @@ extern "C" int stb_icp_loss_forward(const float *src_depth, const float *src_nor
   const dim3 grid(blocks_x(npix), num_pairs);
   k_g_assoc<<<grid, kT, 0, st>>>(a, keys, distance_thresh_sq(distance_thresh),
                                  angle_cos_max(normal_angle_thresh));
-  k_g_loss<<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
-                                reinterpret_cast<unsigned *>(ws + g.tickets), loss);
+  k_g_loss<false><<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
+                                       reinterpret_cast<unsigned *>(ws + g.tickets), loss,
+                                       nullptr, nullptr);
   return check_launch("stb_icp_loss_forward");
+}
+
+extern "C" int stb_icp_loss_forward_adjoint(
+    const float *src_depth, const float *src_normals, const uint8_t *src_mask,
+    const float *tgt_points, const float *tgt_normals, const uint8_t *tgt_mask,
+    int32_t num_pairs, int32_t height, int32_t width, float fx, float fy, float cx, float cy,
+    const double *poses, double distance_thresh, double normal_angle_thresh, void *workspace,
+    size_t workspace_bytes, double *loss, double *tangent, float *depth_adjoint,
+    void *stream) {
+  clear_error();
+  const LossArgs a = loss_args(src_depth, src_normals, src_mask, tgt_points, tgt_normals,
+                               tgt_mask, num_pairs, height, width, fx, fy, cx, cy, poses);
+  STB_TRY(check_loss_args(a, workspace, workspace_bytes));
+  STB_TRY(check_device_ptr(loss, "loss"));
+  STB_TRY(check_device_ptr(tangent, "tangent"));
+  STB_TRY(check_device_ptr(depth_adjoint, "depth_adjoint", true));
+  const int64_t npix = (int64_t)height * width;
+  const GradLayout g = grad_layout(num_pairs, npix);
+  char *ws = static_cast<char *>(workspace);
+  const cudaStream_t st = as_stream(stream);
+  unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + g.keys);
+  cudaMemsetAsync(ws + g.tickets, 0, sizeof(unsigned) * (size_t)num_pairs, st);
+  cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * (size_t)num_pairs * npix, st);
+  if (depth_adjoint)
+    cudaMemsetAsync(depth_adjoint, 0, sizeof(float) * (size_t)num_pairs * npix, st);
+  const dim3 grid(blocks_x(npix), num_pairs);
+  k_g_assoc<<<grid, kT, 0, st>>>(a, keys, distance_thresh_sq(distance_thresh),
+                                 angle_cos_max(normal_angle_thresh));
+  k_g_loss<true><<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
+                                      reinterpret_cast<unsigned *>(ws + g.tickets), loss,
+                                      tangent, depth_adjoint);
+  return check_launch("stb_icp_loss_forward_adjoint");
+}
+
+extern "C" int stb_icp_loss_scale_adjoint(const double *grad_loss, const double *tangent,
+                                          const float *depth_adjoint, int32_t num_pairs,
+                                          int32_t height, int32_t width, double *grad_tangent,
+                                          float *grad_depth, void *stream) {
+  clear_error();
+  if (num_pairs <= 0 || height <= 0 || width <= 0)
+    return fail(STB_EINVAL, "Check failed: sizes must be positive, got %d pairs of %dx%d",
+                num_pairs, height, width);
+  if ((int64_t)height * width >= (1ll << 24))
+    return fail(STB_EINVAL, "Check failed: frames must have fewer than 2^24 pixels");
+  STB_TRY(check_device_ptr(grad_loss, "grad_loss"));
+  STB_TRY(check_device_ptr(grad_tangent, "grad_tangent", true));
+  STB_TRY(check_device_ptr(grad_depth, "grad_depth", true));
+  if (grad_tangent) STB_TRY(check_device_ptr(tangent, "tangent"));
+  if (grad_depth) STB_TRY(check_device_ptr(depth_adjoint, "depth_adjoint"));
+  const int npix = height * width;
+  int bx = (npix / 4 + 255) / 256;
+  bx = bx < 1 ? 1 : (bx > 256 ? 256 : bx);
+  k_g_scale<<<dim3(bx, num_pairs), 256, 0, as_stream(stream)>>>(
+      grad_loss, tangent, depth_adjoint, npix, grad_tangent, grad_depth);
+  return check_launch("stb_icp_loss_scale_adjoint");
 }
 
 extern "C" int stb_icp_loss_backward(const float *src_depth, const float *src_normals,

@@ -79,6 +79,10 @@ _SIGNATURES = {
         _vp, _f64, _f64, _vp, _sz, _vp, _vp]),
     "stb_icp_loss_backward": (ctypes.c_int, [_vp] * 6 + [_i32] * 3 + [_f32] * 4 + [
         _vp, _vp, _vp, _sz, _vp, _vp, _vp]),
+    "stb_icp_loss_forward_adjoint": (ctypes.c_int, [_vp] * 6 + [_i32] * 3 + [_f32] * 4 + [
+        _vp, _f64, _f64, _vp, _sz, _vp, _vp, _vp, _vp]),
+    "stb_icp_loss_scale_adjoint": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp,
+                                                  _vp]),
     "stb_icp_estimate_static": (ctypes.c_int, [
         _vp, _vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _i32,
         _i32, _vp, _i32, _f64, _f64, _f64, _f64, _f64, _i32, _vp, _vp, _vp]),

@@ -2,18 +2,23 @@
 
 ``PointToPlaneLoss`` is a ``torch.autograd.Function`` over a batch of frame
 pairs: forward = the ICP association at ``exp(twist) @ pose`` and
-``L_p = sum r^2`` (``stb_icp_loss_forward``); backward = the adjoint kernel
-(``stb_icp_loss_backward``) giving dL/d(source depth) per pixel and the
-gradient with respect to the left perturbation of the pose, which
-``stb_se3_twist_grad`` maps through the SE(3) left Jacobian to dL/dtwist
-(twist ordered [translation; rotation]).  The correspondences of the forward
-pass are held fixed; source normals only gate the association and get no
-gradient.
+``L_p = sum r^2``; when the twist or the depth needs a gradient, the same
+pass also evaluates the hand-written adjoint at a unit output gradient
+(``stb_icp_loss_forward_adjoint``: dL_p/d(source depth) per pixel and the
+gradient with respect to the left perturbation of the pose), so backward
+only scales it by grad_loss (``stb_icp_loss_scale_adjoint``) and
+``stb_se3_twist_grad`` maps the pose part through the SE(3) left Jacobian to
+dL/dtwist (twist ordered [translation; rotation]).  Without gradients the
+forward is ``stb_icp_loss_forward`` alone; ``stb_icp_loss_backward`` is the
+same adjoint as a separate pass for callers of the C ABI.  The
+correspondences of the forward pass are held fixed; source normals only
+gate the association and get no gradient.
 
 The reference differentiates its registration through PyTorch ops and a
 custom matcher (``slamtb/registration/autogradicp.py:145-239``,
-``src/fpcl_matcher.cu:197-229``); here the whole loss and its adjoint are
-two kernels per direction for the batch, reading dense (B, H, W) arrays.
+``src/fpcl_matcher.cu:197-229``); here the loss and its adjoint are two kernels
+for the batch, reading dense (B, H, W) arrays, and the backward one
+elementwise kernel.
 """
 import torch
 
@@ -72,26 +77,39 @@ class PointToPlaneLoss(torch.autograd.Function):
         ws = torch.empty(need, dtype=torch.uint8, device=dev)
         loss = torch.empty(B, dtype=torch.float64, device=dev)
         k = tuple(float(x) for x in kcam)
+        want_twist, want_depth = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
         with torch.cuda.device(dev):
-            N.check(N.lib().stb_icp_loss_forward(
+            if not (want_twist or want_depth):
+                N.check(N.lib().stb_icp_loss_forward(
+                    *[N.ptr(t) for t in ins], B, H, W, *k, N.ptr(T),
+                    float(distance_threshold), float(normals_angle_thresh), N.ptr(ws), need,
+                    N.ptr(loss), N.stream_of(dev)))
+                return loss
+            # the adjoint at a unit output gradient in the same pass: the
+            # backward only scales it by grad_loss
+            tangent = torch.empty(B, 6, dtype=torch.float64, device=dev)
+            dadj = (torch.empty(B, H, W, dtype=torch.float32, device=dev)
+                    if want_depth else None)
+            N.check(N.lib().stb_icp_loss_forward_adjoint(
                 *[N.ptr(t) for t in ins], B, H, W, *k, N.ptr(T), float(distance_threshold),
-                float(normals_angle_thresh), N.ptr(ws), need, N.ptr(loss), N.stream_of(dev)))
-        ctx.keep = (ins, ws, T, tw, k)
+                float(normals_angle_thresh), N.ptr(ws), need, N.ptr(loss), N.ptr(tangent),
+                N.ptr(dadj), N.stream_of(dev)))
+        ctx.keep = (tw, tangent, dadj, B, H, W)
         return loss
 
     @staticmethod
     def backward(ctx, grad_loss):
-        ins, ws, T, tw, k = ctx.keep
-        B, H, W = ins[0].shape
-        dev = ws.device
+        tw, tangent, dadj, B, H, W = ctx.keep
+        dev = tangent.device
         g = grad_loss.detach().to(device=dev, dtype=torch.float64).contiguous()
         grad_tangent = torch.empty(B, 6, dtype=torch.float64, device=dev)
         grad_twist = torch.empty(B, 6, dtype=torch.float64, device=dev)
-        grad_depth = torch.empty(B, H, W, dtype=torch.float32, device=dev)
+        grad_depth = (torch.empty(B, H, W, dtype=torch.float32, device=dev)
+                      if dadj is not None else None)
         with torch.cuda.device(dev):
-            N.check(N.lib().stb_icp_loss_backward(
-                *[N.ptr(t) for t in ins], B, H, W, *k, N.ptr(T), N.ptr(g), N.ptr(ws),
-                ws.numel(), N.ptr(grad_tangent), N.ptr(grad_depth), N.stream_of(dev)))
+            N.check(N.lib().stb_icp_loss_scale_adjoint(
+                N.ptr(g), N.ptr(tangent), N.ptr(dadj), B, H, W, N.ptr(grad_tangent),
+                N.ptr(grad_depth), N.stream_of(dev)))
             N.check(N.lib().stb_se3_twist_grad(N.ptr(tw), N.ptr(grad_tangent),
                                                N.ptr(grad_twist), B, N.stream_of(dev)))
         return (grad_twist, grad_depth) + (None,) * 9

@@ -502,6 +502,42 @@ STB_API int stb_icp_loss_backward(const float *src_depth, const float *src_norma
                                   double *grad_tangent, float *grad_depth, void *stream);
 
 /*
+ * stb_icp_loss_forward with the adjoint at a unit output gradient computed
+ * in the same pass over the correspondences: loss[p] as stb_icp_loss_forward,
+ * tangent[p] = dL_p/de (device float64 [num_pairs][6]) and depth_adjoint
+ * [p][i] = dL_p/dz_i (device float32 [B][H][W], 0 where source pixel i has
+ * no correspondence; may be NULL), i.e. stb_icp_loss_backward's outputs at
+ * grad_loss = 1, bit for bit.  stb_icp_loss_scale_adjoint then gives the
+ * gradients for any grad_loss without reading the frames again.  Same
+ * counterpart as stb_icp_loss_forward (the reference's autograd ICP,
+ * slamtb/registration/autogradicp.py:145-239, differentiates through
+ * PyTorch ops).
+ */
+STB_API int stb_icp_loss_forward_adjoint(const float *src_depth, const float *src_normals,
+                                         const uint8_t *src_mask, const float *tgt_points,
+                                         const float *tgt_normals, const uint8_t *tgt_mask,
+                                         int32_t num_pairs, int32_t height, int32_t width,
+                                         float fx, float fy, float cx, float cy,
+                                         const double *poses, double distance_thresh,
+                                         double normal_angle_thresh, void *workspace,
+                                         size_t workspace_bytes, double *loss,
+                                         double *tangent, float *depth_adjoint,
+                                         void *stream);
+
+/*
+ * The gradients of stb_icp_loss_backward from stb_icp_loss_forward_adjoint's
+ * unit-gradient outputs: grad_tangent[p] = grad_loss[p] * tangent[p] (FP64)
+ * and grad_depth[p][i] = (float)grad_loss[p] * depth_adjoint[p][i].  Either
+ * output may be NULL (then its input may be NULL too).  Equal to
+ * stb_icp_loss_backward at grad_loss = 1; otherwise within float32 rounding
+ * of it (the product is rounded once more).
+ */
+STB_API int stb_icp_loss_scale_adjoint(const double *grad_loss, const double *tangent,
+                                       const float *depth_adjoint, int32_t num_pairs,
+                                       int32_t height, int32_t width, double *grad_tangent,
+                                       float *grad_depth, void *stream);
+
+/*
  * stb_icp_estimate without any allocation.  No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc while they track -- C or
  * FFI hosts with no CUDA allocator of their own, and applications that fix

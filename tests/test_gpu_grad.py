@@ -284,3 +284,95 @@ def test_full_size_32_pairs_640x480(cuda):
     fd = io.loss_twist_grad_fd(T0, np.zeros(6), d0["src"]["points"], m, h=1e-6)
     _, sc = io.loss_twist_grad64(T0, d0["src"]["points"], m)
     assert np.abs(gtw[0] - fd).max() <= 1e-5 * sc
+
+
+def _abi_args(cuda, pairs, poses):
+    """The dense C-ABI arguments of a batch (inputs, sizes, intrinsics, poses)."""
+    inp = _inputs(cuda, pairs)
+    ins = [inp[k].contiguous() for k in ("source_depth", "source_normals", "source_mask",
+                                         "target_points", "target_normals", "target_mask")]
+    ins[2], ins[5] = ins[2].to(torch.uint8), ins[5].to(torch.uint8)
+    B, H, W = ins[0].shape
+    return ins, (B, H, W), _kcam_params(pairs[0]["kcam"]), torch.from_numpy(poses).to(cuda)
+
+
+def test_fused_adjoint_equals_the_separate_adjoint(cuda, batch):
+    """stb_icp_loss_forward_adjoint (loss and adjoint in one pass) against
+    stb_icp_loss_forward + stb_icp_loss_backward on the same batch: the loss,
+    the tangent gradient and the depth gradient are the same bits at
+    grad_loss = 1.  After stb_icp_loss_scale_adjoint with other output
+    gradients (one of them 0), where the separate adjoint rounds g r in
+    float32 in every term and the scale multiplies the FP64 sum once: the
+    tangent gradient within 1e-6 of sum 2 |g| |J| |r|, and the depth gradient
+    within 2^-22 relative (four float32 roundings) of the separate
+    adjoint's."""
+    from slamtb_gb300 import _native as N
+    pairs, poses = batch
+    ins, (B, H, W), k, T = _abi_args(cuda, pairs, poses)
+    lib, st = N.lib(), N.stream_of(cuda)
+    need = int(lib.stb_icp_loss_workspace_bytes(B, H, W))
+    ws1 = torch.empty(need, dtype=torch.uint8, device=cuda)
+    ws2 = torch.empty(need, dtype=torch.uint8, device=cuda)
+    loss1 = torch.empty(B, dtype=torch.float64, device=cuda)
+    loss2 = torch.empty(B, dtype=torch.float64, device=cuda)
+    tangent = torch.empty(B, 6, dtype=torch.float64, device=cuda)
+    dadj = torch.full((B, H, W), float("nan"), dtype=torch.float32, device=cuda)
+    p = [N.ptr(x) for x in ins]
+    N.check(lib.stb_icp_loss_forward(*p, B, H, W, *k, N.ptr(T), DIST, ANGLE, N.ptr(ws1), need,
+                                     N.ptr(loss1), st))
+    N.check(lib.stb_icp_loss_forward_adjoint(*p, B, H, W, *k, N.ptr(T), DIST, ANGLE,
+                                             N.ptr(ws2), need, N.ptr(loss2), N.ptr(tangent),
+                                             N.ptr(dadj), st))
+    assert torch.equal(loss1, loss2)
+    for g in ([1.0] * B, [0.5, -3.0, 0.0][:B]):
+        gl = torch.tensor(g, dtype=torch.float64, device=cuda)
+        gt1 = torch.empty(B, 6, dtype=torch.float64, device=cuda)
+        gz1 = torch.empty(B, H, W, dtype=torch.float32, device=cuda)
+        N.check(lib.stb_icp_loss_backward(*p, B, H, W, *k, N.ptr(T), N.ptr(gl), N.ptr(ws1),
+                                          need, N.ptr(gt1), N.ptr(gz1), st))
+        gt2 = torch.empty(B, 6, dtype=torch.float64, device=cuda)
+        gz2 = torch.empty(B, H, W, dtype=torch.float32, device=cuda)
+        N.check(lib.stb_icp_loss_scale_adjoint(N.ptr(gl), N.ptr(tangent), N.ptr(dadj), B, H, W,
+                                               N.ptr(gt2), N.ptr(gz2), st))
+        a1, a2 = gt1.cpu().numpy(), gt2.cpu().numpy()
+        z1, z2 = gz1.cpu().numpy(), gz2.cpu().numpy()
+        if g[0] == 1.0:
+            np.testing.assert_array_equal(a1, a2)
+            np.testing.assert_array_equal(z1, z2)
+            assert np.count_nonzero(z2) > 1000
+            continue
+        for q in range(B):
+            _, m = _oracle(pairs[q], poses[q])
+            _, scale = io.loss_twist_grad64(poses[q], pairs[q]["src"]["points"], m)
+            assert np.abs(a1[q] - a2[q]).max() <= 1e-6 * abs(g[q]) * scale
+        np.testing.assert_allclose(z2, z1, rtol=2.0 ** -22, atol=0.0)
+    # only the tangent: a NULL depth adjoint and a NULL depth gradient
+    gt3 = torch.empty(B, 6, dtype=torch.float64, device=cuda)
+    N.check(lib.stb_icp_loss_forward_adjoint(*p, B, H, W, *k, N.ptr(T), DIST, ANGLE,
+                                             N.ptr(ws2), need, N.ptr(loss2), N.ptr(gt3), None,
+                                             st))
+    assert torch.equal(gt3, tangent)
+    N.check(lib.stb_icp_loss_scale_adjoint(N.ptr(torch.ones(B, dtype=torch.float64,
+                                                             device=cuda)),
+                                           N.ptr(gt3), None, B, H, W, N.ptr(gt2), None, st))
+    assert torch.equal(gt2, tangent)
+
+
+def test_loss_without_gradients_equals_the_fused_forward(cuda, batch):
+    """With no input needing a gradient the forward runs the loss alone
+    (stb_icp_loss_forward); its values are the fused forward's bits, and a
+    gradient only for the twist leaves the depth without one."""
+    from slamtb_gb300.registration import point_to_plane_loss
+    pairs, poses = batch
+    B = len(pairs)
+    kw = dict(kcam=_kcam_params(pairs[0]["kcam"]), poses=torch.from_numpy(poses).to(cuda),
+              distance_threshold=DIST, normals_angle_thresh=ANGLE, **_inputs(cuda, pairs))
+    with torch.no_grad():
+        plain = point_to_plane_loss(torch.zeros(B, 6, dtype=torch.float64, device=cuda), **kw)
+    tw = torch.zeros(B, 6, dtype=torch.float64, device=cuda, requires_grad=True)
+    fused = point_to_plane_loss(tw, **kw)
+    assert torch.equal(plain, fused.detach())
+    fused.sum().backward()
+    loss, gtw, _ = _run(cuda, pairs, poses)
+    np.testing.assert_array_equal(tw.grad.cpu().numpy(), gtw)
+    assert kw["source_depth"].grad is None
