@@ -593,18 +593,37 @@ def secondary_loss(device, seed, B=32):
         loss = point_to_plane_loss(twist, depth, sn, sm, tp, tn, tm, kcam, poses,
                                    DIST, ANGLE)
         loss.sum().backward()
-    for _ in range(3):
-        step()
+    # the same step with the loss captured once as CUDA graphs (forward and
+    # backward, torch.cuda.make_graphed_callables): the same kernels and
+    # bytes, without the host's per-step launch and autograd overhead, which
+    # otherwise sets the eager step's time
+    def loss_fn(tw, z):
+        return point_to_plane_loss(tw, z, sn, sm, tp, tn, tm, kcam, poses, DIST, ANGLE)
+
+    graphed = torch.cuda.make_graphed_callables(loss_fn, (twist, depth))
+
+    def gstep():
+        twist.grad = None
+        depth.grad = None
+        graphed(twist, depth).sum().backward()
+
     stream = torch.cuda.current_stream(device)
     reps = 50
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize(device)
-    a.record(stream)
-    for _ in range(reps):
-        step()
-    b.record(stream)
-    torch.cuda.synchronize(device)
-    t = a.elapsed_time(b) / 1e3 / reps
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize(device)
+        return a.elapsed_time(b) / 1e3 / reps
+
+    t_eager = timed(step)
+    t = timed(gstep)
     npx = B * H * W
     # forward: assoc 50 B/px (depth, normal, masks, target point+normal,
     # key) + key init 8 + the loss with its adjoint at a unit output
@@ -615,6 +634,9 @@ def secondary_loss(device, seed, B=32):
     return {"workload": f"point-to-plane loss forward + backward, {B} pairs 640x480 at the "
                         "poses of 5 GN iterations", "pairs": B,
             "pairs_per_s": B / t, "ms_per_step": t * 1e3,
+            "path": "PointToPlaneLoss under torch.cuda.make_graphed_callables (forward and "
+                    "backward graphs)",
+            "eager": {"pairs_per_s": B / t_eager, "ms_per_step": t_eager * 1e3},
             "launches_per_step": 8,
             "roofline": {"bound": "hbm", "alg_bytes_per_step": alg,
                          "achieved": alg / t / 1e9, "peak": peak, "peak_source": kind,
@@ -927,7 +949,8 @@ def summarize(sec):
                                   "median": _r(t["median"]),
                                   "within_1e-5": _r(t["within_1e-5"])} if t else None
         elif name == "loss_grad_32x640x480":
-            out[name] = {"pairs_per_s": _r(d["pairs_per_s"]), "frac": _r(d["roofline"]["frac"])}
+            out[name] = {"pairs_per_s": _r(d["pairs_per_s"]), "frac": _r(d["roofline"]["frac"]),
+                         "eager_pairs_per_s": _r(d["eager"]["pairs_per_s"])}
         elif name == "plain_kernels_larger_images":
             out[name] = {size: {launch: {"gn_iters_per_s": _r(c["gn_iters_per_s"]),
                                          **{k: _r(v["frac"]) for k, v in c.items()

@@ -376,3 +376,37 @@ def test_loss_without_gradients_equals_the_fused_forward(cuda, batch):
     loss, gtw, _ = _run(cuda, pairs, poses)
     np.testing.assert_array_equal(tw.grad.cpu().numpy(), gtw)
     assert kw["source_depth"].grad is None
+
+
+def test_graph_captured_loss_equals_eager(cuda, batch):
+    """PointToPlaneLoss captured as CUDA graphs (torch.cuda.make_graphed_
+    callables over twist and depth, as the benchmark runs it): two replays
+    at different twists give the eager call's loss and gradients bit for
+    bit."""
+    from slamtb_gb300.registration import point_to_plane_loss
+    pairs, poses = batch
+    B = len(pairs)
+    inp = _inputs(cuda, pairs)
+    depth = inp.pop("source_depth").clone().requires_grad_(True)
+    kw = dict(kcam=_kcam_params(pairs[0]["kcam"]), poses=torch.from_numpy(poses).to(cuda),
+              distance_threshold=DIST, normals_angle_thresh=ANGLE, **inp)
+
+    def fn(tw, z):
+        return point_to_plane_loss(tw, z, **kw)
+
+    tw = torch.zeros(B, 6, dtype=torch.float64, device=cuda, requires_grad=True)
+    graphed = torch.cuda.make_graphed_callables(fn, (tw, depth))
+    for scale in (0.0, 1e-3):
+        twist = torch.full((B, 6), scale, dtype=torch.float64, device=cuda)
+        t1 = twist.clone().requires_grad_(True)
+        z1 = depth.detach().clone().requires_grad_(True)
+        e = fn(t1, z1)
+        e.sum().backward()
+        t2 = twist.clone().requires_grad_(True)
+        z2 = depth.detach().clone().requires_grad_(True)
+        g = graphed(t2, z2)
+        g.sum().backward()
+        torch.cuda.synchronize(cuda)
+        assert torch.equal(e.detach(), g.detach())
+        assert torch.equal(t1.grad, t2.grad)
+        assert torch.equal(z1.grad, z2.grad)
