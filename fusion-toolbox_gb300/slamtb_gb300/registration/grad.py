@@ -20,21 +20,47 @@ custom matcher (``slamtb/registration/autogradicp.py:145-239``,
 for the batch, reading dense (B, H, W) arrays, and the backward one
 elementwise kernel.
 """
+import contextlib
+
 import torch
 
 from .. import _native as N
+
+
+def _on(dev):
+    """The device context for the library's calls, entered only when dev is
+    not already current (entering and leaving costs host time every step)."""
+    return (contextlib.nullcontext() if dev.index == torch.cuda.current_device()
+            else torch.cuda.device(dev))
+
+
+def _exp_compose(twist, base, stream):
+    """exp(twist) @ base into a new (B, 4, 4) tensor; twist float64
+    contiguous on the device, stream the caller's."""
+    base = base.detach().to(device=twist.device, dtype=torch.float64).contiguous()
+    out = torch.empty(twist.size(0), 4, 4, dtype=torch.float64, device=twist.device)
+    N.check(N.lib().stb_se3_exp_compose(N.ptr(twist), N.ptr(base), N.ptr(out), twist.size(0),
+                                        stream))
+    return out
 
 
 def se3_exp_compose(twist, base):
     """exp(twist) @ base for (B, 6) float64 twists and (B, 4, 4) poses, on
     the device in FP64."""
     twist = twist.detach().to(torch.float64).contiguous()
-    base = base.detach().to(device=twist.device, dtype=torch.float64).contiguous()
-    out = torch.empty(twist.size(0), 4, 4, dtype=torch.float64, device=twist.device)
-    with torch.cuda.device(twist.device):
-        N.check(N.lib().stb_se3_exp_compose(N.ptr(twist), N.ptr(base), N.ptr(out),
-                                            twist.size(0), N.stream_of(twist.device)))
-    return out
+    with _on(twist.device):
+        return _exp_compose(twist, base, N.stream_of(twist.device))
+
+
+_WS_BYTES = {}
+
+
+def _workspace_bytes(B, H, W):
+    key = (B, H, W)
+    n = _WS_BYTES.get(key)
+    if n is None:
+        n = _WS_BYTES[key] = int(N.lib().stb_icp_loss_workspace_bytes(B, H, W))
+    return n
 
 
 def _f32(name, t, shape):
@@ -72,18 +98,19 @@ class PointToPlaneLoss(torch.autograd.Function):
                _f32("target_normals", target_normals, (B, H, W, 3)),
                _mask("target_mask", target_mask, (B, H, W))]
         tw = twist.detach().to(device=dev, dtype=torch.float64).contiguous()
-        T = se3_exp_compose(tw, poses)
-        need = int(N.lib().stb_icp_loss_workspace_bytes(B, H, W))
+        need = _workspace_bytes(B, H, W)
         ws = torch.empty(need, dtype=torch.uint8, device=dev)
         loss = torch.empty(B, dtype=torch.float64, device=dev)
         k = tuple(float(x) for x in kcam)
         want_twist, want_depth = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
-        with torch.cuda.device(dev):
+        with _on(dev):
+            st = N.stream_of(dev)
+            T = _exp_compose(tw, poses, st)
             if not (want_twist or want_depth):
                 N.check(N.lib().stb_icp_loss_forward(
                     *[N.ptr(t) for t in ins], B, H, W, *k, N.ptr(T),
                     float(distance_threshold), float(normals_angle_thresh), N.ptr(ws), need,
-                    N.ptr(loss), N.stream_of(dev)))
+                    N.ptr(loss), st))
                 return loss
             # the adjoint at a unit output gradient in the same pass: the
             # backward only scales it by grad_loss
@@ -93,7 +120,7 @@ class PointToPlaneLoss(torch.autograd.Function):
             N.check(N.lib().stb_icp_loss_forward_adjoint(
                 *[N.ptr(t) for t in ins], B, H, W, *k, N.ptr(T), float(distance_threshold),
                 float(normals_angle_thresh), N.ptr(ws), need, N.ptr(loss), N.ptr(tangent),
-                N.ptr(dadj), N.stream_of(dev)))
+                N.ptr(dadj), st))
         ctx.keep = (tw, tangent, dadj, B, H, W)
         return loss
 
@@ -106,12 +133,13 @@ class PointToPlaneLoss(torch.autograd.Function):
         grad_twist = torch.empty(B, 6, dtype=torch.float64, device=dev)
         grad_depth = (torch.empty(B, H, W, dtype=torch.float32, device=dev)
                       if dadj is not None else None)
-        with torch.cuda.device(dev):
+        with _on(dev):
+            st = N.stream_of(dev)
             N.check(N.lib().stb_icp_loss_scale_adjoint(
                 N.ptr(g), N.ptr(tangent), N.ptr(dadj), B, H, W, N.ptr(grad_tangent),
-                N.ptr(grad_depth), N.stream_of(dev)))
+                N.ptr(grad_depth), st))
             N.check(N.lib().stb_se3_twist_grad(N.ptr(tw), N.ptr(grad_tangent),
-                                               N.ptr(grad_twist), B, N.stream_of(dev)))
+                                               N.ptr(grad_twist), B, st))
         return (grad_twist, grad_depth) + (None,) * 9
 
 
