@@ -61,6 +61,28 @@ inline int blocks_x(int64_t px) {
 
 inline size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Blocks per pair of the passes that fold per-pair sums (k_g_loss,
+// k_g_adjoint): about two waves of 4 blocks per SM over the whole batch,
+// at most blocks_x(npix); the grid-stride loop covers the rest, and the
+// slots of the workspace fit any grid up to blocks_x.  Every block folds
+// its partial sums and takes the pair's ticket at its end, so with few
+// pixels a block that fold sets the time (32 pairs of 640x480, graph-
+// captured step: 300 blocks a pair 94 k pairs/s, 38 a pair 105 k).  The
+// loss and both forms of the adjoint use the same grid, so their sums
+// agree bit for bit.
+int fold_blocks(int B, int64_t npix) {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms <= 0) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  const int want = (8 * sms + B - 1) / B;
+  const int cap = blocks_x(npix);
+  return want < 1 ? 1 : (want > cap ? cap : want);
+}
+
 inline GradLayout grad_layout(int B, int64_t px) {
   GradLayout g;
   size_t o = 0;
@@ -632,7 +654,8 @@ extern "C" int stb_icp_loss_forward(const float *src_depth, const float *src_nor
   const dim3 grid(blocks_x(npix), num_pairs);
   k_g_assoc<<<grid, kT, 0, st>>>(a, keys, distance_thresh_sq(distance_thresh),
                                  angle_cos_max(normal_angle_thresh));
-  k_g_loss<false><<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
+  const dim3 fgrid(fold_blocks(num_pairs, npix), num_pairs);
+  k_g_loss<false><<<fgrid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
                                        reinterpret_cast<unsigned *>(ws + g.tickets), loss,
                                        nullptr, nullptr);
   return check_launch("stb_icp_loss_forward");
@@ -664,7 +687,8 @@ extern "C" int stb_icp_loss_forward_adjoint(
   const dim3 grid(blocks_x(npix), num_pairs);
   k_g_assoc<<<grid, kT, 0, st>>>(a, keys, distance_thresh_sq(distance_thresh),
                                  angle_cos_max(normal_angle_thresh));
-  k_g_loss<true><<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
+  const dim3 fgrid(fold_blocks(num_pairs, npix), num_pairs);
+  k_g_loss<true><<<fgrid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
                                       reinterpret_cast<unsigned *>(ws + g.tickets), loss,
                                       tangent, depth_adjoint);
   return check_launch("stb_icp_loss_forward_adjoint");
@@ -713,8 +737,8 @@ extern "C" int stb_icp_loss_backward(const float *src_depth, const float *src_no
   char *ws = static_cast<char *>(workspace);
   const cudaStream_t st = as_stream(stream);
   if (grad_depth) cudaMemsetAsync(grad_depth, 0, sizeof(float) * (size_t)num_pairs * npix, st);
-  const dim3 grid(blocks_x(npix), num_pairs);
-  k_g_adjoint<<<grid, kT, 0, st>>>(a, reinterpret_cast<const unsigned long long *>(ws + g.keys),
+  const dim3 fgrid(fold_blocks(num_pairs, npix), num_pairs);
+  k_g_adjoint<<<fgrid, kT, 0, st>>>(a, reinterpret_cast<const unsigned long long *>(ws + g.keys),
                                    grad_loss, reinterpret_cast<float *>(ws + g.part),
                                    reinterpret_cast<unsigned *>(ws + g.tickets), grad_tangent,
                                    grad_depth);
