@@ -61,15 +61,16 @@ inline int blocks_x(int64_t px) {
 
 inline size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Blocks per pair of the passes that fold per-pair sums (k_g_loss,
-// k_g_adjoint): about two waves of 4 blocks per SM over the whole batch,
-// at most blocks_x(npix); the grid-stride loop covers the rest, and the
-// slots of the workspace fit any grid up to blocks_x.  Every block folds
-// its partial sums and takes the pair's ticket at its end, so with few
-// pixels a block that fold sets the time (32 pairs of 640x480, graph-
-// captured step: 300 blocks a pair 94 k pairs/s, 38 a pair 105 k).  The
-// loss and both forms of the adjoint use the same grid, so their sums
-// agree bit for bit.
+// Blocks per pair of the per-pixel loss passes: about two waves of 4
+// blocks per SM over the whole batch, at most blocks_x(npix); the grid-
+// stride loops cover the rest, and the slots of the workspace fit any grid
+// up to blocks_x.  A block of k_g_loss / k_g_adjoint ends with a per-pair
+// fold and ticket, and every block sets up its pair's float32 pose first,
+// so with few pixels a block those set the time (32 pairs of 640x480,
+// graph-captured step: 300 blocks a pair 94 k pairs/s; the folding passes
+// on 38 a pair 106 k; the association too 110 k).  The loss and both forms
+// of the adjoint use the same grid, so their sums agree bit for bit; the
+// association's key map does not depend on the grid.
 int fold_blocks(int B, int64_t npix) {
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -651,11 +652,10 @@ extern "C" int stb_icp_loss_forward(const float *src_depth, const float *src_nor
   unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + g.keys);
   cudaMemsetAsync(ws + g.tickets, 0, sizeof(unsigned) * (size_t)num_pairs, st);
   cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * (size_t)num_pairs * npix, st);
-  const dim3 grid(blocks_x(npix), num_pairs);
+  const dim3 grid(fold_blocks(num_pairs, npix), num_pairs);
   k_g_assoc<<<grid, kT, 0, st>>>(a, keys, distance_thresh_sq(distance_thresh),
                                  angle_cos_max(normal_angle_thresh));
-  const dim3 fgrid(fold_blocks(num_pairs, npix), num_pairs);
-  k_g_loss<false><<<fgrid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
+  k_g_loss<false><<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
                                        reinterpret_cast<unsigned *>(ws + g.tickets), loss,
                                        nullptr, nullptr);
   return check_launch("stb_icp_loss_forward");
@@ -684,11 +684,10 @@ extern "C" int stb_icp_loss_forward_adjoint(
   cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * (size_t)num_pairs * npix, st);
   if (depth_adjoint)
     cudaMemsetAsync(depth_adjoint, 0, sizeof(float) * (size_t)num_pairs * npix, st);
-  const dim3 grid(blocks_x(npix), num_pairs);
+  const dim3 grid(fold_blocks(num_pairs, npix), num_pairs);
   k_g_assoc<<<grid, kT, 0, st>>>(a, keys, distance_thresh_sq(distance_thresh),
                                  angle_cos_max(normal_angle_thresh));
-  const dim3 fgrid(fold_blocks(num_pairs, npix), num_pairs);
-  k_g_loss<true><<<fgrid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
+  k_g_loss<true><<<grid, kT, 0, st>>>(a, keys, reinterpret_cast<float *>(ws + g.part),
                                       reinterpret_cast<unsigned *>(ws + g.tickets), loss,
                                       tangent, depth_adjoint);
   return check_launch("stb_icp_loss_forward_adjoint");
