@@ -451,6 +451,8 @@ def _time_plain(ms, pyrs, reps):
 
 
 def _time_batch(br, plan, reps, device):
+    """Seconds per BatchRegistration.run (CUDA graph replay), best of reps
+    CUDA-event timings, as _time_plain takes the best of its passes."""
     import torch
     stream = torch.cuda.current_stream(device)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -461,7 +463,7 @@ def _time_batch(br, plan, reps, device):
         b.record(stream)
     torch.cuda.synchronize(device)
     ms = [a.elapsed_time(b) for a, b in ev]
-    return statistics.median(ms) / 1e3
+    return min(ms) / 1e3
 
 
 def _compare(batch_res, plain_T):
