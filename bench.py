@@ -389,7 +389,9 @@ def _error_table(transforms, outs):
             "median": statistics.median(vals) if vals else None,
             "within_1e-5": sum(1 for v in vals if v <= 1e-5) / max(len(vals), 1),
             "within_1e-3": sum(1 for v in vals if v <= 1e-3) / max(len(vals), 1),
-            "worst": [{"pair": k, "err": e, "cond_JtJ": c} for k, e, c in worst]}
+            "worst": [{"pair": k, "err": e, "cond_JtJ": c} for k, e, c in worst],
+            # every pair's error (None: both failed; inf: one of them failed)
+            "per_pair": [None if e is None else float(f"{e:.3g}") for _, e, _ in errs]}
 
 
 def _reference_arithmetic(jobs, outs, max_pairs):
