@@ -93,3 +93,27 @@ def test_port_multiscale_follows_the_oracle_hand_over():
     np.testing.assert_array_equal(p2["transform"], single["transform"])
     with pytest.raises(ValueError):
         port.multiscale_estimate(levels, [dict(e, channel_mode="sum") for e in ests])
+
+
+def test_bench_accuracy_tables_on_cpu():
+    """The benchmark's accuracy rows run without a GPU: the FP64 oracle's
+    free-running registrations (spawned processes), the error table of a set
+    of final poses against them (the oracle's own poses give 0 up to the
+    rounding of the rotation angle; a failed pair counts as infinite), and the port's registrations of the same jobs
+    (the reference CPU arithmetic), within 1e-3 of the motion here."""
+    import bench
+    jobs = []
+    for seed in (3, 4):
+        d = synthetic_pair(seed, width=160, height=120)
+        ests = [dict(num_iters=n, geom_weight=1.0, feat_weight=0.0, distance_threshold=0.1,
+                     normals_angle_thresh=math.radians(20)) for n in (3, 2)]
+        jobs.append((_levels(d, [1.0, 0.5]), ests, "last"))
+    outs = bench._oracle_runs(jobs, 1)
+    assert all(T is not None and np.isfinite(c) for T, c in outs)
+    own = bench._error_table([T for T, _ in outs], outs)
+    assert own["max"] < 1e-12 and own["within_1e-5"] == 1.0
+    assert all(e < 1e-12 for e in own["per_pair"])
+    failed = bench._error_table([outs[0][0], None], outs)
+    assert failed["per_pair"][1] == math.inf
+    ref = bench._reference_arithmetic(jobs, outs, 2)
+    assert ref["pairs"] == 2 and ref["max"] < 1e-3
